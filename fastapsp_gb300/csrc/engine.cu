@@ -1,0 +1,1161 @@
+// engine.cu -- the Fast-APSP engine behind the C ABI (include/fastapsp.h).
+//
+// Reference counterpart: fapGraph::run / solve / solveSubGraph
+// (fap/fap.cpp:195-545).  The reference allocates, copies and frees device
+// memory around every phase of every part and synchronizes after each kernel.
+// Here the engine keeps the graph, its metadata and all work buffers resident
+// on one GPU and runs each phase as one launch over a group of parts:
+//   SSSP (all boundary sources of the group) -> build (all part matrices) ->
+//   FW rounds (diagonal / panels / remaining tiles) -> min-plus -> decode.
+// FAP_MODE_PLAIN uses groups of one part in part order (the reference's host
+// loop); FAP_MODE_BATCHED uses one group of all parts and replays the launch
+// sequence from a CUDA graph that is captured once per (output, parts) key.
+//
+// All work tables (segments, jobs, batches) for one solve are built on the
+// host, uploaded once and kept with the plan, so a replay reads the same
+// device tables.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fap_internal.h"
+#include "kernels.cuh"
+#include "launch.h"
+
+using fapk::FwDiagJob;
+using fapk::MpSegment;
+using fapk::PartDesc;
+using fapk::SsspBatch;
+
+namespace fapi {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int status, const std::string &msg) {
+  g_last_error = msg;
+  return status;
+}
+void clear_error() { g_last_error.clear(); }
+const char *last_error() { return g_last_error.c_str(); }
+
+}  // namespace fapi
+
+using fapi::set_error;
+
+#define FAP_CUDA(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return set_error(e_ == cudaErrorMemoryAllocation ? FAP_ERR_NOMEM : FAP_ERR_CUDA, \
+                       std::string(#call) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+namespace {
+
+// Device buffer that only grows.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need) {
+    if (need <= bytes) return FAP_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, need);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return set_error(FAP_ERR_NOMEM, "cudaMalloc of " + std::to_string(need) + " bytes failed");
+    }
+    bytes = need;
+    return FAP_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// A fully prepared launch sequence for a list of part groups.
+struct Plan {
+  // key
+  int mode = -1;
+  void *dist = nullptr;
+  int32_t *pred = nullptr;
+  std::vector<int32_t> parts;
+  std::vector<int64_t> row_offs;
+  std::vector<const void *> sig;  // engine work buffers the tables point into
+  // device tables (one allocation)
+  DevBuf tables;
+  struct Group {
+    // SSSP
+    const SsspBatch *batches = nullptr;
+    int nbatches = 0;
+    // build / decode
+    const PartDesc *pdesc = nullptr;
+    const int64_t *row_begin = nullptr;
+    int nparts = 0;
+    int64_t total_rows = 0;
+    // FW: per round r, diag jobs [diag_off[r], +diag_cnt[r]) and segments
+    std::vector<const FwDiagJob *> diag;
+    std::vector<int> diag_cnt;
+    std::vector<const MpSegment *> panel;
+    std::vector<int> panel_nseg, panel_tiles;
+    std::vector<const MpSegment *> rest;
+    std::vector<int> rest_nseg, rest_tiles;
+    // min-plus
+    const MpSegment *mp = nullptr;
+    int mp_nseg = 0, mp_tiles = 0;
+  };
+  std::vector<Group> groups;
+  size_t fw_elems = 0;  // FW arena elements needed
+  // graph (batched mode)
+  cudaGraphExec_t exec = nullptr;
+  ~Plan() {
+    if (exec) cudaGraphExecDestroy(exec);
+    tables.release();
+  }
+};
+
+// Host-side table builder: appends POD records into one byte buffer and
+// remembers offsets, which become device pointers after the upload.
+struct TableBuilder {
+  std::vector<unsigned char> bytes;
+  template <typename T>
+  size_t add(const T *data, size_t count) {
+    size_t off = align_up(bytes.size(), 64);
+    bytes.resize(off + sizeof(T) * count);
+    if (count) std::memcpy(bytes.data() + off, data, sizeof(T) * count);
+    return off;
+  }
+};
+
+}  // namespace
+
+struct fap_engine {
+  int device = 0;
+  bool has_graph = false;
+  int dtype = FAP_DTYPE_F32;
+  int32_t n = 0;
+  int64_t m = 0;
+  int32_t K = 0;
+  int sm_count = 0;
+  std::vector<int32_t> ro, col, graph_id, st2ed, ed2st, ver_num, ver_offset, bdy_num, bdy_offset;
+  std::vector<float> w;
+  // device graph
+  int32_t *d_ro = nullptr, *d_col = nullptr, *d_iro = nullptr, *d_icol = nullptr;
+  int32_t *d_gid = nullptr, *d_st2ed = nullptr, *d_ed2st = nullptr;
+  void *d_w = nullptr, *d_iw = nullptr;
+  unsigned *d_status = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev_sync[2] = {};
+  // work buffers
+  DevBuf fw_d, fw_p;           // FW matrices arena
+  DevBuf sssp_scratch, sssp_stamps, sssp_epoch;
+  int sssp_slots_alloc = 0;
+  DevBuf res_d, res_p;         // device results when the caller passes host memory
+  DevBuf small;                // tables of standalone calls
+  std::vector<std::unique_ptr<Plan>> plans;
+  double times[5] = {0, 0, 0, 0, 0};
+  std::mutex mu;
+
+  bool f32() const { return dtype == FAP_DTYPE_F32; }
+};
+
+namespace {
+
+int max_sssp_slots(fap_engine *e) {
+  // Two 512-thread CTAs per SM, bounded by a 16 GiB scratch budget.
+  int slots = std::max(1, 2 * e->sm_count);
+  size_t per = fapk::sssp_slot_bytes(e->n) + (size_t)e->n * 4;
+  size_t budget = (size_t)16 << 30;
+  slots = (int)std::max<size_t>(1, std::min<size_t>((size_t)slots, budget / std::max<size_t>(per, 1)));
+  return slots;
+}
+
+int ensure_sssp_scratch(fap_engine *e, int slots) {
+  if (slots <= e->sssp_slots_alloc) return FAP_OK;
+  int st;
+  if ((st = e->sssp_scratch.ensure(fapk::sssp_slot_bytes(e->n) * slots)) != FAP_OK) return st;
+  if ((st = e->sssp_stamps.ensure((size_t)e->n * 4 * slots)) != FAP_OK) return st;
+  if ((st = e->sssp_epoch.ensure((size_t)4 * slots)) != FAP_OK) return st;
+  FAP_CUDA(cudaMemset(e->sssp_stamps.p, 0, (size_t)e->n * 4 * slots));
+  FAP_CUDA(cudaMemset(e->sssp_epoch.p, 0, (size_t)4 * slots));
+  e->sssp_slots_alloc = slots;
+  return FAP_OK;
+}
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes attr;
+  cudaError_t err = cudaPointerGetAttributes(&attr, p);
+  if (err != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+// FW segments of one matrix for pivot block r (row panel + column panel, and
+// the remaining tiles).  Matrices are size x size with leading dimension ld.
+void fw_segments(void *D, int32_t *P, int64_t ld, int size, int r, MpSegment &rowp,
+                 MpSegment &colp, MpSegment &rest, int &t_rowp, int &t_colp, int &t_rest,
+                 bool f32) {
+  const int B = fapk::fw_block();
+  const int nb = (size + B - 1) / B;
+  const size_t es = 4;
+  (void)f32;
+  MpSegment s{};
+  s.A = static_cast<const unsigned char *>(D) + (size_t)r * B * es;
+  s.lda = ld;
+  s.B = static_cast<const unsigned char *>(D) + (size_t)r * B * ld * es;
+  s.ldb = ld;
+  s.Bp = P ? P + (size_t)r * B * ld : nullptr;
+  s.ldbp = ld;
+  s.C = D;
+  s.ldc = ld;
+  s.Cp = P;
+  s.ldcp = ld;
+  s.M = size;
+  s.N = size;
+  s.K = std::min(B, size - r * B);
+  s.init_from_c = 1;
+  const int others = nb - 1;
+  const int pairs = (others + 1) / 2;
+  rowp = s;
+  rowp.row_skip = -1;
+  rowp.row_fix = r;
+  rowp.col_skip = r;
+  rowp.col_fix = -1;
+  rowp.tiles_x = pairs;
+  t_rowp = pairs;
+  colp = s;
+  colp.row_skip = r;
+  colp.row_fix = -1;
+  colp.col_skip = -1;
+  colp.col_fix = r;
+  colp.tiles_x = 1;
+  t_colp = pairs;
+  rest = s;
+  rest.row_skip = r;
+  rest.row_fix = -1;
+  rest.col_skip = r;
+  rest.col_fix = -1;
+  rest.tiles_x = pairs;
+  t_rest = pairs * pairs;
+}
+
+// Min-plus segment C = A (x) B (fresh C), tiled in 128x128.
+MpSegment mp_segment(const void *A, int64_t lda, const void *B, int64_t ldb, const int32_t *Bp,
+                     int64_t ldbp, void *C, int64_t ldc, int32_t *Cp, int64_t ldcp, int M, int N,
+                     int K, int &tiles) {
+  MpSegment s{};
+  s.A = A;
+  s.lda = lda;
+  s.B = B;
+  s.ldb = ldb;
+  s.Bp = Bp;
+  s.ldbp = ldbp;
+  s.C = C;
+  s.ldc = ldc;
+  s.Cp = Cp;
+  s.ldcp = ldcp;
+  s.M = M;
+  s.N = N;
+  s.K = K;
+  s.row_skip = s.col_skip = s.row_fix = s.col_fix = -1;
+  s.init_from_c = 0;
+  const int T = fapk::minplus_tile_rows();
+  s.tiles_x = (N + T - 1) / T;
+  tiles = ((M + T - 1) / T) * s.tiles_x;
+  return s;
+}
+
+// Builds the plan for `parts` (row offsets into dist/pred given per part),
+// grouped one part per group (plain) or all in one group (batched).
+int build_plan(fap_engine *e, Plan &pl) {
+  const bool batched = pl.mode == FAP_MODE_BATCHED;
+  const int B = fapk::fw_block();
+  const int64_t n = e->n;
+  std::vector<std::vector<int>> groups;
+  if (batched) {
+    groups.emplace_back();
+    for (size_t i = 0; i < pl.parts.size(); i++) groups[0].push_back((int)i);
+  } else {
+    for (size_t i = 0; i < pl.parts.size(); i++) groups.push_back({(int)i});
+  }
+  // FW arena layout: every part of the plan gets its own matrix.
+  std::vector<int64_t> mat_off(pl.parts.size());
+  std::vector<int32_t> ldv(pl.parts.size());
+  size_t arena = 0;
+  for (size_t i = 0; i < pl.parts.size(); i++) {
+    int p = pl.parts[i];
+    int sub = e->ver_num[p];
+    int ld = sub > 0 ? (int)align_up((size_t)sub, (size_t)B) : 0;
+    ldv[i] = ld;
+    mat_off[i] = (int64_t)arena;
+    arena += (size_t)ld * ld;
+  }
+  pl.fw_elems = arena;
+  char *fwd = static_cast<char *>(e->fw_d.p);
+  int32_t *fwp = static_cast<int32_t *>(e->fw_p.p);
+  const bool pred = pl.pred != nullptr;
+  char *dist = static_cast<char *>(pl.dist);
+
+  TableBuilder tb;
+  struct GroupOffs {
+    size_t batches, pdesc, row_begin, mp;
+    std::vector<size_t> diag, panel, rest;
+  };
+  std::vector<GroupOffs> goffs(groups.size());
+  pl.groups.assign(groups.size(), Plan::Group{});
+  for (size_t g = 0; g < groups.size(); g++) {
+    Plan::Group &G = pl.groups[g];
+    GroupOffs &O = goffs[g];
+    // SSSP batches: per part, its boundary vertices in mapping order.
+    std::vector<SsspBatch> batches;
+    std::vector<PartDesc> pdesc;
+    std::vector<int64_t> row_begin(1, 0);
+    std::vector<MpSegment> mps;
+    int mp_tiles = 0;
+    int maxnb = 0;
+    for (int idx : groups[g]) {
+      int p = pl.parts[idx];
+      int sub = e->ver_num[p], bdy = e->bdy_num[p], start = e->ver_offset[p];
+      int64_t roff = pl.row_offs[idx];
+      for (int b0 = 0; b0 < bdy; b0 += 32) {
+        SsspBatch sb{};
+        sb.count = std::min(32, bdy - b0);
+        for (int l = 0; l < sb.count; l++) {
+          sb.src[l] = e->st2ed[start + b0 + l];
+          sb.row_off[l] = roff + (int64_t)(b0 + l) * n;
+        }
+        batches.push_back(sb);
+      }
+      if (sub == 0) continue;
+      PartDesc d{};
+      d.sub = sub;
+      d.bdy = bdy;
+      d.start = start;
+      d.ld = ldv[idx];
+      d.mat_off = mat_off[idx];
+      d.row_off = roff;
+      pdesc.push_back(d);
+      row_begin.push_back(row_begin.back() + d.ld);
+      maxnb = std::max(maxnb, d.ld / B);
+      // min-plus for the inner rows
+      int inner = sub - bdy;
+      if (inner > 0) {
+        int tiles = 0;
+        const size_t es = 4;
+        MpSegment s = mp_segment(fwd + (size_t)(mat_off[idx] + (int64_t)bdy * d.ld) * es, d.ld,
+                                 dist + (size_t)roff * es, n, pred ? pl.pred + roff : nullptr, n,
+                                 dist + (size_t)(roff + (int64_t)bdy * n) * es, n,
+                                 pred ? pl.pred + roff + (int64_t)bdy * n : nullptr, n, inner,
+                                 (int)n, bdy, tiles);
+        s.tile_begin = mp_tiles;
+        mp_tiles += tiles;
+        mps.push_back(s);
+      }
+    }
+    G.nbatches = (int)batches.size();
+    O.batches = tb.add(batches.data(), batches.size());
+    G.nparts = (int)pdesc.size();
+    G.total_rows = row_begin.back();
+    O.pdesc = tb.add(pdesc.data(), pdesc.size());
+    O.row_begin = tb.add(row_begin.data(), row_begin.size());
+    G.mp_nseg = (int)mps.size();
+    G.mp_tiles = mp_tiles;
+    O.mp = tb.add(mps.data(), mps.size());
+    // FW rounds
+    G.diag_cnt.assign(maxnb, 0);
+    G.panel_nseg.assign(maxnb, 0);
+    G.panel_tiles.assign(maxnb, 0);
+    G.rest_nseg.assign(maxnb, 0);
+    G.rest_tiles.assign(maxnb, 0);
+    O.diag.assign(maxnb, 0);
+    O.panel.assign(maxnb, 0);
+    O.rest.assign(maxnb, 0);
+    for (int r = 0; r < maxnb; r++) {
+      std::vector<FwDiagJob> dj;
+      std::vector<MpSegment> ps, rs;
+      int pt = 0, rt = 0;
+      for (const PartDesc &d : pdesc) {
+        int nb = d.ld / B;
+        if (r >= nb) continue;
+        void *D = fwd + (size_t)d.mat_off * 4;
+        int32_t *P = pred ? fwp + d.mat_off : nullptr;
+        FwDiagJob j{};
+        j.D = D;
+        j.P = P;
+        j.ld = d.ld;
+        j.size = d.ld;
+        j.block = r;
+        dj.push_back(j);
+        if (nb > 1) {
+          MpSegment rp, cp, rest;
+          int a1, a2, a3;
+          fw_segments(D, P, d.ld, d.ld, r, rp, cp, rest, a1, a2, a3, e->f32());
+          rp.tile_begin = pt;
+          pt += a1;
+          ps.push_back(rp);
+          cp.tile_begin = pt;
+          pt += a2;
+          ps.push_back(cp);
+          rest.tile_begin = rt;
+          rt += a3;
+          rs.push_back(rest);
+        }
+      }
+      G.diag_cnt[r] = (int)dj.size();
+      O.diag[r] = tb.add(dj.data(), dj.size());
+      G.panel_nseg[r] = (int)ps.size();
+      G.panel_tiles[r] = pt;
+      O.panel[r] = tb.add(ps.data(), ps.size());
+      G.rest_nseg[r] = (int)rs.size();
+      G.rest_tiles[r] = rt;
+      O.rest[r] = tb.add(rs.data(), rs.size());
+    }
+  }
+  int st = pl.tables.ensure(std::max<size_t>(tb.bytes.size(), 64));
+  if (st != FAP_OK) return st;
+  FAP_CUDA(cudaMemcpy(pl.tables.p, tb.bytes.data(), tb.bytes.size(), cudaMemcpyHostToDevice));
+  unsigned char *base = static_cast<unsigned char *>(pl.tables.p);
+  for (size_t g = 0; g < groups.size(); g++) {
+    Plan::Group &G = pl.groups[g];
+    GroupOffs &O = goffs[g];
+    G.batches = reinterpret_cast<const SsspBatch *>(base + O.batches);
+    G.pdesc = reinterpret_cast<const PartDesc *>(base + O.pdesc);
+    G.row_begin = reinterpret_cast<const int64_t *>(base + O.row_begin);
+    G.mp = reinterpret_cast<const MpSegment *>(base + O.mp);
+    size_t R = O.diag.size();
+    G.diag.resize(R);
+    G.panel.resize(R);
+    G.rest.resize(R);
+    for (size_t r = 0; r < R; r++) {
+      G.diag[r] = reinterpret_cast<const FwDiagJob *>(base + O.diag[r]);
+      G.panel[r] = reinterpret_cast<const MpSegment *>(base + O.panel[r]);
+      G.rest[r] = reinterpret_cast<const MpSegment *>(base + O.rest[r]);
+    }
+  }
+  return FAP_OK;
+}
+
+fapk::BuildArgs build_args(fap_engine *e, const Plan &pl, const Plan::Group &G) {
+  fapk::BuildArgs a{};
+  a.n = e->n;
+  a.ro = e->d_ro;
+  a.col = e->d_col;
+  a.w = e->d_w;
+  a.graph_id = e->d_gid;
+  a.st2ed = e->d_st2ed;
+  a.ed2st = e->d_ed2st;
+  a.parts = G.pdesc;
+  a.row_begin = G.row_begin;
+  a.nparts = G.nparts;
+  a.total_rows = G.total_rows;
+  a.mat = e->fw_d.p;
+  a.matp = pl.pred ? static_cast<int32_t *>(e->fw_p.p) : nullptr;
+  a.rows = pl.dist;
+  a.rowsp = pl.pred;
+  a.ldr = e->n;
+  return a;
+}
+
+// Issues the launch sequence of a plan on `st`.  Events ev[0..5] bracket the
+// phases of the whole plan (recorded on the first/last group).
+int issue_plan(fap_engine *e, Plan &pl, cudaStream_t st, bool record_events) {
+  const bool f32 = e->f32();
+  const bool pred = pl.pred != nullptr;
+  for (size_t g = 0; g < pl.groups.size(); g++) {
+    Plan::Group &G = pl.groups[g];
+    if (record_events && g == 0) FAP_CUDA(cudaEventRecord(e->ev[0], st));
+    fapk::SsspArgs sa{};
+    sa.n = e->n;
+    sa.ro = e->d_ro;
+    sa.col = e->d_col;
+    sa.w = e->d_w;
+    sa.iro = e->d_iro;
+    sa.icol = e->d_icol;
+    sa.iw = e->d_iw;
+    sa.batches = G.batches;
+    sa.nbatches = G.nbatches;
+    sa.dist = pl.dist;
+    sa.pred = pl.pred;
+    sa.scratch = e->sssp_scratch.p;
+    sa.slots = std::min(G.nbatches, e->sssp_slots_alloc);
+    sa.stamps = static_cast<int32_t *>(e->sssp_stamps.p);
+    sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
+    sa.status = e->d_status;
+    sa.iter_cap = 2 * e->n + 8;
+    FAP_CUDA(fapk::launch_sssp(f32, sa, st));
+    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[1], st));
+    fapk::BuildArgs ba = build_args(e, pl, G);
+    FAP_CUDA(fapk::launch_build(f32, pred, ba, st));
+    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[2], st));
+    for (size_t r = 0; r < G.diag.size(); r++) {
+      FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], st));
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], st));
+    }
+    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[3], st));
+    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, st));
+    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[4], st));
+    FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, st));
+    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[5], st));
+  }
+  return FAP_OK;
+}
+
+int check_status(fap_engine *e) {
+  unsigned h = 0;
+  FAP_CUDA(cudaMemcpy(&h, e->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (h) {
+    FAP_CUDA(cudaMemset(e->d_status, 0, sizeof(unsigned)));
+    if (h & fapk::kErrSsspCap) return set_error(FAP_ERR_NOT_CONVERGED, "SSSP reached its iteration cap");
+    return set_error(FAP_ERR_INVALID, "a kernel saw an out-of-range index");
+  }
+  return FAP_OK;
+}
+
+std::vector<const void *> buffer_signature(const fap_engine *e) {
+  return {e->fw_d.p, e->fw_p.p, e->sssp_scratch.p, e->sssp_stamps.p, e->sssp_epoch.p,
+          reinterpret_cast<const void *>((intptr_t)e->sssp_slots_alloc)};
+}
+
+Plan *find_plan(fap_engine *e, int mode, void *dist, int32_t *pred,
+                const std::vector<int32_t> &parts, const std::vector<int64_t> &offs) {
+  const std::vector<const void *> sig = buffer_signature(e);
+  for (auto &p : e->plans)
+    if (p->mode == mode && p->dist == dist && p->pred == pred && p->parts == parts &&
+        p->row_offs == offs && p->sig == sig)
+      return p.get();
+  return nullptr;
+}
+
+// Runs `parts` (row offsets `offs` into the device buffers dist/pred).
+int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vector<int32_t> &parts,
+              const std::vector<int64_t> &offs, cudaStream_t st) {
+  int rc;
+  // work buffers
+  size_t fw_elems = 0;
+  int max_batches = 0;
+  for (int p : parts) {
+    size_t ld = align_up((size_t)e->ver_num[p], (size_t)fapk::fw_block());
+    fw_elems += ld * ld;
+    max_batches += (e->bdy_num[p] + 31) / 32;
+  }
+  if ((rc = e->fw_d.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
+  if (pred && (rc = e->fw_p.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
+  int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e));
+  if ((rc = ensure_sssp_scratch(e, slots)) != FAP_OK) return rc;
+
+  Plan *pl = find_plan(e, mode, dist, pred, parts, offs);
+  if (!pl) {
+    if (e->plans.size() >= 8) e->plans.erase(e->plans.begin());
+    auto np = std::make_unique<Plan>();
+    np->mode = mode;
+    np->dist = dist;
+    np->pred = pred;
+    np->parts = parts;
+    np->row_offs = offs;
+    np->sig = buffer_signature(e);
+    if ((rc = build_plan(e, *np)) != FAP_OK) return rc;
+    e->plans.push_back(std::move(np));
+    pl = e->plans.back().get();
+  }
+  if (mode == FAP_MODE_BATCHED) {
+    if (!pl->exec) {
+      cudaGraph_t graph = nullptr;
+      cudaStream_t cap = e->stream;
+      FAP_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+      int irc = issue_plan(e, *pl, cap, true);
+      cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+      if (irc != FAP_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return irc;
+      }
+      if (ce != cudaSuccess) return set_error(FAP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&pl->exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        pl->exec = nullptr;
+        return set_error(FAP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+      }
+    }
+    if (st != e->stream) {
+      FAP_CUDA(cudaEventRecord(e->ev_sync[0], st));
+      FAP_CUDA(cudaStreamWaitEvent(e->stream, e->ev_sync[0], 0));
+    }
+    FAP_CUDA(cudaGraphLaunch(pl->exec, e->stream));
+    if (st != e->stream) {
+      FAP_CUDA(cudaEventRecord(e->ev_sync[1], e->stream));
+      FAP_CUDA(cudaStreamWaitEvent(st, e->ev_sync[1], 0));
+    }
+  } else {
+    if ((rc = issue_plan(e, *pl, st, true)) != FAP_OK) return rc;
+  }
+  return FAP_OK;
+}
+
+void read_times(fap_engine *e) {
+  float t[5] = {0, 0, 0, 0, 0};
+  cudaEventElapsedTime(&t[0], e->ev[0], e->ev[1]);  // sssp
+  float b = 0, f = 0, mp = 0, dc = 0;
+  cudaEventElapsedTime(&b, e->ev[1], e->ev[2]);
+  cudaEventElapsedTime(&f, e->ev[2], e->ev[3]);
+  cudaEventElapsedTime(&mp, e->ev[3], e->ev[4]);
+  cudaEventElapsedTime(&dc, e->ev[4], e->ev[5]);
+  float tot = 0;
+  cudaEventElapsedTime(&tot, e->ev[0], e->ev[5]);
+  (void)cudaGetLastError();
+  e->times[0] = t[0];
+  e->times[1] = f;
+  e->times[2] = mp;
+  e->times[3] = b + dc;
+  e->times[4] = tot;
+}
+
+cudaStream_t pick_stream(fap_engine *e, void *stream) {
+  return stream ? static_cast<cudaStream_t>(stream) : e->stream;
+}
+
+int init_device(fap_engine *e, int device) {
+  int count = 0;
+  cudaError_t ce = cudaGetDeviceCount(&count);
+  if (ce != cudaSuccess || count == 0) {
+    (void)cudaGetLastError();
+    return set_error(FAP_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (device < 0 || device >= count) return set_error(FAP_ERR_INVALID, "device ordinal out of range");
+  FAP_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  FAP_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) return set_error(FAP_ERR_NO_DEVICE, "the engine is built for sm_103a (Blackwell Ultra) only");
+  e->device = device;
+  e->sm_count = prop.multiProcessorCount;
+  FAP_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  for (auto &ev : e->ev) FAP_CUDA(cudaEventCreate(&ev));
+  for (auto &ev : e->ev_sync) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  FAP_CUDA(cudaMalloc(&e->d_status, sizeof(unsigned)));
+  FAP_CUDA(cudaMemset(e->d_status, 0, sizeof(unsigned)));
+  FAP_CUDA(fapk::init_minplus_kernels());
+  return FAP_OK;
+}
+
+template <typename T>
+int upload(T **dst, const T *src, size_t count) {
+  FAP_CUDA(cudaMalloc((void **)dst, std::max<size_t>(count, 1) * sizeof(T)));
+  if (count) FAP_CUDA(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  return FAP_OK;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+// ============================ C ABI ========================================
+extern "C" {
+
+const char *fap_version(void) { return "fastapsp-gb300 0.1 (sm_103a)"; }
+
+const char *fap_status_string(int status) {
+  switch (status) {
+    case FAP_OK: return "ok";
+    case FAP_ERR_INVALID: return "invalid argument";
+    case FAP_ERR_CUDA: return "CUDA error";
+    case FAP_ERR_NOMEM: return "out of memory";
+    case FAP_ERR_STATE: return "invalid state";
+    case FAP_ERR_NOT_CONVERGED: return "SSSP did not converge";
+    case FAP_ERR_IO: return "I/O error";
+    case FAP_ERR_NO_DEVICE: return "no suitable CUDA device";
+    case FAP_ERR_RANGE: return "value out of range";
+    default: return "unknown status";
+  }
+}
+
+const char *fap_last_error(void) { return fapi::last_error(); }
+
+int fap_device_count(int32_t *count) {
+  if (!count) return set_error(FAP_ERR_INVALID, "null count");
+  int c = 0;
+  if (cudaGetDeviceCount(&c) != cudaSuccess) {
+    (void)cudaGetLastError();
+    c = 0;
+  }
+  *count = c;
+  return FAP_OK;
+}
+
+int fap_mtx_counts(const char *path, int32_t directed, int32_t weighted, int32_t *n, int64_t *m) {
+  (void)weighted;
+  if (!path || !n || !m) return set_error(FAP_ERR_INVALID, "null argument");
+  return fapi::mtx_counts(path, directed != 0, n, m);
+}
+
+int fap_mtx_read(const char *path, int32_t directed, int32_t weighted, int32_t n, int64_t m,
+                 int32_t *adj_size, int32_t *row_offset, int32_t *col_val, float *weight) {
+  if (!path || !adj_size || !row_offset || (m > 0 && (!col_val || !weight)))
+    return set_error(FAP_ERR_INVALID, "null argument");
+  return fapi::mtx_read(path, directed != 0, weighted != 0, n, m, adj_size, row_offset, col_val,
+                        weight);
+}
+
+int fap_partition(int32_t n, const int32_t *row_offset, const int32_t *col_val, int32_t K,
+                  uint64_t seed, int32_t *graph_id, int64_t *edge_cut) {
+  if (!row_offset || !graph_id || (n > 0 && !col_val && row_offset[n] > 0))
+    return set_error(FAP_ERR_INVALID, "null argument");
+  return fapi::partition(n, row_offset, col_val, K, seed, graph_id, edge_cut);
+}
+
+int fap_preprocess(int32_t K, int32_t n, const int32_t *graph_id, const int32_t *row_offset,
+                   const int32_t *col_val, int32_t *st2ed, int32_t *ed2st, int32_t *ver_num,
+                   int32_t *ver_offset, int32_t *bdy_num, int32_t *bdy_offset) {
+  if (!graph_id || !row_offset || !st2ed || !ed2st || !ver_num || !ver_offset || !bdy_num ||
+      !bdy_offset)
+    return set_error(FAP_ERR_INVALID, "null argument");
+  return fapi::preprocess(K, n, graph_id, row_offset, col_val, st2ed, ed2st, ver_num, ver_offset,
+                          bdy_num, bdy_offset, nullptr);
+}
+
+int fap_create_context(int32_t device, fap_engine **out) {
+  if (!out) return set_error(FAP_ERR_INVALID, "null out");
+  *out = nullptr;
+  auto e = std::make_unique<fap_engine>();
+  int rc = init_device(e.get(), device);
+  if (rc != FAP_OK) {
+    fap_destroy(e.release());
+    return rc;
+  }
+  *out = e.release();
+  return FAP_OK;
+}
+
+int fap_create(int32_t n, int64_t m, const int32_t *row_offset, const int32_t *col_val,
+               const float *weight, int32_t K, const int32_t *graph_id, int32_t dtype,
+               int32_t device, fap_engine **out) {
+  if (!out) return set_error(FAP_ERR_INVALID, "null out");
+  *out = nullptr;
+  if (n < 0 || m < 0 || K < 1 || !row_offset || (m > 0 && (!col_val || !weight)))
+    return set_error(FAP_ERR_INVALID, "fap_create: bad graph arguments");
+  if (dtype != FAP_DTYPE_F32 && dtype != FAP_DTYPE_I32)
+    return set_error(FAP_ERR_INVALID, "fap_create: unknown dtype");
+  if (row_offset[0] != 0 || (int64_t)row_offset[n] != m)
+    return set_error(FAP_ERR_INVALID, "fap_create: row_offset must start at 0 and end at m");
+  for (int32_t i = 0; i < n; i++)
+    if (row_offset[i + 1] < row_offset[i]) return set_error(FAP_ERR_INVALID, "fap_create: row_offset not monotone");
+  float wmax = 0.0f;
+  for (int64_t j = 0; j < m; j++) {
+    if (col_val[j] < 0 || col_val[j] >= n) return set_error(FAP_ERR_INVALID, "fap_create: column id out of range");
+    float wj = weight[j];
+    if (!(wj >= 0.0f) || std::isinf(wj)) return set_error(FAP_ERR_RANGE, "fap_create: weights must be finite and >= 0");
+    if (dtype == FAP_DTYPE_I32 && wj != std::floor(wj))
+      return set_error(FAP_ERR_RANGE, "fap_create: int32 mode needs integer weights");
+    wmax = std::max(wmax, wj);
+  }
+  if (dtype == FAP_DTYPE_I32 && (double)wmax * std::max<int64_t>(n - 1, 1) >= (double)FAP_INF_I32)
+    return set_error(FAP_ERR_RANGE, "fap_create: (n-1) * max weight must stay below 2^30 in int32 mode");
+
+  auto e = std::make_unique<fap_engine>();
+  e->n = n;
+  e->m = m;
+  e->K = K;
+  e->dtype = dtype;
+  e->ro.assign(row_offset, row_offset + n + 1);
+  e->col.assign(col_val, col_val + m);
+  e->w.assign(weight, weight + m);
+  e->graph_id.resize(n);
+  int rc;
+  if (graph_id) {
+    for (int32_t i = 0; i < n; i++) {
+      if (graph_id[i] < 1 || graph_id[i] > K) return set_error(FAP_ERR_INVALID, "fap_create: part id outside 1..K");
+      e->graph_id[i] = graph_id[i];
+    }
+  } else {
+    if ((rc = fapi::partition(n, row_offset, col_val, K, 1, e->graph_id.data(), nullptr)) != FAP_OK) return rc;
+  }
+  e->st2ed.resize(n);
+  e->ed2st.resize(n);
+  e->ver_num.resize(K + 1);
+  e->ver_offset.resize(K + 1);
+  e->bdy_num.resize(K + 1);
+  e->bdy_offset.resize(K + 1);
+  if ((rc = fapi::preprocess(K, n, e->graph_id.data(), row_offset, col_val, e->st2ed.data(),
+                             e->ed2st.data(), e->ver_num.data(), e->ver_offset.data(),
+                             e->bdy_num.data(), e->bdy_offset.data(), nullptr)) != FAP_OK)
+    return rc;
+  if ((rc = init_device(e.get(), device)) != FAP_OK) {
+    fap_destroy(e.release());
+    return rc;
+  }
+  // in-edge CSR (counting sort by destination, sources ascending)
+  std::vector<int32_t> iro(n + 1, 0), icol(m);
+  std::vector<float> iw(m);
+  for (int64_t j = 0; j < m; j++) iro[col_val[j] + 1]++;
+  for (int32_t i = 0; i < n; i++) iro[i + 1] += iro[i];
+  {
+    std::vector<int32_t> fill(iro.begin(), iro.end() - 1);
+    for (int32_t u = 0; u < n; u++)
+      for (int32_t j = row_offset[u]; j < row_offset[u + 1]; j++) {
+        int32_t pos = fill[col_val[j]]++;
+        icol[pos] = u;
+        iw[pos] = weight[j];
+      }
+  }
+  std::vector<uint32_t> wbits(m), iwbits(m);
+  for (int64_t j = 0; j < m; j++) {
+    if (dtype == FAP_DTYPE_F32) {
+      std::memcpy(&wbits[j], &weight[j], 4);
+      std::memcpy(&iwbits[j], &iw[j], 4);
+    } else {
+      wbits[j] = (uint32_t)weight[j];
+      iwbits[j] = (uint32_t)iw[j];
+    }
+  }
+  fap_engine *E = e.get();
+  if ((rc = upload(&E->d_ro, row_offset, (size_t)n + 1)) != FAP_OK ||
+      (rc = upload(&E->d_col, col_val, (size_t)m)) != FAP_OK ||
+      (rc = upload(&E->d_iro, iro.data(), (size_t)n + 1)) != FAP_OK ||
+      (rc = upload(&E->d_icol, icol.data(), (size_t)m)) != FAP_OK ||
+      (rc = upload(&E->d_gid, E->graph_id.data(), (size_t)n)) != FAP_OK ||
+      (rc = upload(&E->d_st2ed, E->st2ed.data(), (size_t)n)) != FAP_OK ||
+      (rc = upload(&E->d_ed2st, E->ed2st.data(), (size_t)n)) != FAP_OK ||
+      (rc = upload((uint32_t **)&E->d_w, wbits.data(), (size_t)m)) != FAP_OK ||
+      (rc = upload((uint32_t **)&E->d_iw, iwbits.data(), (size_t)m)) != FAP_OK) {
+    fap_destroy(e.release());
+    return rc;
+  }
+  E->has_graph = true;
+  *out = e.release();
+  return FAP_OK;
+}
+
+int fap_destroy(fap_engine *e) {
+  if (!e) return FAP_OK;
+  {
+    DeviceGuard g(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    e->plans.clear();
+    e->fw_d.release();
+    e->fw_p.release();
+    e->sssp_scratch.release();
+    e->sssp_stamps.release();
+    e->sssp_epoch.release();
+    e->res_d.release();
+    e->res_p.release();
+    e->small.release();
+    void *ptrs[] = {e->d_ro, e->d_col, e->d_iro, e->d_icol, e->d_gid, e->d_st2ed, e->d_ed2st,
+                    e->d_w, e->d_iw, e->d_status};
+    for (void *p : ptrs)
+      if (p) cudaFree(p);
+    for (auto &ev : e->ev)
+      if (ev) cudaEventDestroy(ev);
+    for (auto &ev : e->ev_sync)
+      if (ev) cudaEventDestroy(ev);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    (void)cudaGetLastError();
+  }
+  delete e;
+  return FAP_OK;
+}
+
+int fap_num_vertices(const fap_engine *e, int32_t *n, int32_t *K) {
+  if (!e || !n || !K) return set_error(FAP_ERR_INVALID, "null argument");
+  *n = e->n;
+  *K = e->K;
+  return FAP_OK;
+}
+
+int fap_mapping(const fap_engine *e, int32_t *st2ed) {
+  if (!e || !st2ed) return set_error(FAP_ERR_INVALID, "null argument");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  std::copy(e->st2ed.begin(), e->st2ed.end(), st2ed);
+  return FAP_OK;
+}
+
+int fap_graph_id(const fap_engine *e, int32_t *graph_id) {
+  if (!e || !graph_id) return set_error(FAP_ERR_INVALID, "null argument");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  std::copy(e->graph_id.begin(), e->graph_id.end(), graph_id);
+  return FAP_OK;
+}
+
+int fap_part_info(const fap_engine *e, int32_t part, int32_t *sub, int32_t *bdy, int32_t *offset) {
+  if (!e) return set_error(FAP_ERR_INVALID, "null engine");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  if (part < 1 || part > e->K) return set_error(FAP_ERR_INVALID, "part id outside 1..K");
+  if (sub) *sub = e->ver_num[part];
+  if (bdy) *bdy = e->bdy_num[part];
+  if (offset) *offset = e->ver_offset[part];
+  return FAP_OK;
+}
+
+static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_t rows, void *dist,
+                        int32_t *pred, int mode, void *stream) {
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard g(e->device);
+  fapi::clear_error();
+  cudaStream_t st = pick_stream(e, stream);
+  const size_t bytes = (size_t)rows * e->n * 4;
+  const bool dev_d = is_device_ptr(dist);
+  const bool dev_p = pred == nullptr || is_device_ptr(pred);
+  void *dd = dist;
+  int32_t *dp = pred;
+  int rc;
+  if (!dev_d) {
+    if ((rc = e->res_d.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
+    dd = e->res_d.p;
+  }
+  if (pred && !dev_p) {
+    if ((rc = e->res_p.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
+    dp = static_cast<int32_t *>(e->res_p.p);
+  }
+  std::vector<int64_t> offs;
+  int64_t acc = 0;
+  for (int32_t p : parts) {
+    offs.push_back(acc * e->n);
+    acc += e->ver_num[p];
+  }
+  if ((rc = run_parts(e, mode, dd, dp, parts, offs, st)) != FAP_OK) return rc;
+  if (!dev_d) FAP_CUDA(cudaMemcpyAsync(dist, dd, bytes, cudaMemcpyDeviceToHost, st));
+  if (pred && !dev_p) FAP_CUDA(cudaMemcpyAsync(pred, dp, bytes, cudaMemcpyDeviceToHost, st));
+  FAP_CUDA(cudaStreamSynchronize(st));
+  if (mode == FAP_MODE_BATCHED && st != e->stream) FAP_CUDA(cudaStreamSynchronize(e->stream));
+  read_times(e);
+  return check_status(e);
+}
+
+int fap_solve_part(fap_engine *e, int32_t part, void *dist, int32_t *pred, void *stream) {
+  if (!e || !dist) return set_error(FAP_ERR_INVALID, "null argument");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  if (part < 1 || part > e->K) return set_error(FAP_ERR_INVALID, "part id outside 1..K");
+  return solve_common(e, {part}, e->ver_num[part], dist, pred, FAP_MODE_PLAIN, stream);
+}
+
+int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode, void *stream) {
+  if (!e || !dist) return set_error(FAP_ERR_INVALID, "null argument");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  if (mode != FAP_MODE_PLAIN && mode != FAP_MODE_BATCHED) return set_error(FAP_ERR_INVALID, "unknown mode");
+  std::vector<int32_t> parts;
+  for (int32_t p = 1; p <= e->K; p++) parts.push_back(p);
+  return solve_common(e, parts, e->n, dist, pred, mode, stream);
+}
+
+int fap_last_times(const fap_engine *e, double *times5) {
+  if (!e || !times5) return set_error(FAP_ERR_INVALID, "null argument");
+  for (int i = 0; i < 5; i++) times5[i] = e->times[i];
+  return FAP_OK;
+}
+
+int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, const void *A,
+                int64_t lda, const void *B, int64_t ldb, const int32_t *Bpath, int64_t ldbp,
+                void *C, int64_t ldc, int32_t *Cpath, int64_t ldcp, void *stream) {
+  if (!e || M < 0 || N < 0 || K < 0 || !C || (K > 0 && (!A || !B)))
+    return set_error(FAP_ERR_INVALID, "fap_minplus: bad arguments");
+  if (dtype != FAP_DTYPE_F32 && dtype != FAP_DTYPE_I32) return set_error(FAP_ERR_INVALID, "unknown dtype");
+  if ((Bpath == nullptr) != (Cpath == nullptr)) return set_error(FAP_ERR_INVALID, "Bpath and Cpath go together");
+  if (lda < K || ldb < N || ldc < N || (Bpath && (ldbp < N || ldcp < N)))
+    return set_error(FAP_ERR_INVALID, "leading dimension too small");
+  if (M == 0 || N == 0) return FAP_OK;
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard g(e->device);
+  cudaStream_t st = pick_stream(e, stream);
+  int tiles = 0;
+  MpSegment s = mp_segment(A, lda, B, ldb, Bpath, ldbp, C, ldc, Cpath, ldcp, M, N, K, tiles);
+  s.tile_begin = 0;
+  int rc;
+  if ((rc = e->small.ensure(sizeof(MpSegment))) != FAP_OK) return rc;
+  FAP_CUDA(cudaMemcpyAsync(e->small.p, &s, sizeof(s), cudaMemcpyHostToDevice, st));
+  FAP_CUDA(fapk::launch_minplus_tiles(dtype == FAP_DTYPE_F32, Bpath != nullptr,
+                                      static_cast<const MpSegment *>(e->small.p), 1, tiles, st));
+  FAP_CUDA(cudaStreamSynchronize(st));
+  return FAP_OK;
+}
+
+int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t *sizes,
+                      void *const *D, const int64_t *ld, int32_t *const *P, void *stream) {
+  if (!e || count < 0 || (count > 0 && (!sizes || !D || !ld)))
+    return set_error(FAP_ERR_INVALID, "fap_floyd_batched: bad arguments");
+  if (dtype != FAP_DTYPE_F32 && dtype != FAP_DTYPE_I32) return set_error(FAP_ERR_INVALID, "unknown dtype");
+  const bool pred = P != nullptr;
+  const int Bk = fapk::fw_block();
+  int maxnb = 0;
+  for (int32_t b = 0; b < count; b++) {
+    if (sizes[b] < 0 || ld[b] < sizes[b] || (sizes[b] > 0 && !D[b]) || (pred && sizes[b] > 0 && !P[b]))
+      return set_error(FAP_ERR_INVALID, "fap_floyd_batched: bad matrix " + std::to_string(b));
+    maxnb = std::max(maxnb, (sizes[b] + Bk - 1) / Bk);
+  }
+  if (count == 0 || maxnb == 0) return FAP_OK;
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard g(e->device);
+  cudaStream_t st = pick_stream(e, stream);
+  TableBuilder tb;
+  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb);
+  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb);
+  for (int r = 0; r < maxnb; r++) {
+    std::vector<FwDiagJob> dj;
+    std::vector<MpSegment> ps, rs;
+    int pt = 0, rt = 0;
+    for (int32_t b = 0; b < count; b++) {
+      int nb = (sizes[b] + Bk - 1) / Bk;
+      if (r >= nb) continue;
+      FwDiagJob j{};
+      j.D = D[b];
+      j.P = pred ? P[b] : nullptr;
+      j.ld = ld[b];
+      j.size = sizes[b];
+      j.block = r;
+      dj.push_back(j);
+      if (nb > 1) {
+        MpSegment a, c, rest;
+        int t1, t2, t3;
+        fw_segments(D[b], pred ? P[b] : nullptr, ld[b], sizes[b], r, a, c, rest, t1, t2, t3,
+                    dtype == FAP_DTYPE_F32);
+        a.tile_begin = pt;
+        pt += t1;
+        ps.push_back(a);
+        c.tile_begin = pt;
+        pt += t2;
+        ps.push_back(c);
+        rest.tile_begin = rt;
+        rt += t3;
+        rs.push_back(rest);
+      }
+    }
+    nd[r] = (int)dj.size();
+    od[r] = tb.add(dj.data(), dj.size());
+    np[r] = (int)ps.size();
+    tp[r] = pt;
+    op[r] = tb.add(ps.data(), ps.size());
+    nr[r] = (int)rs.size();
+    tr[r] = rt;
+    orr[r] = tb.add(rs.data(), rs.size());
+  }
+  int rc;
+  if ((rc = e->small.ensure(std::max<size_t>(tb.bytes.size(), 64))) != FAP_OK) return rc;
+  FAP_CUDA(cudaMemcpyAsync(e->small.p, tb.bytes.data(), tb.bytes.size(), cudaMemcpyHostToDevice, st));
+  unsigned char *base = static_cast<unsigned char *>(e->small.p);
+  const bool f32 = dtype == FAP_DTYPE_F32;
+  for (int r = 0; r < maxnb; r++) {
+    FAP_CUDA(fapk::launch_fw_diag(f32, pred, reinterpret_cast<const FwDiagJob *>(base + od[r]), nd[r], st));
+    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], st));
+    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]), nr[r], tr[r], st));
+  }
+  FAP_CUDA(cudaStreamSynchronize(st));
+  return FAP_OK;
+}
+
+int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *dist, int32_t *pred,
+             int64_t ld, void *stream) {
+  if (!e || num_sources < 0 || (num_sources > 0 && (!sources || !dist)))
+    return set_error(FAP_ERR_INVALID, "fap_sssp: bad arguments");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  if (ld < e->n) return set_error(FAP_ERR_INVALID, "fap_sssp: ld < n");
+  for (int32_t i = 0; i < num_sources; i++)
+    if (sources[i] < 0 || sources[i] >= e->n) return set_error(FAP_ERR_INVALID, "fap_sssp: source out of range");
+  if (num_sources == 0) return FAP_OK;
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard g(e->device);
+  cudaStream_t st = pick_stream(e, stream);
+  std::vector<SsspBatch> batches;
+  for (int b0 = 0; b0 < num_sources; b0 += 32) {
+    SsspBatch sb{};
+    sb.count = std::min(32, num_sources - b0);
+    for (int l = 0; l < sb.count; l++) {
+      sb.src[l] = sources[b0 + l];
+      sb.row_off[l] = (int64_t)(b0 + l) * ld;
+    }
+    batches.push_back(sb);
+  }
+  int rc;
+  int slots = std::min((int)batches.size(), max_sssp_slots(e));
+  if ((rc = ensure_sssp_scratch(e, slots)) != FAP_OK) return rc;
+  if ((rc = e->small.ensure(batches.size() * sizeof(SsspBatch))) != FAP_OK) return rc;
+  FAP_CUDA(cudaMemcpyAsync(e->small.p, batches.data(), batches.size() * sizeof(SsspBatch),
+                           cudaMemcpyHostToDevice, st));
+  fapk::SsspArgs sa{};
+  sa.n = e->n;
+  sa.ro = e->d_ro;
+  sa.col = e->d_col;
+  sa.w = e->d_w;
+  sa.iro = e->d_iro;
+  sa.icol = e->d_icol;
+  sa.iw = e->d_iw;
+  sa.batches = static_cast<const SsspBatch *>(e->small.p);
+  sa.nbatches = (int)batches.size();
+  sa.dist = dist;
+  sa.pred = pred;
+  sa.scratch = e->sssp_scratch.p;
+  sa.slots = std::min(sa.nbatches, e->sssp_slots_alloc);
+  sa.stamps = static_cast<int32_t *>(e->sssp_stamps.p);
+  sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
+  sa.status = e->d_status;
+  sa.iter_cap = 2 * e->n + 8;
+  FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
+  FAP_CUDA(cudaStreamSynchronize(st));
+  return check_status(e);
+}
+
+int fap_backward(fap_engine *e, const int32_t *pred, int32_t num_pairs, const int32_t *s,
+                 const int32_t *t, const float *g, float *dw, void *stream) {
+  if (!e || num_pairs < 0 || (num_pairs > 0 && (!pred || !s || !t || !g || !dw)))
+    return set_error(FAP_ERR_INVALID, "fap_backward: bad arguments");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  if (!e->f32()) return set_error(FAP_ERR_INVALID, "fap_backward: FP32 engines only");
+  if (num_pairs == 0) return FAP_OK;
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard dg(e->device);
+  cudaStream_t st = pick_stream(e, stream);
+  FAP_CUDA(fapk::launch_backward_graph(e->n, e->d_ro, e->d_col, static_cast<const float *>(e->d_w),
+                                       e->d_ed2st, pred, num_pairs, s, t, g, dw, e->d_status, st));
+  FAP_CUDA(cudaStreamSynchronize(st));
+  return check_status(e);
+}
+
+int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes, int32_t *const *P,
+                       float *const *dW, const int64_t *ld, int32_t num_pairs, const int32_t *b,
+                       const int32_t *s, const int32_t *t, const float *g, void *stream) {
+  if (!e || count < 0 || num_pairs < 0 || (count > 0 && (!sizes || !P || !dW || !ld)) ||
+      (num_pairs > 0 && (!b || !s || !t || !g)))
+    return set_error(FAP_ERR_INVALID, "fap_backward_dense: bad arguments");
+  for (int32_t i = 0; i < count; i++)
+    if (sizes[i] < 0 || ld[i] < sizes[i] || (sizes[i] > 0 && (!P[i] || !dW[i])))
+      return set_error(FAP_ERR_INVALID, "fap_backward_dense: bad instance " + std::to_string(i));
+  if (num_pairs == 0 || count == 0) return FAP_OK;
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard dg(e->device);
+  cudaStream_t st = pick_stream(e, stream);
+  const size_t rec = fapk::dense_inst_bytes();
+  std::vector<unsigned char> tab(rec * count);
+  for (int32_t i = 0; i < count; i++) fapk::fill_dense_inst(tab.data() + rec * i, P[i], dW[i], ld[i], sizes[i]);
+  int rc;
+  if ((rc = e->small.ensure(tab.size())) != FAP_OK) return rc;
+  FAP_CUDA(cudaMemcpyAsync(e->small.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, st));
+  FAP_CUDA(fapk::launch_backward_dense(e->small.p, count, num_pairs, b, s, t, g, e->d_status, st));
+  FAP_CUDA(cudaStreamSynchronize(st));
+  return check_status(e);
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// launch.h -- host-side launchers of the engine's CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.cuh"
+
+namespace fapk {
+
+// minplus.cu
+cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, int nseg,
+                                 int total_tiles, cudaStream_t st);
+cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njobs,
+                           cudaStream_t st);
+int minplus_tile_rows();  // CTA output tile edge (128)
+int fw_block();           // FW pivot block edge (64)
+cudaError_t init_minplus_kernels();
+
+// sssp.cu
+struct SsspArgs {
+  int32_t n;
+  const int32_t *ro, *col;    // out-edge CSR
+  const void *w;              // out-edge weights (float or uint32)
+  const int32_t *iro, *icol;  // in-edge CSR (for predecessors)
+  const void *iw;
+  const SsspBatch *batches;
+  int32_t nbatches;
+  void *dist;                 // output base (rows addressed by SsspBatch::row_off)
+  int32_t *pred;              // may be null
+  void *scratch;              // per-slot scratch, sssp_slot_bytes(n) each
+  int32_t slots;              // number of CTAs (= scratch slots)
+  int32_t *stamps;            // slots * n ints, zeroed once at allocation
+  int32_t *slot_epoch;        // slots ints, zeroed once at allocation
+  unsigned *status;           // device status word (error flags are or-ed in)
+  int32_t iter_cap;
+};
+size_t sssp_slot_bytes(int32_t n);  // bytes of one slot's scratch (excluding stamps)
+int sssp_threads();
+cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st);
+
+// transform.cu
+struct PartDesc {
+  int32_t sub, bdy, start;  // part size, boundary count, first sorted position
+  int32_t ld;               // leading dimension of the part's FW matrix
+  int64_t mat_off;          // element offset of the FW matrix in the arena
+  int64_t row_off;          // element offset of the part's first result row
+};
+struct BuildArgs {
+  int32_t n;
+  const int32_t *ro, *col;
+  const void *w;
+  const int32_t *graph_id, *st2ed, *ed2st;
+  const PartDesc *parts;
+  const int64_t *row_begin;  // prefix sums of padded rows per part (nparts+1)
+  int32_t nparts;
+  int64_t total_rows;
+  void *mat;                 // FW matrices arena (dist)
+  int32_t *matp;             // FW matrices arena (pred), may be null
+  const void *rows;          // result rows (dist), source of boundary rows
+  const int32_t *rowsp;      // result rows (pred)
+  int64_t ldr;               // leading dimension of the result rows (n)
+};
+cudaError_t launch_build(bool f32, bool pred, const BuildArgs &a, cudaStream_t st);
+cudaError_t launch_decode(bool f32, bool pred, const BuildArgs &a, void *rows, int32_t *rowsp,
+                          cudaStream_t st);
+
+// adjoint.cu
+cudaError_t launch_backward_graph(int32_t n, const int32_t *ro, const int32_t *col, const float *w,
+                                  const int32_t *ed2st, const int32_t *pred, int32_t npairs,
+                                  const int32_t *s, const int32_t *t, const float *g, float *dw,
+                                  unsigned *status, cudaStream_t st);
+cudaError_t launch_backward_dense(const void *inst, int32_t ninst, int32_t npairs,
+                                  const int32_t *b, const int32_t *s, const int32_t *t,
+                                  const float *g, unsigned *status, cudaStream_t st);
+size_t dense_inst_bytes();
+void fill_dense_inst(void *dst, const int32_t *P, float *dW, int64_t ld, int32_t size);
+
+}  // namespace fapk

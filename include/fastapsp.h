@@ -1,0 +1,214 @@
+/*
+ * fastapsp.h -- C ABI of the GB300 Fast-APSP engine.
+ *
+ * The engine computes all-pairs shortest paths by the divide-and-conquer
+ * method of TomerHaham/FastAPSP: the vertex set is split into K parts on the
+ * host; per part, an SSSP runs from every boundary vertex over the whole
+ * graph, a Floyd-Warshall closes the part's dense sub x sub matrix, and a
+ * (min,+) product extends the inner rows to every vertex.  The hot path runs as
+ * hand-written sm_103a CUDA kernels on one GPU.
+ *
+ * Conventions
+ *  - Every function returns an int status: FAP_OK (0) or a negative FAP_ERR_*
+ *    code.  Nothing calls exit(); fap_last_error() gives a message.
+ *  - Vertex ids are 0-based; part ids are 1-based (1..K), as in the reference
+ *    (fap/utils/readIdFile.h:279-283).
+ *  - Distances are FP32 (unreached = 1e8, FAP_MAXVALUE_F32, as
+ *    fap/utils/parameter.h:26) or int32 (unreached = 2^30, FAP_INF_I32).
+ *    Predecessors are int32 original vertex ids, -1 = unreached, and
+ *    pred[s][s] = s.
+ *  - Result rows follow the reference layout (fap/fap.cpp:507-518,
+ *    fap/utils/util_Myalgorithm.h:236-247): the rows of part i are the part's
+ *    vertices in mapping (st2ed) order -- boundary vertices first -- and the
+ *    columns are original vertex ids.  solve() stacks the parts 1..K.
+ *  - Result buffers may be host memory (pageable or pinned) or device memory
+ *    of the engine's GPU; the engine detects which.  Streams are passed as
+ *    `void *` (a cudaStream_t) so that this header needs no CUDA headers;
+ *    NULL means the engine's own stream.
+ */
+#ifndef FASTAPSP_H_
+#define FASTAPSP_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define FAP_OK 0
+#define FAP_ERR_INVALID (-1)       /* bad argument */
+#define FAP_ERR_CUDA (-2)          /* a CUDA runtime call failed */
+#define FAP_ERR_NOMEM (-3)         /* device or host allocation failed */
+#define FAP_ERR_STATE (-4)         /* call not valid in the handle's state */
+#define FAP_ERR_NOT_CONVERGED (-5) /* SSSP hit its iteration cap */
+#define FAP_ERR_IO (-6)            /* file could not be read */
+#define FAP_ERR_NO_DEVICE (-7)     /* no CUDA device / wrong architecture */
+#define FAP_ERR_RANGE (-8)         /* value outside the supported range */
+
+#define FAP_DTYPE_F32 0
+#define FAP_DTYPE_I32 1
+
+#define FAP_MAXVALUE_F32 1e8f
+#define FAP_INF_I32 0x40000000
+
+/* Solve modes. */
+#define FAP_MODE_PLAIN 0   /* one launch sequence per part, parts in order */
+#define FAP_MODE_BATCHED 1 /* all parts per phase launch, in a CUDA graph */
+
+typedef struct fap_engine fap_engine; /* opaque */
+
+/* ---- library ------------------------------------------------------------ */
+const char *fap_version(void);
+const char *fap_status_string(int status);
+/* Message of the last failing call on this thread ("" if none). */
+const char *fap_last_error(void);
+/* Number of usable CUDA devices (0 without a GPU; never fails). */
+int fap_device_count(int32_t *count);
+
+/* ---- host preprocessing (CPU only, no GPU needed) ------------------------ */
+
+/* Replaces readVerEdges (fap/utils/readMatFile.h:36-64): vertex count and
+ * CSR entry count (doubled for undirected input) from a MatrixMarket
+ * header.  `path` is the full path of the .mtx file. */
+int fap_mtx_counts(const char *path, int32_t directed, int32_t weighted,
+                   int32_t *n, int64_t *m);
+
+/* Replaces readMatFile (fap/utils/readMatFile.h:66-173): CSR with 1-based
+ * input ids, undirected lines doubled, |w| for weighted input, w = 1 for
+ * unweighted input, duplicates and self loops kept, each row in reverse input
+ * order.  Arrays sized from fap_mtx_counts: adj_size[n], row_offset[n+1],
+ * col_val[m], weight[m]. */
+int fap_mtx_read(const char *path, int32_t directed, int32_t weighted,
+                 int32_t n, int64_t m, int32_t *adj_size, int32_t *row_offset,
+                 int32_t *col_val, float *weight);
+
+/* Replaces readIdFile_METIS / Graph_decomposition
+ * (fap/utils/readIdFile.h:79-304): K-way partition of the symmetrized graph
+ * by the engine's multilevel partitioner (heavy-edge coarsening, greedy
+ * growing bisection, boundary refinement; 3% imbalance).  Writes 1-based part
+ * ids into graph_id[n]; edge_cut (nullable) receives the number of cut
+ * undirected edges. */
+int fap_partition(int32_t n, const int32_t *row_offset, const int32_t *col_val,
+                  int32_t K, uint64_t seed, int32_t *graph_id,
+                  int64_t *edge_cut);
+
+/* Replaces findBoundry + sort_and_encode (fap/utils/util_preprocess.h:32-106):
+ * boundary marks (both endpoints of every cross-part CSR entry), the vertex
+ * order (part ascending, boundary first; st2ed[pos] = original id, ed2st its
+ * inverse) and the per-part counts/offsets ver_num, ver_offset, bdy_num,
+ * bdy_offset (K+1 entries each, index 0 unused).  The order inside a
+ * (part, boundary) group is that of the reference's std::sort call. */
+int fap_preprocess(int32_t K, int32_t n, const int32_t *graph_id,
+                   const int32_t *row_offset, const int32_t *col_val,
+                   int32_t *st2ed, int32_t *ed2st, int32_t *ver_num,
+                   int32_t *ver_offset, int32_t *bdy_num, int32_t *bdy_offset);
+
+/* ---- engine: one graph on one GPU --------------------------------------- */
+
+/* Replaces fapGraph(num_vertexs, num_edges, row_offset, col_val, weight, K)
+ * (fap/fap.h:102-104; empty in the reference, fap/fap.cpp:94-98) followed by
+ * preCondition() (fap/fap.cpp:100-114).  Copies the CSR (row_offset[n+1],
+ * col_val[m], weight[m]) to device `device`.  graph_id (n, 1-based) may be
+ * NULL, in which case fap_partition(seed 1) supplies it.  dtype selects the
+ * distance arithmetic: FAP_DTYPE_F32 (weights used as given) or
+ * FAP_DTYPE_I32 (weights must be non-negative integers below 2^20). */
+int fap_create(int32_t n, int64_t m, const int32_t *row_offset,
+               const int32_t *col_val, const float *weight, int32_t K,
+               const int32_t *graph_id, int32_t dtype, int32_t device,
+               fap_engine **out);
+
+/* A handle without a graph, for the standalone kernels below. */
+int fap_create_context(int32_t device, fap_engine **out);
+
+int fap_destroy(fap_engine *e);
+
+/* Metadata getters (fap/fap.cpp:546-566, 640-670).  Arrays are copied. */
+int fap_num_vertices(const fap_engine *e, int32_t *n, int32_t *K);
+int fap_mapping(const fap_engine *e, int32_t *st2ed);     /* n entries */
+int fap_graph_id(const fap_engine *e, int32_t *graph_id); /* n entries */
+/* sub = C_BlockVer_num[part], bdy = C_BlockBdy_num[part],
+ * offset = C_BlockVer_offset[part]. */
+int fap_part_info(const fap_engine *e, int32_t part, int32_t *sub,
+                  int32_t *bdy, int32_t *offset);
+
+/* Replaces solveSubGraph(id) (fap/fap.cpp:520-545) and the per-part
+ * pipeline fapGraph::run (fap/fap.cpp:195-503): writes the part's sub x n
+ * rows (dist of the engine dtype, pred int32; pred may be NULL). */
+int fap_solve_part(fap_engine *e, int32_t part, void *dist, int32_t *pred,
+                   void *stream);
+
+/* Replaces solve() (fap/fap.cpp:507-518): all parts, n x n rows stacked by
+ * part.  mode = FAP_MODE_PLAIN (per-part launch sequences, like the
+ * reference's host loop) or FAP_MODE_BATCHED (every phase runs over all parts
+ * in one launch; the launch sequence is replayed from a CUDA graph). */
+int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode,
+              void *stream);
+
+/* Device time of the last solve's phases in milliseconds:
+ * [sssp, floyd, min_plus, data, total] (the getTime* counters of
+ * fap/fap.cpp:622-639, measured with CUDA events). */
+int fap_last_times(const fap_engine *e, double *times5);
+
+/* ---- standalone kernels on caller device memory ------------------------- */
+
+/* Replaces min_plus_path_advanced_gpu (fap/kernel/minplus.h:81-90,
+ * minplus_NVIDIA_path_gpu, fap/kernel/cuda/minplus.cu:268-359):
+ *   C[i][j] = min_k A[i][k] + B[k][j],  Cpath[i][j] = Bpath[k*][j]
+ * for i < M, j < N, k < K, with k* the first k that reaches the minimum and
+ * C = unreached / Cpath = -1 where no k gives a finite sum.  All pointers are
+ * device memory, row-major with the given leading dimensions (elements).
+ * Bpath and Cpath may both be NULL (distances only). */
+int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K,
+                const void *A, int64_t lda, const void *B, int64_t ldb,
+                const int32_t *Bpath, int64_t ldbp, void *C, int64_t ldc,
+                int32_t *Cpath, int64_t ldcp, void *stream);
+
+/* Replaces floyd_path_gpu (fap/kernel/floyd.h:150-158,
+ * floyd_GPU_Nvidia_path_gpu, fap/kernel/cuda/floyd.cu:286-342): in-place
+ * Floyd-Warshall of `count` independent square matrices in one batched launch
+ * sequence.  D[b] is sizes[b] x sizes[b] with leading dimension ld[b]; P[b]
+ * (same shape and leading dimension, may be NULL for all b) is updated as
+ * P[i][j] = P[k][j] on every strict improvement.  The pointer arrays live in
+ * host memory; the matrices in device memory. */
+int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count,
+                      const int32_t *sizes, void *const *D, const int64_t *ld,
+                      int32_t *const *P, void *stream);
+
+/* Replaces handle_boundry_path_data_on_gpu (fap/kernel/batch_sssp.h:254-278,
+ * multi_source_Nvidia_sssp_data_on_gpu, fap/kernel/cuda/batch_sssp.cu:
+ * 361-414): SSSP from `num_sources` vertices (host array) of the engine's
+ * graph; row r of dist/pred (device memory, leading dimension ld) receives
+ * the distances/predecessors from sources[r].  Predecessors follow the
+ * reference's Dijkstra (batch_sssp.h:79-114): among the in-neighbours u of v
+ * whose relaxation reaches dist[v], the one first in (dist[u], u) order. */
+int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources,
+             void *dist, int32_t *pred, int64_t ld, void *stream);
+
+/* Adjoint of the APSP distances with respect to the edge weights (no
+ * reference counterpart).  For each (s[i], t[i], g[i]) triple, g[i] is added
+ * to dw[e] for every CSR entry e on the predecessor path from s[i] to t[i]
+ * (the lightest entry u->v of each step).  pred holds full n x n rows in
+ * solve() layout (row of vertex s = its mapping position); pred, s, t, g and
+ * dw (m entries, accumulated into) are device memory.  Unreached pairs add
+ * nothing. */
+int fap_backward(fap_engine *e, const int32_t *pred, int32_t num_pairs, const int32_t *s,
+                 const int32_t *t, const float *g, float *dw, void *stream);
+
+/* Adjoint for batches of dense instances (no reference counterpart): for each
+ * (b[i], s[i], t[i], g[i]), g[i] is added to dW[b][u][v] for every step u->v
+ * of the predecessor path from s[i] to t[i] in instance b.  P[b] and dW[b]
+ * are device matrices of sizes[b] x sizes[b] with leading dimension ld[b]
+ * (the P matrices of fap_floyd_batched); the pointer arrays live in host
+ * memory; b, s, t, g are device arrays. */
+int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes,
+                       int32_t *const *P, float *const *dW, const int64_t *ld,
+                       int32_t num_pairs, const int32_t *b, const int32_t *s,
+                       const int32_t *t, const float *g, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTAPSP_H_ */

@@ -1,0 +1,377 @@
+// fap_oracle.cpp -- CPU oracle for the Fast-APSP hot path.
+//
+// TEST INFRASTRUCTURE ONLY: a CPU restatement of the reference's CPU code path
+// (TomerHaham/FastAPSP).  Loaded only by tests/, __graft_entry__.smoke() and
+// bench.py's CPU-baseline leg; the CUDA engine never links or calls it.
+// Each function cites the reference file:line whose algorithm it restates.
+// The restatement keeps the reference's arithmetic (FP32, strict comparisons,
+// loop orders, sentinel 1e8) so that its outputs are bit-identical to the
+// reference compiled from its own sources (see oracle/Makefile, target `ref`).
+
+#include "fap_oracle.h"
+
+#include <math.h>
+#include <omp.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <fstream>
+#include <functional>
+#include <queue>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace {
+
+const float kMax = ORACLE_MAXVALUE;
+
+double now_s() {
+  return std::chrono::duration<double>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+void skip_comments(std::ifstream &in) {
+  // readMatFile.h:54-55 / :84-85: skip every leading line that starts with '%'.
+  while (in.peek() == '%') in.ignore(2048, '\n');
+}
+
+}  // namespace
+
+extern "C" {
+
+// readVerEdges (readMatFile.h:36-64): header "n n m", m doubled if undirected.
+int oracle_mtx_counts(const char *path, int directed, int weighted,
+                      int32_t *n, int64_t *m) {
+  (void)weighted;
+  std::ifstream in(path);
+  if (!in.is_open()) return -1;
+  skip_comments(in);
+  long long nn = 0, t = 0, mm = 0;
+  in >> nn >> t >> mm;
+  if (!directed) mm *= 2;
+  *n = (int32_t)nn;
+  *m = (int64_t)mm;
+  return 0;
+}
+
+// readMatFile (readMatFile.h:66-173).  Edges go into per-vertex linked lists
+// by prepending, so each CSR row lists its entries in reverse input order.
+int oracle_mtx_read(const char *path, int directed, int weighted, int32_t n,
+                    int64_t m, int32_t *adj_size, int32_t *row_offset,
+                    int32_t *col_val, float *weight) {
+  std::ifstream in(path);
+  if (!in.is_open()) return -1;
+  skip_comments(in);
+  long long nn = 0, t = 0, mm = 0;
+  in >> nn >> t >> mm;
+  std::vector<int64_t> head((size_t)n + 10, -1);
+  std::vector<int32_t> e;
+  std::vector<int64_t> next;
+  std::vector<float> w;
+  e.reserve((size_t)m);
+  next.reserve((size_t)m);
+  w.reserve((size_t)m);
+  auto add = [&](int a, int b, float c) {
+    e.push_back(b);
+    w.push_back(c);
+    next.push_back(head[a]);
+    head[a] = (int64_t)e.size() - 1;
+  };
+  int a, b;
+  double c;
+  if (!weighted) {
+    while (in >> a >> b) {
+      a--;
+      b--;
+      add(a, b, 1.0f);
+      if (!directed) add(b, a, 1.0f);
+    }
+  } else {
+    while (in >> a >> b >> c) {
+      a--;
+      b--;
+      c = fabs(c);
+      float tc = (float)c;
+      add(a, b, tc);
+      if (!directed) add(b, a, tc);
+    }
+  }
+  int64_t edges = 0;
+  row_offset[0] = 0;
+  for (int32_t i = 0; i < n; i++) {
+    int32_t count = 0;
+    for (int64_t j = head[i]; j != -1; j = next[j]) {
+      if (edges < m) {
+        col_val[edges] = e[j];
+        weight[edges] = w[j];
+      }
+      edges++;
+      count++;
+    }
+    adj_size[i] = count;
+    row_offset[i + 1] = row_offset[i] + count;
+  }
+  return 0;
+}
+
+// dijkstra_path (batch_sssp.h:79-114): binary heap over (distance, vertex)
+// pairs, strict improvement, path[u] = u, unreached = 1e8 / -1.
+void oracle_dijkstra_path(int32_t u, int32_t n, const int32_t *adj_size,
+                          const int32_t *row_offset, const int32_t *col_val,
+                          const float *weight, float *dist, int32_t *path) {
+  std::fill_n(dist, n, kMax);
+  std::fill_n(path, n, -1);
+  dist[u] = 0;
+  path[u] = u;
+  std::vector<bool> st(n, false);
+  typedef std::pair<float, int> PDI;
+  std::priority_queue<PDI, std::vector<PDI>, std::greater<PDI>> q;
+  q.push({0.0f, u});
+  while (!q.empty()) {
+    PDI x = q.top();
+    q.pop();
+    int ver = x.second;
+    float distance = x.first;
+    if (st[ver]) continue;
+    st[ver] = true;
+    int cnt = adj_size[ver];
+    int off = row_offset[ver];
+    for (int i = 0; i < cnt; i++) {
+      int nx = col_val[off + i];
+      float wv = weight[off + i];
+      if (dist[nx] > distance + wv) {
+        q.push({distance + wv, nx});
+        dist[nx] = distance + wv;
+        path[nx] = ver;
+      }
+    }
+  }
+}
+
+void oracle_dijkstra_f64(int32_t u, int32_t n, const int32_t *row_offset,
+                         const int32_t *col_val, const float *weight,
+                         double *dist) {
+  for (int32_t i = 0; i < n; i++) dist[i] = 1e300;
+  dist[u] = 0.0;
+  std::vector<bool> st(n, false);
+  typedef std::pair<double, int> PDI;
+  std::priority_queue<PDI, std::vector<PDI>, std::greater<PDI>> q;
+  q.push({0.0, u});
+  while (!q.empty()) {
+    PDI x = q.top();
+    q.pop();
+    int ver = x.second;
+    if (st[ver]) continue;
+    st[ver] = true;
+    for (int i = row_offset[ver]; i < row_offset[ver + 1]; i++) {
+      int nx = col_val[i];
+      double cand = x.first + (double)weight[i];
+      if (dist[nx] > cand) {
+        dist[nx] = cand;
+        q.push({cand, nx});
+      }
+    }
+  }
+}
+
+// batched_sssp_path (batch_sssp.h:232-252): OpenMP over sources, row i of the
+// output belongs to sources[i].
+void oracle_batched_sssp_path(const int32_t *sources, int32_t num, int32_t n,
+                              const int32_t *adj_size,
+                              const int32_t *row_offset,
+                              const int32_t *col_val, const float *weight,
+                              float *dist, int32_t *path) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int i = 0; i < num; i++) {
+    oracle_dijkstra_path(sources[i], n, adj_size, row_offset, col_val, weight,
+                         dist + (int64_t)i * n, path + (int64_t)i * n);
+  }
+}
+
+// floyd_CPU_path (floyd.h:38-49).
+void oracle_floyd_path(int32_t num, float *mat, int32_t *path) {
+  for (int64_t k = 0; k < num; k++)
+    for (int64_t i = 0; i < num; i++)
+      for (int64_t j = 0; j < num; j++) {
+        float cand = mat[i * num + k] + mat[k * num + j];
+        if (mat[i * num + j] > cand) {
+          mat[i * num + j] = cand;
+          path[i * num + j] = path[k * num + j];
+        }
+      }
+}
+
+// min_plus_path_CPU_advanced (minplus.h:51-65).
+void oracle_min_plus_path_advanced(const float *mat1, const float *mat2,
+                                   const int32_t *mat2_path, float *res,
+                                   int32_t *path, int32_t M, int32_t N,
+                                   int32_t K) {
+  for (int64_t i = 0; i < M; i++)
+    for (int64_t j = 0; j < N; j++) {
+      float r = kMax;
+      int32_t p = -1;
+      for (int64_t k = 0; k < K; k++) {
+        float cand = mat1[i * K + k] + mat2[k * N + j];
+        if (r > cand) {
+          r = cand;
+          p = mat2_path[k * N + j];
+        }
+      }
+      res[i * N + j] = r;
+      path[i * N + j] = p;
+    }
+}
+
+namespace {
+// Element and ordering of sort_and_encode (util_preprocess.h:60-71): part id
+// ascending, boundary vertices first.  The same std::sort call on the same
+// input sequence yields the same permutation as the reference.
+struct dense_node {
+  int v;
+  int GraphId;
+  int isBound;
+};
+bool node_before(const dense_node &a, const dense_node &b) {
+  if (a.GraphId == b.GraphId) return a.isBound > b.isBound;
+  return a.GraphId < b.GraphId;
+}
+}  // namespace
+
+// findBoundry (util_preprocess.h:32-58) + sort_and_encode (:73-106).
+void oracle_preprocess(int32_t K, int32_t n, const int32_t *graph_id,
+                       const int32_t *adj_size, const int32_t *row_offset,
+                       const int32_t *col_val, int32_t *st2ed, int32_t *ed2st,
+                       int32_t *ver_num, int32_t *ver_offset, int32_t *bdy_num,
+                       int32_t *bdy_offset, int32_t *is_boundary) {
+  std::vector<int> isb(n, 0);
+  std::vector<int> cnt_ver(K + 1, 0), cnt_bdy(K + 1, 0);
+  for (int32_t u = 0; u < n; u++) {
+    cnt_ver[graph_id[u]]++;
+    for (int32_t j = 0; j < adj_size[u]; j++) {
+      int nx = col_val[row_offset[u] + j];
+      if (graph_id[nx] != graph_id[u]) {
+        isb[u] = 1;
+        isb[nx] = 1;
+      }
+    }
+  }
+  for (int32_t i = 0; i < n; i++)
+    if (isb[i]) cnt_bdy[graph_id[i]]++;
+  std::vector<dense_node> ver(n);
+  for (int32_t i = 0; i < n; i++) ver[i] = dense_node{i, graph_id[i], isb[i]};
+  std::vector<dense_node> sorted(ver);
+  std::sort(sorted.begin(), sorted.end(), node_before);
+  for (int32_t i = 0; i < n; i++) {
+    st2ed[ver[i].v] = sorted[i].v;
+    ed2st[sorted[i].v] = ver[i].v;
+  }
+  int cnt = 0;
+  ver_num[0] = ver_offset[0] = bdy_num[0] = bdy_offset[0] = 0;
+  for (int i = 1; i <= K; i++) {
+    ver_offset[i] = cnt;
+    ver_num[i] = cnt_ver[i];
+    bdy_offset[i] = cnt;
+    bdy_num[i] = cnt_bdy[i];
+    cnt += cnt_ver[i];
+  }
+  if (is_boundary)
+    for (int32_t i = 0; i < n; i++) is_boundary[i] = isb[i];
+}
+
+// fapGraph::run, host-buffer branch (fap.cpp:400-502), with the helpers
+// MysubMatBuild_path (util_Myalgorithm.h:44-84), MyMat1Build (:278-285) and
+// MysubMatDecode_path (:236-247) inlined in the same order.
+void oracle_run_part(int32_t part_id, int32_t n, const int32_t *adj_size,
+                     const int32_t *row_offset, const int32_t *col_val,
+                     const float *weight, const int32_t *graph_id,
+                     const int32_t *st2ed, const int32_t *ed2st,
+                     const int32_t *ver_num, const int32_t *ver_offset,
+                     const int32_t *bdy_num_a, float *dist, int32_t *path,
+                     int32_t mp_rows, oracle_times *times) {
+  const int bdy = bdy_num_a[part_id];
+  const int sub = ver_num[part_id];
+  const int inner = sub - bdy;
+  const int start = ver_offset[part_id];
+  std::vector<float> mat1((size_t)inner * bdy, kMax);
+  std::vector<float> sm((size_t)sub * sub, kMax);
+  std::vector<int32_t> sp((size_t)sub * sub, -1);
+  oracle_times t = {0, 0, 0, 0};
+
+  // Stage 1: SSSP from every boundary vertex (handle_boundry_path).
+  double t0 = now_s();
+  std::vector<int32_t> src(bdy);
+  for (int i = 0; i < bdy; i++) src[i] = st2ed[start + i];
+  oracle_batched_sssp_path(src.data(), bdy, n, adj_size, row_offset, col_val,
+                           weight, dist, path);
+  double t1 = now_s();
+  t.sssp = t1 - t0;
+
+  // Stage 2.1: dense sub x sub matrix: local CSR edges (last entry wins),
+  // boundary rows from the SSSP rows, zero diagonal.
+  for (int i = 0; i < sub; i++) {
+    int v = st2ed[i + start];
+    for (int j = 0; j < adj_size[v]; j++) {
+      int nb = col_val[row_offset[v] + j];
+      if (graph_id[v] != graph_id[nb]) continue;
+      int idx = ed2st[nb] - start;
+      if (idx >= 0 && idx < sub) {
+        sm[(int64_t)i * sub + idx] = weight[row_offset[v] + j];
+        sp[(int64_t)i * sub + idx] = v;
+      }
+    }
+  }
+  for (int i = 0; i < bdy; i++)
+    for (int j = 0; j < sub; j++) {
+      int v = st2ed[j + start];
+      sm[(int64_t)i * sub + j] = dist[(int64_t)i * n + v];
+      sp[(int64_t)i * sub + j] = path[(int64_t)i * n + v];
+    }
+  for (int i = 0; i < sub; i++) {
+    sm[(int64_t)i * sub + i] = 0;
+    sp[(int64_t)i * sub + i] = st2ed[i + start];
+  }
+  double t2 = now_s();
+  t.data += t2 - t1;
+
+  // Stage 2.2: Floyd-Warshall on the part.
+  oracle_floyd_path(sub, sm.data(), sp.data());
+  double t3 = now_s();
+  t.floyd = t3 - t2;
+
+  // Stage 3.1: mat1 = FW[inner rows][boundary columns].
+  for (int i = 0; i < inner; i++)
+    memcpy(mat1.data() + (size_t)i * bdy, sm.data() + (size_t)(i + bdy) * sub,
+           bdy * sizeof(float));
+  double t4 = now_s();
+  t.data += t4 - t3;
+
+  // Stage 3.2: inner rows = mat1 (min,+) boundary rows.
+  int rows = (mp_rows < 0) ? inner : std::min(inner, (int)mp_rows);
+  int64_t off = (int64_t)bdy * n;
+  oracle_min_plus_path_advanced(mat1.data(), dist, path, dist + off, path + off,
+                                rows, n, bdy);
+  double t5 = now_s();
+  t.min_plus = t5 - t4;
+
+  // Stage 3.3: scatter the FW matrix into the part's rows (original columns).
+  for (int i = 0; i < sub; i++)
+    for (int j = 0; j < sub; j++) {
+      int v = st2ed[j + start];
+      dist[(int64_t)i * n + v] = sm[(size_t)i * sub + j];
+      path[(int64_t)i * n + v] = sp[(size_t)i * sub + j];
+    }
+  t.data += now_s() - t5;
+  if (times) *times = t;
+}
+
+void oracle_set_threads(int32_t threads) {
+  if (threads > 0) omp_set_num_threads(threads);
+}
+
+int32_t oracle_get_threads(void) { return omp_get_max_threads(); }
+
+}  // extern "C"
