@@ -60,6 +60,7 @@ SIGNATURES = {
     "fap_sssp": (C.c_int, [_p, _p, _i32, _p, _p, _i64, _p]),
     "fap_backward": (C.c_int, [_p, _p, _i32, _p, _p, _p, _p, _p]),
     "fap_backward_dense": (C.c_int, [_p, _i32, _p, _p, _p, _p, _i32, _p, _p, _p, _p, _p]),
+    "fap_addmin_peak": (C.c_int, [_p, _i32, C.POINTER(C.c_double)]),
 }
 
 _lib = None

@@ -18,9 +18,10 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libfastapsp.so"
+EXAMPLE = PKG / "fap_single_node"
 INCLUDE = PKG.parent / "include"
 
-CUDA_SOURCES = ["minplus.cu", "sssp.cu", "transform.cu", "adjoint.cu", "engine.cu"]
+CUDA_SOURCES = ["minplus.cu", "sssp.cu", "transform.cu", "adjoint.cu", "probe.cu", "engine.cu"]
 CXX_SOURCES = ["host_prep.cpp", "fap_graph.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -82,6 +83,10 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
         _run([nvcc, *GENCODE, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs),
               "-lpthread", "-ldl", "-lrt"])
         os.replace(tmp, LIB)
+    ex_src = CSRC / "single_node_example.cpp"
+    if not EXAMPLE.exists() or EXAMPLE.stat().st_mtime < max(LIB.stat().st_mtime, ex_src.stat().st_mtime):
+        _run([cxx, "-O2", "-std=c++17", "-I", str(INCLUDE), str(ex_src), "-o", str(EXAMPLE),
+              "-L", str(PKG), "-lfastapsp", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         for o in outputs:
             if o.strip():

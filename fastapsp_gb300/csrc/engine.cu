@@ -975,8 +975,9 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
   if (!e || M < 0 || N < 0 || K < 0 || !C || (K > 0 && (!A || !B)))
     return set_error(FAP_ERR_INVALID, "fap_minplus: bad arguments");
   if (dtype != FAP_DTYPE_F32 && dtype != FAP_DTYPE_I32) return set_error(FAP_ERR_INVALID, "unknown dtype");
-  if ((Bpath == nullptr) != (Cpath == nullptr)) return set_error(FAP_ERR_INVALID, "Bpath and Cpath go together");
-  if (lda < K || ldb < N || ldc < N || (Bpath && (ldbp < N || ldcp < N)))
+  if (Cpath == nullptr ? Bpath != nullptr : (Bpath == nullptr && K > 0))
+    return set_error(FAP_ERR_INVALID, "Bpath and Cpath go together");
+  if (lda < K || ldb < N || ldc < N || (Cpath && ldcp < N) || (Bpath && ldbp < N))
     return set_error(FAP_ERR_INVALID, "leading dimension too small");
   if (M == 0 || N == 0) return FAP_OK;
   std::lock_guard<std::mutex> lk(e->mu);
@@ -988,7 +989,7 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
   int rc;
   if ((rc = e->small.ensure(sizeof(MpSegment))) != FAP_OK) return rc;
   FAP_CUDA(cudaMemcpyAsync(e->small.p, &s, sizeof(s), cudaMemcpyHostToDevice, st));
-  FAP_CUDA(fapk::launch_minplus_tiles(dtype == FAP_DTYPE_F32, Bpath != nullptr,
+  FAP_CUDA(fapk::launch_minplus_tiles(dtype == FAP_DTYPE_F32, Cpath != nullptr,
                                       static_cast<const MpSegment *>(e->small.p), 1, tiles, st));
   FAP_CUDA(cudaStreamSynchronize(st));
   return FAP_OK;
@@ -1156,6 +1157,14 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes, int32
   FAP_CUDA(fapk::launch_backward_dense(e->small.p, count, num_pairs, b, s, t, g, e->d_status, st));
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);
+}
+
+int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s) {
+  if (!e || !ops_per_s || mode < 0 || mode > 3) return set_error(FAP_ERR_INVALID, "fap_addmin_peak: bad arguments");
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard dg(e->device);
+  FAP_CUDA(fapk::measure_addmin_peak(mode, e->sm_count, ops_per_s));
+  return FAP_OK;
 }
 
 }  // extern "C"

@@ -76,4 +76,7 @@ cudaError_t launch_backward_dense(const void *inst, int32_t ninst, int32_t npair
 size_t dense_inst_bytes();
 void fill_dense_inst(void *dst, const int32_t *P, float *dW, int64_t ld, int32_t size);
 
+// probe.cu
+cudaError_t measure_addmin_peak(int mode, int sm_count, double *ops_per_s);
+
 }  // namespace fapk

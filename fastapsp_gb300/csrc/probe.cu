@@ -1,0 +1,127 @@
+// probe.cu -- add-min issue-rate microbenchmark (the roofline denominator of
+// the Floyd-Warshall and min-plus phases; no counterpart in the reference).
+//
+// Each thread keeps 64 independent accumulators and applies the add-min
+// operation of the chosen kind to them from register operands only (no
+// memory traffic), so the kernel runs at the SM's issue limit for that
+// instruction sequence.  Operands rotate over 4 register sets and one set is
+// bumped per pass so that the compiler cannot fold repeated minima; the bump
+// costs 16 of every 272 instructions, which makes the measured peak a slight
+// underestimate.
+//   mode 0: int32 DPX add-min   acc = __viaddmin_u32(a, b, acc)
+//   mode 1: FP32 add-min        acc = fminf(a + b, acc)
+//   mode 2: int32 add-min keeping the argmin (the tile kernel's inner step)
+//   mode 3: FP32 add-min keeping the argmin
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "launch.h"
+
+namespace fapk {
+
+namespace {
+
+template <int MODE>
+__global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int iters, unsigned seed) {
+  constexpr bool F = (MODE == 1 || MODE == 3);
+  constexpr bool ARG = (MODE >= 2);
+  using T = typename std::conditional<F, float, unsigned>::type;
+  T a[4][4], b[4][16], acc[4][16];
+  int arg[4][16];
+  const unsigned t = threadIdx.x + blockIdx.x * blockDim.x + seed;
+#pragma unroll
+  for (int s = 0; s < 4; s++)
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      if (i < 4) a[s][i] = (T)((t * 7 + s * 13 + i * 3) & 1023);
+      b[s][i] = (T)((t * 5 + s * 11 + i * 17) & 1023);
+    }
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < 16; c++) {
+      acc[r][c] = (T)(1 << 20);
+      arg[r][c] = 0;
+    }
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          const T x = a[s][r], y = b[s][c];
+          if (MODE == 0) {
+            acc[r][c] = (T)__viaddmin_u32((unsigned)x, (unsigned)y, (unsigned)acc[r][c]);
+          } else if (MODE == 1) {
+            acc[r][c] = fminf((float)x + (float)y, (float)acc[r][c]);
+          } else {
+            const T v = x + y;
+            if (v < acc[r][c]) {
+              acc[r][c] = v;
+              arg[r][c] = s;
+            }
+          }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) b[it & 3][i] = b[it & 3][i] - (T)1;
+  }
+  unsigned x = 0;
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < 16; c++) {
+      unsigned v;
+      if (F) v = __float_as_uint((float)acc[r][c]); else v = (unsigned)acc[r][c];
+      x ^= v + (ARG ? (unsigned)arg[r][c] : 0u);
+    }
+  out[threadIdx.x + blockIdx.x * blockDim.x] = x;
+}
+
+template <int MODE>
+cudaError_t run_mode(unsigned *buf, int blocks, int iters, cudaStream_t st) {
+  addmin_peak_kernel<MODE><<<blocks, 256, 0, st>>>(buf, iters, 1u);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Returns add-min operations per second of `mode` on the current device.
+cudaError_t measure_addmin_peak(int mode, int sm_count, double *ops_per_s) {
+  const int blocks = sm_count * 8;  // 8 x 256 threads per SM
+  const int iters = 2048;
+  unsigned *buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, (size_t)blocks * 256 * sizeof(unsigned));
+  if (e != cudaSuccess) return e;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; rep++) {
+    cudaEventRecord(a, 0);
+    switch (mode) {
+      case 0: e = run_mode<0>(buf, blocks, iters, 0); break;
+      case 1: e = run_mode<1>(buf, blocks, iters, 0); break;
+      case 2: e = run_mode<2>(buf, blocks, iters, 0); break;
+      default: e = run_mode<3>(buf, blocks, iters, 0); break;
+    }
+    cudaEventRecord(b, 0);
+    if (e != cudaSuccess) break;
+    e = cudaEventSynchronize(b);
+    if (e != cudaSuccess) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep > 0) best = ms < best ? ms : best;  // first launch is warm-up
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  if (e != cudaSuccess) return e;
+  const double ops = (double)blocks * 256 * iters * 4 * 4 * 16;
+  *ops_per_s = ops / (best * 1e-3);
+  return cudaSuccess;
+}
+
+}  // namespace fapk

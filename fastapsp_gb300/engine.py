@@ -201,6 +201,13 @@ class Context:
         check(lib().fap_floyd_batched(self._h, int(dtype), cnt, ptr(sizes), D, ptr(lds), P, stream),
               "fap_floyd_batched")
 
+    def addmin_peak(self, mode: int) -> float:
+        """Add-min ops/s issued from registers (0: int32 DPX, 1: FP32,
+        2: int32 with argmin, 3: FP32 with argmin)."""
+        v = C.c_double(0)
+        check(lib().fap_addmin_peak(self._h, int(mode), C.byref(v)), "fap_addmin_peak")
+        return float(v.value)
+
     def backward_dense(self, preds, dWs, b, s, t, g, stream=None):
         cnt = len(preds)
         sizes = np.array([p.shape[0] for p in preds], np.int32)

@@ -113,7 +113,8 @@ int fap_preprocess(int32_t K, int32_t n, const int32_t *graph_id,
  * col_val[m], weight[m]) to device `device`.  graph_id (n, 1-based) may be
  * NULL, in which case fap_partition(seed 1) supplies it.  dtype selects the
  * distance arithmetic: FAP_DTYPE_F32 (weights used as given) or
- * FAP_DTYPE_I32 (weights must be non-negative integers below 2^20). */
+ * FAP_DTYPE_I32 (non-negative integer weights with (n-1) * max weight below
+ * 2^30, so that no finite distance reaches the int32 "unreached" value). */
 int fap_create(int32_t n, int64_t m, const int32_t *row_offset,
                const int32_t *col_val, const float *weight, int32_t K,
                const int32_t *graph_id, int32_t dtype, int32_t device,
@@ -206,6 +207,15 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes,
                        int32_t *const *P, float *const *dW, const int64_t *ld,
                        int32_t num_pairs, const int32_t *b, const int32_t *s,
                        const int32_t *t, const float *g, void *stream);
+
+/* ---- diagnostics -------------------------------------------------------- */
+
+/* Add-min operations per second that the GPU issues from registers alone
+ * (no reference counterpart; the roofline denominator of the FW and min-plus
+ * phases).  mode 0: int32 DPX add-min (__viaddmin_u32); 1: FP32
+ * fminf(a + b, c); 2: int32 add-min keeping the argmin; 3: FP32 add-min
+ * keeping the argmin. */
+int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s);
 
 #ifdef __cplusplus
 }

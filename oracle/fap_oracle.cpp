@@ -153,7 +153,7 @@ void oracle_dijkstra_path(int32_t u, int32_t n, const int32_t *adj_size,
 }
 
 void oracle_dijkstra_f64(int32_t u, int32_t n, const int32_t *row_offset,
-                         const int32_t *col_val, const float *weight,
+                         const int32_t *col_val, const double *weight,
                          double *dist) {
   for (int32_t i = 0; i < n; i++) dist[i] = 1e300;
   dist[u] = 0.0;
@@ -169,7 +169,7 @@ void oracle_dijkstra_f64(int32_t u, int32_t n, const int32_t *row_offset,
     st[ver] = true;
     for (int i = row_offset[ver]; i < row_offset[ver + 1]; i++) {
       int nx = col_val[i];
-      double cand = x.first + (double)weight[i];
+      double cand = x.first + weight[i];
       if (dist[nx] > cand) {
         dist[nx] = cand;
         q.push({cand, nx});

@@ -41,9 +41,10 @@ int oracle_mtx_read(const char *path, int directed, int weighted,
 void oracle_dijkstra_path(int32_t u, int32_t n, const int32_t *adj_size,
                           const int32_t *row_offset, const int32_t *col_val,
                           const float *weight, float *dist, int32_t *path);
-/* FP64 Dijkstra over the same CSR (distance only, 1e300 = unreached). */
+/* FP64 Dijkstra over the same CSR with FP64 weights (distance only,
+ * 1e300 = unreached). */
 void oracle_dijkstra_f64(int32_t u, int32_t n, const int32_t *row_offset,
-                         const int32_t *col_val, const float *weight,
+                         const int32_t *col_val, const double *weight,
                          double *dist);
 /* Batched SSSP over `num` sources, OpenMP over sources like
  * batched_sssp_path (batch_sssp.h:232-252). */

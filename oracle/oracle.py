@@ -94,7 +94,7 @@ def dijkstra_path(u, ro, col, w):
 
 def dijkstra_f64(u, ro, col, w):
     ro, col = _i32(ro), _i32(col)
-    w = np.ascontiguousarray(w, np.float32)
+    w = np.ascontiguousarray(w, np.float64)
     n = ro.shape[0] - 1
     d = np.empty(n, np.float64)
     lib().oracle_dijkstra_f64(int(u), n, _p(ro), _p(col), _p(w), _p(d))

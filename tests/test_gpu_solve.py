@@ -1,0 +1,112 @@
+"""Full Fast-APSP solves through the C ABI against the reference's own outputs
+(golden fixtures) and the CPU oracle."""
+import numpy as np
+import pytest
+import torch
+from conftest import GOLDEN, load_golden
+from helpers import MAXV, check_pred_tight, has_parallel_edges, to_ref_float
+
+pytestmark = pytest.mark.gpu
+
+INT_CASES = [n for n in GOLDEN if not n.endswith("f32")]
+F32_CASES = [n for n in GOLDEN if n.endswith("f32")]
+
+
+def solve_engine(gpu, z, g, dtype, mode, on_device):
+    n = g.n
+    with gpu.Engine(n, g.row_offset, g.col_val, g.weight, int(z["K"]), graph_id=z["graph_id"],
+                    dtype=dtype) as eng:
+        assert np.array_equal(eng.mapping(), z["mapping"])
+        npdt = np.int32 if dtype == gpu.DTYPE_I32 else np.float32
+        if on_device:
+            d = torch.empty((n, n), dtype=torch.int32 if dtype == gpu.DTYPE_I32 else torch.float32, device="cuda")
+            p = torch.empty((n, n), dtype=torch.int32, device="cuda")
+            eng.solve(d, p, mode)
+            torch.cuda.synchronize()
+            d, p = d.cpu().numpy(), p.cpu().numpy()
+        else:
+            d = np.empty((n, n), npdt)
+            p = np.empty((n, n), np.int32)
+            eng.solve(d, p, mode)
+        # second call reuses the cached plan / graph
+        if not on_device:
+            d2 = np.empty_like(d)
+            p2 = np.empty_like(p)
+            eng.solve(d2, p2, mode)
+            assert np.array_equal(d, d2) and np.array_equal(p, p2)
+    return to_ref_float(d), p
+
+
+def out_of_part_mask(z):
+    gid = z["graph_id"]
+    rows_part = gid[z["mapping"]]
+    return rows_part[:, None] != gid[None, :]
+
+
+@pytest.mark.parametrize("name", INT_CASES)
+@pytest.mark.parametrize("dtype_name", ["i32", "f32"])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_solve_integer_graphs_bit_exact(gpu, name, dtype_name, mode):
+    z, g = load_golden(name)
+    dtype = gpu.DTYPE_I32 if dtype_name == "i32" else gpu.DTYPE_F32
+    d, p = solve_engine(gpu, z, g, dtype, mode, on_device=(mode == 1))
+    assert np.array_equal(d.view(np.int32), z["dist"].view(np.int32))
+    # predecessors: identical to the reference outside each part's own columns
+    # (SSSP and min-plus region); tight shortest-path edges everywhere
+    m = out_of_part_mask(z)
+    assert np.array_equal(p[m], z["path"][m])
+    check_pred_tight(d, p, z["mapping"], g.n, g.row_offset, g.col_val, g.weight)
+
+
+@pytest.mark.parametrize("name", F32_CASES)
+@pytest.mark.parametrize("mode", [0, 1])
+def test_solve_f32_graphs_within_tolerance(gpu, oracle_lib, name, mode):
+    z, g = load_golden(name)
+    d, p = solve_engine(gpu, z, g, gpu.DTYPE_F32, mode, on_device=False)
+    ref = z["dist"]
+    fin = ref < MAXV
+    assert np.array_equal(fin, d < MAXV)
+    rel = np.abs(d[fin] - ref[fin]) / np.maximum(ref[fin], 1e-30)
+    assert rel.max() <= 1e-6
+    # against FP64 Dijkstra.  Not with parallel edges: the reference's part
+    # matrix keeps the last CSR entry of parallel edges, not the lightest
+    # (util_Myalgorithm.h:54-63), and the engine reproduces that.
+    rows = [] if has_parallel_edges(g.n, g.row_offset, g.col_val) else range(0, g.n, max(1, g.n // 20))
+    for r in rows:
+        s = int(z["mapping"][r])
+        d64 = oracle_lib.dijkstra_f64(s, g.row_offset, g.col_val, g.weight)
+        f = d64 < 1e299
+        assert np.all((d[r] < MAXV) == f)
+        assert np.max(np.abs(d[r][f] - d64[f]) / np.maximum(d64[f], 1e-30)) <= 1e-6
+    check_pred_tight(d, p, z["mapping"], g.n, g.row_offset, g.col_val, g.weight, rtol=1e-6)
+
+
+def test_solve_part_matches_reference_sub_graph(gpu):
+    z, g = load_golden("grid16_sub")
+    K = int(z["K"])
+    with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, K, graph_id=z["graph_id"],
+                    dtype=gpu.DTYPE_I32) as eng:
+        for part in (1, K):
+            sub, bdy, off = eng.part_info(part)
+            d = np.empty((sub, g.n), np.int32)
+            p = np.empty((sub, g.n), np.int32)
+            eng.solve_part(part, d, p)
+            assert np.array_equal(to_ref_float(d), z[f"sub{part}_dist"])
+            assert np.array_equal(eng.mapping()[off:off + sub], z[f"sub{part}_index"])
+
+
+def test_fapgraph_mirror_solve_and_split(gpu):
+    z, g = load_golden("knn300_dir_int")
+    G = gpu.FapGraph(g.n, g.m, g.row_offset, g.col_val, g.weight, int(z["K"]), graph_id=z["graph_id"])
+    G.preCondition()
+    assert not G.isSplit()
+    assert G.solve() == 0
+    assert np.array_equal(G.getAllDistance(), z["dist"])
+    assert np.array_equal(G.getMapping(), z["mapping"])
+    assert G.solveSubGraph(2) == 0
+    assert G.solveSubGraph(2) == 0  # already processed: warning, no work
+    off = int(G.C_BlockVer_offset[2])
+    sub = int(G.C_BlockVer_num[2])
+    assert np.array_equal(G.getSubGraphDistance(2), z["dist"][off:off + sub])
+    assert np.array_equal(G.getSubGraphIndex(2), z["mapping"][off:off + sub])
+    G.close()
