@@ -184,15 +184,18 @@ def run_ours(args, rank, world, local_rank):
     # roofline of the dominant kernel (min-plus) against the add-min issue peak
     peak_dpx = eng_ctx_peak(fap, dev, 0)
     peak_arg = eng_ctx_peak(fap, dev, 2)
-    mp_rate = addmin_mp / (ph["min_plus"] / 1e3)
-    fw_rate = addmin_fw / (ph["floyd"] / 1e3)
+    def rate(x, ms):
+        return x / (ms / 1e3) if ms and ms > 0 else float("nan")
+
+    mp_rate = rate(addmin_mp, ph["min_plus"])
+    fw_rate = rate(addmin_fw, ph["floyd"])
     peaks, peak_src = read_peaks()
     hbm = float(peaks.get("hbm_gbs", HBM_PEAK_FALLBACK))
     srcs = int(bdys.sum())
     sssp_bytes = srcs * (4 * (n + 1) + 8 * g.m + 8 * n)
-    sssp_gbs = sssp_bytes / (ph["sssp"] / 1e3) / 1e9
+    sssp_gbs = rate(sssp_bytes, ph["sssp"]) / 1e9
     mp_bytes = int(((subs - bdys) * n * 8).sum() + (bdys * n * 8).sum())  # C written + B read once
-    mp_gbs = mp_bytes / (ph["min_plus"] / 1e3) / 1e9
+    mp_gbs = rate(mp_bytes, ph["min_plus"]) / 1e9
 
     # plain form (per-part launches) on the same graph, for batched-vs-plain
     plain_ms = []

@@ -106,8 +106,10 @@ struct Plan {
     // build / decode
     const PartDesc *pdesc = nullptr;
     const int64_t *row_begin = nullptr;
+    const int64_t *dec_begin = nullptr;
     int nparts = 0;
     int64_t total_rows = 0;
+    int64_t dec_rows = 0;
     // FW: per round r, diag jobs [diag_off[r], +diag_cnt[r]) and segments
     std::vector<const FwDiagJob *> diag;
     std::vector<int> diag_cnt;
@@ -118,9 +120,13 @@ struct Plan {
     // min-plus
     const MpSegment *mp = nullptr;
     int mp_nseg = 0, mp_tiles = 0;
+    int max_sub = 0;  // largest part of the group (bound of the packed form)
   };
   std::vector<Group> groups;
   size_t fw_elems = 0;  // FW arena elements needed
+  int max_sub = 0;      // largest part of the plan
+  int max_mp_k = 0;     // largest min-plus K (boundary count) of the plan
+  int pack = -1;        // packed int32 form: -1 undecided, 0 no, 1 yes
   // graph (batched mode)
   cudaGraphExec_t exec = nullptr;
   ~Plan() {
@@ -154,6 +160,7 @@ struct fap_engine {
   int sm_count = 0;
   std::vector<int32_t> ro, col, graph_id, st2ed, ed2st, ver_num, ver_offset, bdy_num, bdy_offset;
   std::vector<float> w;
+  uint32_t wmax = 0;  // largest weight (int32 mode)
   // device graph
   int32_t *d_ro = nullptr, *d_col = nullptr, *d_iro = nullptr, *d_icol = nullptr;
   int32_t *d_gid = nullptr, *d_st2ed = nullptr, *d_ed2st = nullptr;
@@ -317,7 +324,7 @@ int build_plan(fap_engine *e, Plan &pl) {
 
   TableBuilder tb;
   struct GroupOffs {
-    size_t batches, pdesc, row_begin, mp;
+    size_t batches, pdesc, row_begin, dec_begin, mp;
     std::vector<size_t> diag, panel, rest;
   };
   std::vector<GroupOffs> goffs(groups.size());
@@ -328,7 +335,7 @@ int build_plan(fap_engine *e, Plan &pl) {
     // SSSP batches: per part, its boundary vertices in mapping order.
     std::vector<SsspBatch> batches;
     std::vector<PartDesc> pdesc;
-    std::vector<int64_t> row_begin(1, 0);
+    std::vector<int64_t> row_begin(1, 0), dec_begin(1, 0);
     std::vector<MpSegment> mps;
     int mp_tiles = 0;
     int maxnb = 0;
@@ -346,6 +353,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         batches.push_back(sb);
       }
       if (sub == 0) continue;
+      G.max_sub = std::max(G.max_sub, sub);
       PartDesc d{};
       d.sub = sub;
       d.bdy = bdy;
@@ -355,6 +363,8 @@ int build_plan(fap_engine *e, Plan &pl) {
       d.row_off = roff;
       pdesc.push_back(d);
       row_begin.push_back(row_begin.back() + d.ld);
+      dec_begin.push_back(dec_begin.back() + bdy);
+      pl.max_sub = std::max(pl.max_sub, sub);
       maxnb = std::max(maxnb, d.ld / B);
       // min-plus for the inner rows
       int inner = sub - bdy;
@@ -366,6 +376,15 @@ int build_plan(fap_engine *e, Plan &pl) {
                                  dist + (size_t)(roff + (int64_t)bdy * n) * es, n,
                                  pred ? pl.pred + roff + (int64_t)bdy * n : nullptr, n, inner,
                                  (int)n, bdy, tiles);
+        // the part's own columns come from the FW matrix (rows bdy..sub-1)
+        s.col_part = e->d_gid;
+        s.part = p;
+        s.col_local = e->d_ed2st;
+        s.local0 = start;
+        s.F = fwd + (size_t)(mat_off[idx] + (int64_t)bdy * d.ld) * es;
+        s.Fp = pred ? fwp + mat_off[idx] + (int64_t)bdy * d.ld : nullptr;
+        s.ldf = d.ld;
+        pl.max_mp_k = std::max(pl.max_mp_k, bdy);
         s.tile_begin = mp_tiles;
         mp_tiles += tiles;
         mps.push_back(s);
@@ -375,8 +394,10 @@ int build_plan(fap_engine *e, Plan &pl) {
     O.batches = tb.add(batches.data(), batches.size());
     G.nparts = (int)pdesc.size();
     G.total_rows = row_begin.back();
+    G.dec_rows = dec_begin.back();
     O.pdesc = tb.add(pdesc.data(), pdesc.size());
     O.row_begin = tb.add(row_begin.data(), row_begin.size());
+    O.dec_begin = tb.add(dec_begin.data(), dec_begin.size());
     G.mp_nseg = (int)mps.size();
     G.mp_tiles = mp_tiles;
     O.mp = tb.add(mps.data(), mps.size());
@@ -440,6 +461,7 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.batches = reinterpret_cast<const SsspBatch *>(base + O.batches);
     G.pdesc = reinterpret_cast<const PartDesc *>(base + O.pdesc);
     G.row_begin = reinterpret_cast<const int64_t *>(base + O.row_begin);
+    G.dec_begin = reinterpret_cast<const int64_t *>(base + O.dec_begin);
     G.mp = reinterpret_cast<const MpSegment *>(base + O.mp);
     size_t R = O.diag.size();
     G.diag.resize(R);
@@ -465,8 +487,10 @@ fapk::BuildArgs build_args(fap_engine *e, const Plan &pl, const Plan::Group &G) 
   a.ed2st = e->d_ed2st;
   a.parts = G.pdesc;
   a.row_begin = G.row_begin;
+  a.dec_begin = G.dec_begin;
   a.nparts = G.nparts;
   a.total_rows = G.total_rows;
+  a.dec_rows = G.dec_rows;
   a.mat = e->fw_d.p;
   a.matp = pl.pred ? static_cast<int32_t *>(e->fw_p.p) : nullptr;
   a.rows = pl.dist;
@@ -475,14 +499,21 @@ fapk::BuildArgs build_args(fap_engine *e, const Plan &pl, const Plan::Group &G) 
   return a;
 }
 
-// Issues the launch sequence of a plan on `st`.  Events ev[0..5] bracket the
-// phases of the whole plan (recorded on the first/last group).
-int issue_plan(fap_engine *e, Plan &pl, cudaStream_t st, bool record_events) {
-  const bool f32 = e->f32();
-  const bool pred = pl.pred != nullptr;
-  for (size_t g = 0; g < pl.groups.size(); g++) {
+// Launch helpers for one plan.  Phase A is the SSSP of one group, phase B
+// the rest of the group (build, FW rounds, min-plus, decode).  Events
+// ev[0..5] bracket the phases: ev0 before the first SSSP, ev1 after the last
+// SSSP, ev2..ev5 after build / FW / min-plus / decode of the last group.
+struct Issuer {
+  fap_engine *e;
+  Plan &pl;
+  cudaStream_t st;
+  bool capturing;
+  cudaError_t rec(int i) {
+    return capturing ? cudaEventRecordWithFlags(e->ev[i], st, cudaEventRecordExternal)
+                     : cudaEventRecord(e->ev[i], st);
+  }
+  int sssp(size_t g) {
     Plan::Group &G = pl.groups[g];
-    if (record_events && g == 0) FAP_CUDA(cudaEventRecord(e->ev[0], st));
     fapk::SsspArgs sa{};
     sa.n = e->n;
     sa.ro = e->d_ro;
@@ -500,23 +531,70 @@ int issue_plan(fap_engine *e, Plan &pl, cudaStream_t st, bool record_events) {
     sa.stamps = static_cast<int32_t *>(e->sssp_stamps.p);
     sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
     sa.status = e->d_status;
+    sa.maxd = e->f32() ? nullptr : e->d_status + 1;
     sa.iter_cap = 2 * e->n + 8;
-    FAP_CUDA(fapk::launch_sssp(f32, sa, st));
-    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[1], st));
+    FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
+    return FAP_OK;
+  }
+  int rest(size_t g, bool last) {
+    const bool f32 = e->f32();
+    const bool pred = pl.pred != nullptr;
+    const bool packed = pl.pack == 1;
+    Plan::Group &G = pl.groups[g];
     fapk::BuildArgs ba = build_args(e, pl, G);
     FAP_CUDA(fapk::launch_build(f32, pred, ba, st));
-    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[2], st));
+    if (last) FAP_CUDA(rec(2));
     for (size_t r = 0; r < G.diag.size(); r++) {
       FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
-      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], st));
-      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], st));
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
     }
-    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[3], st));
-    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, st));
-    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[4], st));
+    if (last) FAP_CUDA(rec(3));
+    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, packed, st));
+    if (last) FAP_CUDA(rec(4));
     FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, st));
-    if (record_events && g + 1 == pl.groups.size()) FAP_CUDA(cudaEventRecord(e->ev[5], st));
+    if (last) FAP_CUDA(rec(5));
+    return FAP_OK;
   }
+  // Plain plans interleave per part (SSSP, rest); batched plans have one group.
+  int all() {
+    int rc;
+    FAP_CUDA(rec(0));
+    for (size_t g = 0; g < pl.groups.size(); g++) {
+      if ((rc = sssp(g)) != FAP_OK) return rc;
+      if (g + 1 == pl.groups.size()) FAP_CUDA(rec(1));
+      if ((rc = rest(g, g + 1 == pl.groups.size())) != FAP_OK) return rc;
+    }
+    return FAP_OK;
+  }
+};
+
+// Decides the packed int32 form for a plan on its first run: runs every
+// group's SSSP, reads back the largest finite SSSP distance, and checks the
+// bound of every finite result: a path inside a part to its first boundary
+// vertex ((max part size - 1) * max weight) plus an SSSP distance from that
+// boundary vertex.  Afterwards runs the rest of every group.
+int first_run(fap_engine *e, Plan &pl, cudaStream_t st) {
+  Issuer is{e, pl, st, false};
+  int rc;
+  if (e->f32()) {
+    pl.pack = 0;
+    return is.all();
+  }
+  FAP_CUDA(cudaMemsetAsync(e->d_status + 1, 0, sizeof(unsigned), st));
+  FAP_CUDA(is.rec(0));
+  for (size_t g = 0; g < pl.groups.size(); g++)
+    if ((rc = is.sssp(g)) != FAP_OK) return rc;
+  FAP_CUDA(is.rec(1));
+  unsigned maxd = 0;
+  FAP_CUDA(cudaMemcpyAsync(&maxd, e->d_status + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  FAP_CUDA(cudaStreamSynchronize(st));
+  const unsigned long long bound =
+      (unsigned long long)maxd + (unsigned long long)std::max(pl.max_sub - 1, 0) * e->wmax;
+  const bool k_ok = pl.pred == nullptr || pl.max_mp_k <= fapk::max_packed_k();
+  pl.pack = (bound < fapk::pack_limit() && k_ok) ? 1 : 0;
+  for (size_t g = 0; g < pl.groups.size(); g++)
+    if ((rc = is.rest(g, g + 1 == pl.groups.size())) != FAP_OK) return rc;
   return FAP_OK;
 }
 
@@ -577,12 +655,14 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
   }
+  if (pl->pack < 0) return first_run(e, *pl, st);
   if (mode == FAP_MODE_BATCHED) {
     if (!pl->exec) {
       cudaGraph_t graph = nullptr;
       cudaStream_t cap = e->stream;
       FAP_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-      int irc = issue_plan(e, *pl, cap, true);
+      Issuer is{e, *pl, cap, true};
+      int irc = is.all();
       cudaError_t ce = cudaStreamEndCapture(cap, &graph);
       if (irc != FAP_OK) {
         if (graph) cudaGraphDestroy(graph);
@@ -606,7 +686,8 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
       FAP_CUDA(cudaStreamWaitEvent(st, e->ev_sync[1], 0));
     }
   } else {
-    if ((rc = issue_plan(e, *pl, st, true)) != FAP_OK) return rc;
+    Issuer is{e, *pl, st, false};
+    if ((rc = is.all()) != FAP_OK) return rc;
   }
   return FAP_OK;
 }
@@ -650,8 +731,9 @@ int init_device(fap_engine *e, int device) {
   FAP_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
   for (auto &ev : e->ev) FAP_CUDA(cudaEventCreate(&ev));
   for (auto &ev : e->ev_sync) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-  FAP_CUDA(cudaMalloc(&e->d_status, sizeof(unsigned)));
-  FAP_CUDA(cudaMemset(e->d_status, 0, sizeof(unsigned)));
+  // status words: [0] error flags, [1]/[2] maxima for the packed-form bound
+  FAP_CUDA(cudaMalloc(&e->d_status, 4 * sizeof(unsigned)));
+  FAP_CUDA(cudaMemset(e->d_status, 0, 4 * sizeof(unsigned)));
   FAP_CUDA(fapk::init_minplus_kernels());
   return FAP_OK;
 }
@@ -847,6 +929,7 @@ int fap_create(int32_t n, int64_t m, const int32_t *row_offset, const int32_t *c
     fap_destroy(e.release());
     return rc;
   }
+  E->wmax = dtype == FAP_DTYPE_I32 ? (uint32_t)wmax : 0u;
   E->has_graph = true;
   *out = e.release();
   return FAP_OK;
@@ -987,12 +1070,32 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
   MpSegment s = mp_segment(A, lda, B, ldb, Bpath, ldbp, C, ldc, Cpath, ldcp, M, N, K, tiles);
   s.tile_begin = 0;
   int rc;
-  if ((rc = e->small.ensure(sizeof(MpSegment))) != FAP_OK) return rc;
-  FAP_CUDA(cudaMemcpyAsync(e->small.p, &s, sizeof(s), cudaMemcpyHostToDevice, st));
-  FAP_CUDA(fapk::launch_minplus_tiles(dtype == FAP_DTYPE_F32, Cpath != nullptr,
-                                      static_cast<const MpSegment *>(e->small.p), 1, tiles, st));
+  const bool i32 = dtype == FAP_DTYPE_I32;
+  TableBuilder tb;
+  size_t o_seg = tb.add(&s, 1);
+  fapk::MatRef refs[2] = {{A, lda, M, K}, {B, ldb, K, N}};
+  size_t o_ref = tb.add(refs, 2);
+  if ((rc = e->small.ensure(tb.bytes.size())) != FAP_OK) return rc;
+  FAP_CUDA(cudaMemcpyAsync(e->small.p, tb.bytes.data(), tb.bytes.size(), cudaMemcpyHostToDevice, st));
+  unsigned char *base = static_cast<unsigned char *>(e->small.p);
+  bool packed = false;
+  if (i32 && K > 0) {
+    // packed form only if max finite A + max finite B stays below the limit
+    const fapk::MatRef *dr = reinterpret_cast<const fapk::MatRef *>(base + o_ref);
+    FAP_CUDA(cudaMemsetAsync(e->d_status + 1, 0, 2 * sizeof(unsigned), st));
+    FAP_CUDA(fapk::launch_max_finite(dr, 1, e->d_status + 1, st));
+    FAP_CUDA(fapk::launch_max_finite(dr + 1, 1, e->d_status + 2, st));
+    unsigned mx[2] = {0, 0};
+    FAP_CUDA(cudaMemcpyAsync(mx, e->d_status + 1, sizeof(mx), cudaMemcpyDeviceToHost, st));
+    FAP_CUDA(cudaStreamSynchronize(st));
+    packed = (unsigned long long)mx[0] + mx[1] < fapk::pack_limit() &&
+             (Cpath == nullptr || K <= fapk::max_packed_k());
+  }
+  FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr,
+                                      reinterpret_cast<const MpSegment *>(base + o_seg), 1, tiles,
+                                      packed, st));
   FAP_CUDA(cudaStreamSynchronize(st));
-  return FAP_OK;
+  return check_status(e);
 }
 
 int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t *sizes,
@@ -1054,18 +1157,37 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
     tr[r] = rt;
     orr[r] = tb.add(rs.data(), rs.size());
   }
+  const bool f32 = dtype == FAP_DTYPE_F32;
+  std::vector<fapk::MatRef> refs;
+  int32_t max_size = 0;
+  for (int32_t b = 0; b < count; b++)
+    if (sizes[b] > 0) {
+      refs.push_back({D[b], ld[b], sizes[b], sizes[b]});
+      max_size = std::max(max_size, sizes[b]);
+    }
+  size_t o_ref = tb.add(refs.data(), refs.size());
   int rc;
   if ((rc = e->small.ensure(std::max<size_t>(tb.bytes.size(), 64))) != FAP_OK) return rc;
   FAP_CUDA(cudaMemcpyAsync(e->small.p, tb.bytes.data(), tb.bytes.size(), cudaMemcpyHostToDevice, st));
   unsigned char *base = static_cast<unsigned char *>(e->small.p);
-  const bool f32 = dtype == FAP_DTYPE_F32;
+  bool packed = false;
+  if (!f32) {
+    // a finite shortest distance is at most (size - 1) * the largest entry
+    FAP_CUDA(cudaMemsetAsync(e->d_status + 1, 0, sizeof(unsigned), st));
+    FAP_CUDA(fapk::launch_max_finite(reinterpret_cast<const fapk::MatRef *>(base + o_ref),
+                                     (int)refs.size(), e->d_status + 1, st));
+    unsigned mx = 0;
+    FAP_CUDA(cudaMemcpyAsync(&mx, e->d_status + 1, sizeof(mx), cudaMemcpyDeviceToHost, st));
+    FAP_CUDA(cudaStreamSynchronize(st));
+    packed = (unsigned long long)mx * (unsigned long long)std::max(max_size - 1, 1) < fapk::pack_limit();
+  }
   for (int r = 0; r < maxnb; r++) {
     FAP_CUDA(fapk::launch_fw_diag(f32, pred, reinterpret_cast<const FwDiagJob *>(base + od[r]), nd[r], st));
-    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], st));
-    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]), nr[r], tr[r], st));
+    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], packed, st));
+    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]), nr[r], tr[r], packed, st));
   }
   FAP_CUDA(cudaStreamSynchronize(st));
-  return FAP_OK;
+  return check_status(e);
 }
 
 int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *dist, int32_t *pred,
@@ -1113,6 +1235,7 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   sa.stamps = static_cast<int32_t *>(e->sssp_stamps.p);
   sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
   sa.status = e->d_status;
+  sa.maxd = nullptr;
   sa.iter_cap = 2 * e->n + 8;
   FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
   FAP_CUDA(cudaStreamSynchronize(st));

@@ -60,6 +60,15 @@ struct MpSegment {
   int32_t init_from_c; // 1: start from C/Cp (keep on ties); 0: start unreached/-1
   int32_t tiles_x;     // CTA tiles along columns
   int32_t tile_begin;  // first global CTA index of this segment
+  // Optional Floyd-Warshall override of the part's own columns (min-plus of
+  // a part's inner rows): where col_part[col] == part, the output takes
+  // F[row][col_local[col] - local0] (and Fp) instead of the product.
+  const int32_t *col_part;  // null: no override
+  const int32_t *col_local;
+  const void *F;
+  const int32_t *Fp;
+  int64_t ldf;
+  int32_t part, local0;
 };
 
 // FW diagonal-block job: close the 64x64 pivot block of one matrix.
@@ -69,6 +78,13 @@ struct FwDiagJob {
   int64_t ld;
   int32_t size;  // matrix size (rows/cols >= size are outside the matrix)
   int32_t block; // pivot block index
+};
+
+// A strided row-major matrix of 4-byte values.
+struct MatRef {
+  const void *p;
+  int64_t ld;
+  int32_t rows, cols;
 };
 
 // One batch of up to 32 SSSP sources: lane l of the batch handles source

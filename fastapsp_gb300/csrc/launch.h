@@ -9,8 +9,16 @@
 namespace fapk {
 
 // minplus.cu
+// packed = true selects the packed int32 form (uint32 distances only); the
+// caller must have checked that every finite result stays below
+// pack_limit() and, with predecessors, that every segment has K <=
+// max_packed_k().
 cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, int nseg,
-                                 int total_tiles, cudaStream_t st);
+                                 int total_tiles, bool packed, cudaStream_t st);
+// Largest finite int32 entry of the matrices, atomicMax-ed into *out.
+cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st);
+unsigned pack_limit();
+int max_packed_k();
 cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njobs,
                            cudaStream_t st);
 int minplus_tile_rows();  // CTA output tile edge (128)
@@ -33,6 +41,7 @@ struct SsspArgs {
   int32_t *stamps;            // slots * n ints, zeroed once at allocation
   int32_t *slot_epoch;        // slots ints, zeroed once at allocation
   unsigned *status;           // device status word (error flags are or-ed in)
+  unsigned *maxd;             // largest finite int32 distance written (atomicMax), may be null
   int32_t iter_cap;
 };
 size_t sssp_slot_bytes(int32_t n);  // bytes of one slot's scratch (excluding stamps)
@@ -53,8 +62,10 @@ struct BuildArgs {
   const int32_t *graph_id, *st2ed, *ed2st;
   const PartDesc *parts;
   const int64_t *row_begin;  // prefix sums of padded rows per part (nparts+1)
+  const int64_t *dec_begin;  // prefix sums of boundary rows per part (nparts+1)
   int32_t nparts;
   int64_t total_rows;
+  int64_t dec_rows;
   void *mat;                 // FW matrices arena (dist)
   int32_t *matp;             // FW matrices arena (pred), may be null
   const void *rows;          // result rows (dist), source of boundary rows

@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "launch.h"
 
@@ -61,9 +63,12 @@ __device__ __forceinline__ int list_block(int g, int skip, int fix, int nblocks)
   return (skip >= 0 && g >= skip) ? g + 1 : g;
 }
 
-template <typename T, bool PRED>
-__device__ __forceinline__ void load_chunk(MpSmem<T> &sm, int buf, const MpSegment &s,
-                                           const int rbase[2], const int cbase[2], int k0) {
+// Stages k-chunk [k0, k0+32) of A (128 rows) and B (128 columns), and of B's
+// predecessors when WITH_BP, with 4-byte cp.async; entries outside the
+// matrices are written directly as "unreached" / -1.
+template <typename T, bool WITH_BP, typename SM>
+__device__ __forceinline__ void load_chunk(SM &sm, int buf, const MpSegment &s, const int rbase[2],
+                                           const int cbase[2], int k0) {
   const int t = threadIdx.x;
   const T INF = Dist<T>::inf();
   // A: 128 rows x 32 k; consecutive threads take consecutive k of one row.
@@ -96,72 +101,106 @@ __device__ __forceinline__ void load_chunk(MpSmem<T> &sm, int buf, const MpSegme
       T *dst = &sm.B[buf][kk][j];
       if (colok && kg < s.K) {
         cp_async4(dst, static_cast<const T *>(s.B) + (int64_t)kg * s.ldb + col);
-        if (PRED) cp_async4(&sm.Bp[buf][kk][j], s.Bp + (int64_t)kg * s.ldbp + col);
+        if constexpr (WITH_BP) cp_async4(&sm.Bp[buf][kk][j], s.Bp + (int64_t)kg * s.ldbp + col);
       } else {
         *dst = INF;
-        if (PRED) sm.Bp[buf][kk][j] = -1;
+        if constexpr (WITH_BP) sm.Bp[buf][kk][j] = -1;
       }
     }
   }
 }
 
-template <typename T, bool PRED>
-__global__ void __launch_bounds__(kThreads, 1)
-    mp_tile_kernel(const MpSegment *__restrict__ segs, int nseg) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  MpSmem<T> &sm = *reinterpret_cast<MpSmem<T> *>(smem_raw);
+// Output tile geometry of one CTA, resolved from its segment.
+struct TileGeom {
+  int rbase[2], cbase[2];
+  int ty, tx;
+};
 
-  // Segment lookup (binary search on tile_begin).
-  const int tile = blockIdx.x;
+__device__ __forceinline__ const MpSegment &find_segment(const MpSegment *__restrict__ segs,
+                                                         int nseg, int tile) {
   int lo = 0, hi = nseg - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
   }
-  const MpSegment s = segs[lo];
+  return segs[lo];
+}
+
+__device__ __forceinline__ TileGeom tile_geom(const MpSegment &s, int tile) {
+  TileGeom g;
   const int local = tile - s.tile_begin;
   const int tyt = local / s.tiles_x, txt = local - tyt * s.tiles_x;
   const int nbr = (s.M + kBlk - 1) / kBlk, nbc = (s.N + kBlk - 1) / kBlk;
-  int rbase[2], cbase[2];
 #pragma unroll
-  for (int g = 0; g < 2; g++) {
-    int rb = list_block(2 * tyt + g, s.row_skip, s.row_fix, nbr);
-    int cb = list_block(2 * txt + g, s.col_skip, s.col_fix, nbc);
-    rbase[g] = rb >= 0 ? rb * kBlk : -1;
-    cbase[g] = cb >= 0 ? cb * kBlk : -1;
+  for (int i = 0; i < 2; i++) {
+    int rb = list_block(2 * tyt + i, s.row_skip, s.row_fix, nbr);
+    int cb = list_block(2 * txt + i, s.col_skip, s.col_fix, nbc);
+    g.rbase[i] = rb >= 0 ? rb * kBlk : -1;
+    g.cbase[i] = cb >= 0 ? cb * kBlk : -1;
   }
+  g.ty = threadIdx.x >> 4;
+  g.tx = threadIdx.x & 15;
+  return g;
+}
 
-  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+__device__ __forceinline__ int out_row(const TileGeom &g, int r) {
+  return g.rbase[r >> 2] < 0 ? -1 : g.rbase[r >> 2] + g.ty * 4 + (r & 3);
+}
+__device__ __forceinline__ int out_col(const TileGeom &g, int c) {
+  return g.cbase[c >> 2] < 0 ? -1 : g.cbase[c >> 2] + g.tx * 4 + (c & 3);
+}
+__device__ __forceinline__ int smem_row(const TileGeom &g, int r) { return (r >> 2) * kBlk + g.ty * 4 + (r & 3); }
+__device__ __forceinline__ int smem_col(const TileGeom &g, int c) { return (c >> 2) * kBlk + g.tx * 4 + (c & 3); }
+
+// In-part columns of the inner rows take the part's Floyd-Warshall values
+// (the decode of MysubMatDecode_path, util_Myalgorithm.h:236-247, for these
+// rows), so the min-plus epilogue writes every column once.
+__device__ __forceinline__ bool fw_column(const MpSegment &s, int col, int64_t &off) {
+  if (s.col_part == nullptr || s.col_part[col] != s.part) return false;
+  off = (int64_t)(s.col_local[col] - s.local0);
+  return true;
+}
+
+template <typename T, bool PRED>
+__device__ __forceinline__ void store_out(const MpSegment &s, int row, int col, T d, int32_t p) {
+  int64_t j;
+  if (fw_column(s, col, j)) {
+    d = static_cast<const T *>(s.F)[(int64_t)row * s.ldf + j];
+    if (PRED) p = s.Fp[(int64_t)row * s.ldf + j];
+  }
+  static_cast<T *>(s.C)[(int64_t)row * s.ldc + col] = d;
+  if (PRED) s.Cp[(int64_t)row * s.ldcp + col] = p;
+}
+
+// Wide form: add, compare, and two selects per add-min; the argmin is the
+// chunk-local k of the last strict improvement.
+template <typename T, bool PRED>
+__device__ __forceinline__ void tile_wide(MpSmem<T> &sm, const MpSegment &s, const TileGeom &g) {
   const T INF = Dist<T>::inf();
-
   T acc[8][8];
   int32_t pred[8][8];
   int arg[8][8];
 #pragma unroll
   for (int r = 0; r < 8; r++) {
-    const int rb = rbase[r >> 2];
-    const int row = rb + ty * 4 + (r & 3);
-    const bool rok = rb >= 0 && row < s.M;
+    const int row = out_row(g, r);
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-      const int cb = cbase[c >> 2];
-      const int col = cb + tx * 4 + (c & 3);
+      const int col = out_col(g, c);
       acc[r][c] = INF;
       pred[r][c] = -1;
       arg[r][c] = -1;
-      if (s.init_from_c && rok && cb >= 0 && col < s.N) {
+      if (s.init_from_c && row >= 0 && row < s.M && col >= 0 && col < s.N) {
         acc[r][c] = static_cast<const T *>(s.C)[(int64_t)row * s.ldc + col];
         if (PRED) pred[r][c] = s.Cp[(int64_t)row * s.ldcp + col];
       }
     }
   }
-
   const int nchunks = (s.K + kBK - 1) / kBK;
-  if (nchunks > 0) load_chunk<T, PRED>(sm, 0, s, rbase, cbase, 0);
+  if (nchunks > 0) load_chunk<T, PRED>(sm, 0, s, g.rbase, g.cbase, 0);
   cp_async_commit();
   for (int ch = 0; ch < nchunks; ch++) {
     const int buf = ch & 1;
-    if (ch + 1 < nchunks) load_chunk<T, PRED>(sm, buf ^ 1, s, rbase, cbase, (ch + 1) * kBK);
+    if (ch + 1 < nchunks) load_chunk<T, PRED>(sm, buf ^ 1, s, g.rbase, g.cbase, (ch + 1) * kBK);
     cp_async_commit();
     cp_async_wait_1();
     __syncthreads();
@@ -169,9 +208,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int kk = 0; kk < kBK; kk++) {
       T a[8], b[8];
 #pragma unroll
-      for (int r = 0; r < 8; r++) a[r] = sm.A[buf][(r >> 2) * kBlk + ty * 4 + (r & 3)][kk];
+      for (int r = 0; r < 8; r++) a[r] = sm.A[buf][smem_row(g, r)][kk];
 #pragma unroll
-      for (int c = 0; c < 8; c++) b[c] = sm.B[buf][kk][(c >> 2) * kBlk + tx * 4 + (c & 3)];
+      for (int c = 0; c < 8; c++) b[c] = sm.B[buf][kk][smem_col(g, c)];
 #pragma unroll
       for (int r = 0; r < 8; r++)
 #pragma unroll
@@ -189,29 +228,172 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int c = 0; c < 8; c++)
           if (arg[r][c] >= 0) {
-            pred[r][c] = sm.Bp[buf][arg[r][c]][(c >> 2) * kBlk + tx * 4 + (c & 3)];
+            pred[r][c] = sm.Bp[buf][arg[r][c]][smem_col(g, c)];
             arg[r][c] = -1;
           }
     }
     __syncthreads();
   }
   cp_async_wait_0();
-
 #pragma unroll
   for (int r = 0; r < 8; r++) {
-    const int rb = rbase[r >> 2];
-    const int row = rb + ty * 4 + (r & 3);
-    if (rb < 0 || row >= s.M) continue;
+    const int row = out_row(g, r);
+    if (row < 0 || row >= s.M) continue;
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-      const int cb = cbase[c >> 2];
-      const int col = cb + tx * 4 + (c & 3);
-      if (cb < 0 || col >= s.N) continue;
-      static_cast<T *>(s.C)[(int64_t)row * s.ldc + col] = acc[r][c];
-      if (PRED) s.Cp[(int64_t)row * s.ldcp + col] = pred[r][c];
+      const int col = out_col(g, c);
+      if (col < 0 || col >= s.N) continue;
+      store_out<T, PRED>(s, row, col, acc[r][c], pred[r][c]);
     }
   }
 }
+
+// Packed int32 form.  Keys are (min(d, kPackH) << 7) | idx: idx 0 marks the
+// value the output held before the product, idx = k+1 the candidate k.  One
+// DPX __viaddmin_u32 per add-min then yields the minimum and, on equal
+// distances, the smallest idx -- the current value first, then the first k
+// -- which is the strict-improvement, ascending-k rule of the reference.  Two
+// keys sum to at most (2 * kPackH) << 7 | 127 < 2^32, so nothing wraps, and
+// saturation at kPackH commutes with + and min, so the results are exact when
+// every finite result stays below kPackH (checked by the caller).  With
+// predecessors K <= 127, so the final idx names k* directly and the
+// predecessor is read once, in the epilogue, from B's predecessor row k*.
+constexpr unsigned kPackH = (1u << 24) - 1;
+constexpr unsigned kIdxBits = 7;
+constexpr unsigned kIdxMask = (1u << kIdxBits) - 1;
+constexpr int kMaxPackedK = 127;
+
+struct KeySmem {
+  unsigned A[2][kTile][kApad];
+  unsigned B[2][kBK][kTile];
+};
+
+// After this thread's copies of a chunk have landed, turns the elements it
+// loaded (same index mapping as load_chunk) into keys.
+__device__ __forceinline__ void keys_from_values(KeySmem &sm, int buf, int k0) {
+  const int t = threadIdx.x;
+  {
+    const int kk = t & 31;
+#pragma unroll 4
+    for (int it = 0; it < kTile / 8; it++) {
+      const int m = (t >> 5) + 8 * it;
+      sm.A[buf][m][kk] = min(sm.A[buf][m][kk], kPackH) << kIdxBits;
+    }
+  }
+  {
+    const int j = t & 127;
+#pragma unroll 4
+    for (int it = 0; it < kBK / 2; it++) {
+      const int kk = (t >> 7) + 2 * it;
+      const unsigned idx = (unsigned)((k0 + kk) & kMaxPackedK) + 1u;
+      sm.B[buf][kk][j] = (min(sm.B[buf][kk][j], kPackH) << kIdxBits) | (idx & kIdxMask);
+    }
+  }
+}
+
+template <bool PRED>
+__global__ void __launch_bounds__(kThreads, 2)
+    mp_tile_packed_kernel(const MpSegment *__restrict__ segs, int nseg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  KeySmem &sm = *reinterpret_cast<KeySmem *>(smem_raw);
+  __shared__ MpSegment seg;
+  const int tile = blockIdx.x;
+  if (threadIdx.x == 0) seg = find_segment(segs, nseg, tile);
+  __syncthreads();
+  const MpSegment &s = seg;
+  const TileGeom g = tile_geom(s, tile);
+  unsigned acc[8][8];
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int row = out_row(g, r);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const int col = out_col(g, c);
+      acc[r][c] = kPackH << kIdxBits;
+      if (s.init_from_c && row >= 0 && row < s.M && col >= 0 && col < s.N)
+        acc[r][c] = min(static_cast<const unsigned *>(s.C)[(int64_t)row * s.ldc + col], kPackH) << kIdxBits;
+    }
+  }
+  const int nchunks = (s.K + kBK - 1) / kBK;
+  if (nchunks > 0) load_chunk<uint32_t, false>(sm, 0, s, g.rbase, g.cbase, 0);
+  cp_async_commit();
+  for (int ch = 0; ch < nchunks; ch++) {
+    const int buf = ch & 1;
+    if (ch + 1 < nchunks) load_chunk<uint32_t, false>(sm, buf ^ 1, s, g.rbase, g.cbase, (ch + 1) * kBK);
+    cp_async_commit();
+    cp_async_wait_1();
+    keys_from_values(sm, buf, ch * kBK);
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < kBK; kk++) {
+      unsigned a[8], b[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++) a[r] = sm.A[buf][smem_row(g, r)][kk];
+#pragma unroll
+      for (int c = 0; c < 8; c++) b[c] = sm.B[buf][kk][smem_col(g, c)];
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+    }
+    __syncthreads();
+  }
+  cp_async_wait_0();
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int row = out_row(g, r);
+    if (row < 0 || row >= s.M) continue;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const int col = out_col(g, c);
+      if (col < 0 || col >= s.N) continue;
+      const unsigned key = acc[r][c];
+      const unsigned d = key >> kIdxBits;
+      const unsigned idx = key & kIdxMask;
+      int32_t p = -1;
+      if (PRED) {
+        if (d >= kPackH || idx == 0) {
+          if (s.init_from_c) p = s.Cp[(int64_t)row * s.ldcp + col];
+        } else {
+          p = s.Bp[(int64_t)(idx - 1) * s.ldbp + col];
+        }
+      }
+      store_out<uint32_t, PRED>(s, row, col, d >= kPackH ? Dist<uint32_t>::inf() : d, p);
+    }
+  }
+}
+
+template <typename T, bool PRED>
+__global__ void __launch_bounds__(kThreads, 1)
+    mp_tile_kernel(const MpSegment *__restrict__ segs, int nseg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MpSmem<T> &sm = *reinterpret_cast<MpSmem<T> *>(smem_raw);
+  // The segment descriptor stays in shared memory (read where needed) so that
+  // the accumulators, argmins and predecessors keep the registers.
+  __shared__ MpSegment seg;
+  const int tile = blockIdx.x;
+  if (threadIdx.x == 0) seg = find_segment(segs, nseg, tile);
+  __syncthreads();
+  const MpSegment &s = seg;
+  const TileGeom g = tile_geom(s, tile);
+  tile_wide<T, PRED>(sm, s, g);
+}
+
+// Largest finite int32 value (< 2^30) of a strided matrix, atomicMax-ed into
+// *out; CTAs (blockIdx.x) row-stride over matrix blockIdx.y.
+__global__ void max_finite_kernel(const MatRef *__restrict__ mats, unsigned *out) {
+  const MatRef mr = mats[blockIdx.y];
+  const unsigned *D = static_cast<const unsigned *>(mr.p);
+  unsigned m = 0;
+  for (int r = blockIdx.x; r < mr.rows; r += gridDim.x)
+    for (int c = threadIdx.x; c < mr.cols; c += blockDim.x) {
+      const unsigned v = D[(int64_t)r * mr.ld + c];
+      if (v < Dist<uint32_t>::inf()) m = max(m, v);
+    }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 
 // Closes the 64x64 pivot block of one matrix per CTA: sequential k inside the
 // block, 16 elements per thread, one barrier per k.  Row k and column k do not
@@ -273,21 +455,45 @@ cudaError_t launch_mp_t(const MpSegment *d_segs, int nseg, int total_tiles, cuda
   return cudaGetLastError();
 }
 
+template <bool PRED>
+cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int total_tiles, cudaStream_t st) {
+  if (total_tiles <= 0 || nseg <= 0) return cudaSuccess;
+  mp_tile_packed_kernel<PRED><<<total_tiles, kThreads, sizeof(KeySmem), st>>>(d_segs, nseg);
+  return cudaGetLastError();
+}
+
 template <typename T, bool PRED>
 cudaError_t set_mp_attr() {
   return cudaFuncSetAttribute(mp_tile_kernel<T, PRED>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MpSmem<T>));
 }
 
+template <bool PRED>
+cudaError_t set_packed_attr() {
+  return cudaFuncSetAttribute(mp_tile_packed_kernel<PRED>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(KeySmem));
+}
+
 }  // namespace
 
 cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, int nseg,
-                                 int total_tiles, cudaStream_t st) {
+                                 int total_tiles, bool packed, cudaStream_t st) {
   if (f32) return pred ? launch_mp_t<float, true>(d_segs, nseg, total_tiles, st)
                        : launch_mp_t<float, false>(d_segs, nseg, total_tiles, st);
+  if (packed) return pred ? launch_packed_t<true>(d_segs, nseg, total_tiles, st)
+                          : launch_packed_t<false>(d_segs, nseg, total_tiles, st);
   return pred ? launch_mp_t<uint32_t, true>(d_segs, nseg, total_tiles, st)
               : launch_mp_t<uint32_t, false>(d_segs, nseg, total_tiles, st);
 }
+
+cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st) {
+  if (nmats <= 0) return cudaSuccess;
+  max_finite_kernel<<<dim3(32, nmats), 256, 0, st>>>(d_mats, out);
+  return cudaGetLastError();
+}
+
+unsigned pack_limit() { return kPackH; }
+int max_packed_k() { return kMaxPackedK; }
 
 cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njobs,
                            cudaStream_t st) {
@@ -307,7 +513,9 @@ cudaError_t init_minplus_kernels() {
   if ((e = set_mp_attr<float, true>()) != cudaSuccess) return e;
   if ((e = set_mp_attr<float, false>()) != cudaSuccess) return e;
   if ((e = set_mp_attr<uint32_t, true>()) != cudaSuccess) return e;
-  return set_mp_attr<uint32_t, false>();
+  if ((e = set_mp_attr<uint32_t, false>()) != cudaSuccess) return e;
+  if ((e = set_packed_attr<true>()) != cudaSuccess) return e;
+  return set_packed_attr<false>();
 }
 
 int minplus_tile_rows() { return kTile; }

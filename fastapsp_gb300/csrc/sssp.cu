@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(kSsspThreads)
   // Stamps persist across launches; each slot continues its own epoch count
   // so that no stamp left by an earlier launch can equal a new epoch.
   int epoch = a.slot_epoch[blockIdx.x];
+  unsigned local_max = 0;  // largest finite distance this thread wrote
   for (int b = blockIdx.x; b < a.nbatches; b += gridDim.x) {
     const int cnt = a.batches[b].count;
     const int my_src = lane < cnt ? a.batches[b].src[lane] : -1;
@@ -156,6 +157,7 @@ __global__ void __launch_bounds__(kSsspThreads)
             }
           }
         }
+        if (lane < cnt && dv < INF) local_max = max(local_max, dv);
         tile_d[vi][lane] = dv;
         tile_p[vi][lane] = p;
       }
@@ -172,6 +174,10 @@ __global__ void __launch_bounds__(kSsspThreads)
     }
   }
   if (threadIdx.x == 0) a.slot_epoch[blockIdx.x] = epoch;
+  if (a.maxd != nullptr) {
+    local_max = __reduce_max_sync(0xffffffffu, local_max);
+    if (lane == 0 && local_max) atomicMax(a.maxd, local_max);
+  }
 }
 
 }  // namespace

@@ -89,13 +89,16 @@ __global__ void __launch_bounds__(128) build_kernel(BuildArgs a) {
   }
 }
 
+// Scatter of the closed matrix into the boundary rows at the part's columns
+// (MysubMatDecode_path for rows [0, bdy)); the inner rows get their part
+// columns from the min-plus epilogue.  One CTA per boundary row.
 template <typename T, bool PRED>
 __global__ void __launch_bounds__(128) decode_kernel(BuildArgs a, T *rows, int32_t *rowsp) {
   const int64_t r = blockIdx.x;
-  const int p = find_part(a.row_begin, a.nparts, r);
+  const int p = find_part(a.dec_begin, a.nparts, r);
   const PartDesc pd = a.parts[p];
-  const int i = (int)(r - a.row_begin[p]);
-  if (i >= pd.sub) return;
+  const int i = (int)(r - a.dec_begin[p]);
+  if (i >= pd.bdy) return;
   const T *D = static_cast<const T *>(a.mat) + pd.mat_off + (int64_t)i * pd.ld;
   const int32_t *P = PRED ? a.matp + pd.mat_off + (int64_t)i * pd.ld : nullptr;
   T *dst = rows + pd.row_off + (int64_t)i * a.ldr;
@@ -124,8 +127,8 @@ cudaError_t launch_build(bool f32, bool pred, const BuildArgs &a, cudaStream_t s
 
 cudaError_t launch_decode(bool f32, bool pred, const BuildArgs &a, void *rows, int32_t *rowsp,
                           cudaStream_t st) {
-  if (a.total_rows <= 0) return cudaSuccess;
-  const unsigned grid = (unsigned)a.total_rows;
+  if (a.dec_rows <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)a.dec_rows;
   if (f32) {
     if (pred) decode_kernel<float, true><<<grid, 128, 0, st>>>(a, (float *)rows, rowsp);
     else decode_kernel<float, false><<<grid, 128, 0, st>>>(a, (float *)rows, rowsp);
