@@ -61,6 +61,8 @@ SIGNATURES = {
     "fap_backward": (C.c_int, [_p, _p, _i32, _p, _p, _p, _p, _p]),
     "fap_backward_dense": (C.c_int, [_p, _i32, _p, _p, _p, _p, _i32, _p, _p, _p, _p, _p]),
     "fap_addmin_peak": (C.c_int, [_p, _i32, C.POINTER(C.c_double)]),
+    "fap_sssp_noalloc": (C.c_int, [_i32, _i32, _i64, _p, _p, _p, _p, _p, _p, _p, _i32, _p, _p, _i64,
+                                   _p]),
 }
 
 _lib = None

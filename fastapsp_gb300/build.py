@@ -21,7 +21,8 @@ LIB = PKG / "libfastapsp.so"
 EXAMPLE = PKG / "fap_single_node"
 INCLUDE = PKG.parent / "include"
 
-CUDA_SOURCES = ["minplus.cu", "sssp.cu", "transform.cu", "adjoint.cu", "probe.cu", "engine.cu"]
+CUDA_SOURCES = ["minplus.cu", "sssp.cu", "transform.cu", "adjoint.cu", "probe.cu", "engine.cu",
+                "noalloc.cu"]
 CXX_SOURCES = ["host_prep.cpp", "fap_graph.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -208,6 +208,33 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes,
                        int32_t num_pairs, const int32_t *b, const int32_t *s,
                        const int32_t *t, const float *g, void *stream);
 
+/* Allocation-free batched SSSP (no counterpart in the reference).  For
+ * callers that cannot call cudaMalloc -- code running under an allocator it
+ * does not own (a framework's memory pool or arena), request paths of
+ * plugins whose host forbids allocation, real-time paths that cannot take an
+ * allocation's latency or implicit synchronization.  Same kernel and same
+ * results as fap_sssp, but without an engine handle: the caller passes the
+ * graph in device memory it owns -- the out-edge CSR (row_offset[n+1],
+ * col_val[m], weight[m]) and, when pred is not NULL, the in-edge CSR -- with
+ * 4-byte weights (float for FAP_DTYPE_F32, int32 for FAP_DTYPE_I32), the
+ * sources in host memory, and device rows dist/pred of num_sources x ld.
+ * All scratch comes from one static device array of FAP_NOALLOC_SCRATCH_BYTES
+ * (64 MiB) that every GPU loading this library holds until exit; graphs whose
+ * scratch does not fit (about n > 450,000 vertices) are rejected with
+ * FAP_ERR_RANGE.  No allocation: neither cudaMalloc/cudaFree nor an
+ * allocating library call.  The first call on a device looks up the array's
+ * device address (so make that first call before any stream capture).  Calls
+ * share the array: each call clears what must start at zero, and calls that
+ * overlap on the GPU race, so serialize them.  The call synchronizes
+ * `stream` before returning its status. */
+#define FAP_NOALLOC_SCRATCH_BYTES (64u << 20)
+int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m,
+                     const int32_t *row_offset, const int32_t *col_val,
+                     const void *weight, const int32_t *in_row_offset,
+                     const int32_t *in_col_val, const void *in_weight,
+                     const int32_t *sources, int32_t num_sources, void *dist,
+                     int32_t *pred, int64_t ld, void *stream);
+
 /* ---- diagnostics -------------------------------------------------------- */
 
 /* Add-min operations per second that the GPU issues from registers alone
