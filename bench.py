@@ -349,6 +349,214 @@ def run_reference(args):
     return res
 
 
+def _device_solve_rate(fap, torch, g, K, dtype, steps, warmup, mode=None):
+    """Device-resident solve of a whole graph: (ms per solve, engine, dist, pred)."""
+    mode = fap.MODE_BATCHED if mode is None else mode
+    gid, cut = fap.partition(g.row_offset, g.col_val, K)
+    eng = fap.Engine(g.n, g.row_offset, g.col_val, g.weight, K, graph_id=gid, dtype=dtype)
+    tdt = torch.int32 if dtype == fap.DTYPE_I32 else torch.float32
+    dist = torch.empty((g.n, g.n), dtype=tdt, device="cuda")
+    pred = torch.empty((g.n, g.n), dtype=torch.int32, device="cuda")
+    flush = torch.empty(64 << 20, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        eng.solve(dist, pred, mode, stream=stream.cuda_stream)
+    times = []
+    for _ in range(steps):
+        flush.fill_(1)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.solve(dist, pred, mode, stream=stream.cuda_stream)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return statistics.mean(times), eng, dist, pred, gid, cut
+
+
+def run_c1(args):
+    """128x128 grid (spanning tree + p=0.6 edges), unweighted, K=16, int32,
+    full solve(); distances checked bit for bit against the oracle's
+    Dijkstra (the reference's dijkstra_path) on sampled rows."""
+    import torch
+
+    import fastapsp_gb300 as fap
+    from fastapsp_gb300 import graphs
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    g = graphs.grid_graph()
+    ms, eng, dist, pred, gid, cut = _device_solve_rate(fap, torch, g, 16, fap.DTYPE_I32, args.steps, args.warmup)
+    plain_ms, *_ = _device_solve_rate(fap, torch, g, 16, fap.DTYPE_I32, 2, 1, mode=fap.MODE_PLAIN)
+    mapping = eng.mapping()
+    rows = np.random.default_rng(0).choice(g.n, size=64, replace=False)
+    d = dist[torch.from_numpy(rows).cuda()].cpu().numpy()
+    exact = True
+    for i, r in enumerate(rows):
+        rd, _ = oracle.dijkstra_path(int(mapping[r]), g.row_offset, g.col_val, g.weight)
+        ref = np.where(rd >= 1e8, 1 << 30, rd).astype(np.int64)
+        exact = exact and np.array_equal(d[i].astype(np.int64), ref)
+    return {"config": "c1", "metric": METRIC, "value": g.n * g.n / (ms / 1e3), "unit": UNIT,
+            "ms_per_step": ms, "dtype": "int32", "n": g.n, "m": g.m, "K": 16, "edge_cut": cut,
+            "plain_ms": plain_ms, "batched_speedup": plain_ms / ms,
+            "parity": f"64 sampled rows bit-exact vs the reference's Dijkstra: {exact}",
+            "phase_ms": eng.last_times()}
+
+
+def run_c3(args):
+    """512 dense int32 instances, sizes log-uniform in [32, 2048], 5% edges,
+    weights U[1,100]: all instances in one launch per FW phase (batched) vs
+    one launch sequence per instance."""
+    import torch
+
+    import fastapsp_gb300 as fap
+    from fastapsp_gb300 import graphs
+
+    mats = graphs.dense_instances()
+    ctx = fap.Context(0)
+    work = float(sum(float(m.shape[0]) ** 3 for m in mats))
+    host = [torch.from_numpy(m) for m in mats]
+    dev = [h.cuda() for h in host]
+    preds = [torch.where(h < (1 << 30), torch.arange(h.shape[0], dtype=torch.int32)[:, None],
+                         torch.full((1, 1), -1, dtype=torch.int32)).contiguous().cuda() for h in host]
+    pinit = [p.clone() for p in preds]
+    stream = torch.cuda.current_stream()
+
+    def reset():
+        for d_, h in zip(dev, host):
+            d_.copy_(h, non_blocking=True)
+        for p_, p0 in zip(preds, pinit):
+            p_.copy_(p0)
+
+    def timed(fn, steps):
+        out = []
+        for _ in range(steps):
+            reset()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            out.append(a.elapsed_time(b))
+        return statistics.mean(out)
+
+    batched = lambda: ctx.floyd_batched(1, dev, preds, stream=stream.cuda_stream)  # noqa: E731
+
+    def per_instance():
+        for d_, p_ in zip(dev, preds):
+            ctx.floyd_batched(1, [d_], [p_], stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        reset()
+        batched()
+    ms_b = timed(batched, args.steps)
+    per_instance()
+    ms_p = timed(per_instance, max(1, args.steps // 2))
+    peak = ctx.addmin_peak(0)
+    ctx.close()
+    return {"config": "c3", "metric": "add-min Gop/s (batched Floyd-Warshall, 512 instances)",
+            "value": work / (ms_b / 1e3) / 1e9, "unit": "Gaddmin/s", "ms_per_step": ms_b,
+            "per_instance_ms": ms_p, "batched_speedup": ms_p / ms_b, "dtype": "int32",
+            "instances": len(mats), "addmins": work, "frac_of_dpx_peak": work / (ms_b / 1e3) / peak}
+
+
+def run_c4(args):
+    """Road-like FP32 graph, 114,599 vertices, K=128, full batched APSP;
+    error against FP64 Dijkstra on 4,096 sampled sources."""
+    import torch
+
+    import fastapsp_gb300 as fap
+    from fastapsp_gb300 import graphs
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    g = graphs.road_like()
+    ms, eng, dist, pred, gid, cut = _device_solve_rate(fap, torch, g, 128, fap.DTYPE_F32, args.steps, args.warmup)
+    phase = eng.last_times()
+    mapping = eng.mapping()
+    inv = np.empty_like(mapping)
+    inv[mapping] = np.arange(g.n)
+    srcs = np.random.default_rng(4).choice(g.n, size=args.c4_sources, replace=False)
+    rows = torch.from_numpy(inv[srcs].astype(np.int64)).cuda()
+    d = dist[rows].cpu().numpy()
+    eng.close()
+    del dist, pred
+    torch.cuda.empty_cache()
+    from concurrent.futures import ThreadPoolExecutor
+
+    def err(i):
+        d64 = oracle.dijkstra_f64(int(srcs[i]), g.row_offset, g.col_val, g.weight)
+        f = d64 < 1e299
+        if not np.array_equal(f, d[i] < 1e8):
+            return float("inf")
+        return float(np.max(np.abs(d[i][f] - d64[f]) / np.maximum(d64[f], 1e-30)))
+
+    with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+        errs = list(ex.map(err, range(len(srcs))))
+    return {"config": "c4", "metric": METRIC, "value": g.n * g.n / (ms / 1e3), "unit": UNIT,
+            "ms_per_step": ms, "dtype": "f32", "n": g.n, "m": g.m, "K": 128, "edge_cut": cut,
+            "sampled_sources": len(srcs), "max_rel_err_vs_fp64": max(errs),
+            "mean_of_row_max_rel_err": float(np.mean(errs)), "phase_ms": phase}
+
+
+def run_c5(args):
+    """256 random 4-regular digraphs (n U[256,1024], FP32 w U(0.5,2)): batched
+    FW with predecessors (forward), loss = sum of D[s,t] over 10,000 pairs,
+    adjoint onto the weights (backward); backward/forward time ratio."""
+    import torch
+
+    import fastapsp_gb300 as fap
+    from fastapsp_gb300 import graphs
+
+    gs = graphs.regular_digraphs()
+    rng = np.random.default_rng(5)
+    npairs = 10000
+    b = rng.integers(0, len(gs), size=npairs)
+    s = np.array([rng.integers(0, gs[i].n) for i in b])
+    t = np.array([rng.integers(0, gs[i].n) for i in b])
+    ctx = fap.Context(0)
+    host = []
+    for g in gs:
+        W = np.full((g.n, g.n), 1e8, np.float32)
+        src = np.repeat(np.arange(g.n), np.diff(g.row_offset))
+        W[src, g.col_val] = g.weight
+        np.fill_diagonal(W, 0)
+        P = np.where(W < 1e8, np.arange(g.n)[:, None], -1).astype(np.int32)
+        host.append((torch.from_numpy(W), torch.from_numpy(P)))
+    D = [h[0].cuda() for h in host]
+    P = [h[1].cuda() for h in host]
+    dW = [torch.zeros_like(d_) for d_ in D]
+    bt, st_, tt = (torch.from_numpy(x.astype(np.int32)).cuda() for x in (b, s, t))
+    gg = torch.ones(npairs, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    fw, bw = [], []
+    for i in range(args.warmup + args.steps):
+        for d_, p_, h in zip(D, P, host):
+            d_.copy_(h[0])
+            p_.copy_(h[1])
+        for w_ in dW:
+            w_.zero_()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        ctx.floyd_batched(0, D, P, stream=stream.cuda_stream)
+        e1.record(stream)
+        ctx.backward_dense(P, dW, bt, st_, tt, gg, stream=stream.cuda_stream)
+        e2.record(stream)
+        e2.synchronize()
+        if i >= args.warmup:
+            fw.append(e0.elapsed_time(e1))
+            bw.append(e1.elapsed_time(e2))
+    ctx.close()
+    work = float(sum(float(g.n) ** 3 for g in gs))
+    return {"config": "c5", "metric": "backward / forward time", "value": statistics.mean(bw) / statistics.mean(fw),
+            "unit": "ratio", "forward_ms": statistics.mean(fw), "backward_ms": statistics.mean(bw),
+            "forward_gaddmin_s": work / (statistics.mean(fw) / 1e3) / 1e9, "graphs": len(gs),
+            "pairs": npairs, "dtype": "f32"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,6 +569,9 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT, help="vertices (profiling cases only)")
     ap.add_argument("--K", type=int, default=K_DEFAULT, help="parts (profiling cases only)")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
+                    help="c2 (default) is the headline workload; the others print their own line")
+    ap.add_argument("--c4-sources", type=int, default=4096)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -369,6 +580,13 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)))
+        return
+    if args.config != "c2":
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        fn = {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config]
+        print(json.dumps(fn(args)))
         return
 
     if world > 1:

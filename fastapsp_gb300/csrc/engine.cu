@@ -127,6 +127,7 @@ struct Plan {
   int max_sub = 0;      // largest part of the plan
   int max_mp_k = 0;     // largest min-plus K (boundary count) of the plan
   int pack = -1;        // packed int32 form: -1 undecided, 0 no, 1 yes
+  int sssp_lanes = 32;  // sources per SSSP batch
   // graph (batched mode)
   cudaGraphExec_t exec = nullptr;
   ~Plan() {
@@ -343,9 +344,10 @@ int build_plan(fap_engine *e, Plan &pl) {
       int p = pl.parts[idx];
       int sub = e->ver_num[p], bdy = e->bdy_num[p], start = e->ver_offset[p];
       int64_t roff = pl.row_offs[idx];
-      for (int b0 = 0; b0 < bdy; b0 += 32) {
+      const int L = pl.sssp_lanes;
+      for (int b0 = 0; b0 < bdy; b0 += L) {
         SsspBatch sb{};
-        sb.count = std::min(32, bdy - b0);
+        sb.count = std::min(L, bdy - b0);
         for (int l = 0; l < sb.count; l++) {
           sb.src[l] = e->st2ed[start + b0 + l];
           sb.row_off[l] = roff + (int64_t)(b0 + l) * n;
@@ -533,6 +535,7 @@ struct Issuer {
     sa.status = e->d_status;
     sa.maxd = e->f32() ? nullptr : e->d_status + 1;
     sa.iter_cap = 2 * e->n + 8;
+    sa.lanes = pl.sssp_lanes;
     FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
     return FAP_OK;
   }
@@ -630,12 +633,16 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   int rc;
   // work buffers
   size_t fw_elems = 0;
-  int max_batches = 0;
+  int64_t batches32 = 0, sources = 0;
   for (int p : parts) {
     size_t ld = align_up((size_t)e->ver_num[p], (size_t)fapk::fw_block());
     fw_elems += ld * ld;
-    max_batches += (e->bdy_num[p] + 31) / 32;
+    batches32 += (e->bdy_num[p] + 31) / 32;
+    sources += e->bdy_num[p];
   }
+  const int lanes = fapk::sssp_lanes_for(sources, batches32, e->sm_count);
+  int max_batches = 0;
+  for (int p : parts) max_batches += (e->bdy_num[p] + lanes - 1) / lanes;
   if ((rc = e->fw_d.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
   if (pred && (rc = e->fw_p.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
   int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e));
@@ -651,6 +658,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     np->parts = parts;
     np->row_offs = offs;
     np->sig = buffer_signature(e);
+    np->sssp_lanes = lanes;
     if ((rc = build_plan(e, *np)) != FAP_OK) return rc;
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
@@ -1202,10 +1210,11 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   std::lock_guard<std::mutex> lk(e->mu);
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
+  const int lanes = fapk::sssp_lanes_for(num_sources, (num_sources + 31) / 32, e->sm_count);
   std::vector<SsspBatch> batches;
-  for (int b0 = 0; b0 < num_sources; b0 += 32) {
+  for (int b0 = 0; b0 < num_sources; b0 += lanes) {
     SsspBatch sb{};
-    sb.count = std::min(32, num_sources - b0);
+    sb.count = std::min(lanes, num_sources - b0);
     for (int l = 0; l < sb.count; l++) {
       sb.src[l] = sources[b0 + l];
       sb.row_off[l] = (int64_t)(b0 + l) * ld;
@@ -1237,6 +1246,7 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   sa.status = e->d_status;
   sa.maxd = nullptr;
   sa.iter_cap = 2 * e->n + 8;
+  sa.lanes = lanes;
   FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);

@@ -43,8 +43,11 @@ struct SsspArgs {
   unsigned *status;           // device status word (error flags are or-ed in)
   unsigned *maxd;             // largest finite int32 distance written (atomicMax), may be null
   int32_t iter_cap;
+  int32_t lanes;              // sources per batch: 16 or 32 (batches hold <= lanes)
 };
-size_t sssp_slot_bytes(int32_t n);  // bytes of one slot's scratch (excluding stamps)
+size_t sssp_slot_bytes(int32_t n);
+// Batch width to use given the number of 32-source batches the work needs.
+int sssp_lanes_for(int64_t sources_total, int64_t batches32, int sm_count);  // bytes of one slot's scratch (excluding stamps)
 int sssp_threads();
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st);
 

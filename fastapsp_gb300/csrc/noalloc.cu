@@ -157,6 +157,7 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   sa.status = reinterpret_cast<unsigned *>(base + o_status);
   sa.maxd = nullptr;
   sa.iter_cap = 2 * n + 8;
+  sa.lanes = 32;
   if ((ce = fapk::launch_sssp(dtype == FAP_DTYPE_F32, sa, st)) != cudaSuccess)
     return set_error(FAP_ERR_CUDA, std::string("fap_sssp_noalloc: ") + cudaGetErrorString(ce));
   unsigned status = 0;

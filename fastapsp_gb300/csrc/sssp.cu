@@ -44,10 +44,15 @@ __host__ __device__ inline size_t slot_bytes(int32_t n) {
   return (b + 255) & ~(size_t)255;
 }
 
-template <typename T, bool PRED>
+// LANES sources per batch (16 or 32): a warp relaxes 32 / LANES frontier
+// vertices at once, each for LANES sources.
+template <typename T, bool PRED, int LANES>
 __global__ void __launch_bounds__(kSsspThreads)
     sssp_lanes_kernel(SsspArgs a) {
+  constexpr int VPW = 32 / LANES;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / LANES, sl = lane % LANES;
+  const unsigned group_mask = LANES == 32 ? 0xffffffffu : (0xffffu << (16 * sub));
   const int nwarps = blockDim.x >> 5;
   const int32_t n = a.n;
   unsigned char *base = static_cast<unsigned char *>(a.scratch) + (size_t)blockIdx.x * slot_bytes(n);
@@ -70,21 +75,21 @@ __global__ void __launch_bounds__(kSsspThreads)
   unsigned local_max = 0;  // largest finite distance this thread wrote
   for (int b = blockIdx.x; b < a.nbatches; b += gridDim.x) {
     const int cnt = a.batches[b].count;
-    const int my_src = lane < cnt ? a.batches[b].src[lane] : -1;
-    for (size_t i = threadIdx.x; i < (size_t)n * 32; i += blockDim.x) dvm[i] = INF;
+    const int my_src = sl < cnt ? a.batches[b].src[sl] : -1;
+    for (size_t i = threadIdx.x; i < (size_t)n * LANES; i += blockDim.x) dvm[i] = INF;
     if (threadIdx.x == 0) {
       s_count[0] = 0;
       s_count[1] = 0;
     }
     epoch++;
     __syncthreads();
-    if (threadIdx.x < 32 && my_src >= 0 && my_src < n) {
-      dvm[(size_t)my_src * 32 + lane] = 0u;
+    if (threadIdx.x < LANES && my_src >= 0 && my_src < n) {
+      dvm[(size_t)my_src * LANES + sl] = 0u;
       if (atomicExch(&stamp[my_src], epoch) != epoch) {
         int pos = atomicAdd(&s_count[0], 1);
         fr[0][pos] = my_src;
       }
-    } else if (threadIdx.x < 32 && my_src >= n) {
+    } else if (threadIdx.x < LANES && my_src >= n) {
       atomicOr(a.status, kErrBadInput);
     }
     __syncthreads();
@@ -101,20 +106,29 @@ __global__ void __launch_bounds__(kSsspThreads)
       epoch++;
       const int32_t *F = fr[cur];
       int32_t *N = fr[cur ^ 1];
-      for (int idx = warp; idx < f; idx += nwarps) {
-        const int u = __ldcg(&F[idx]);
-        const unsigned du = __ldcg(&dvm[(size_t)u * 32 + lane]);
-        const int e1 = a.ro[u + 1];
-        for (int e = a.ro[u]; e < e1; e++) {
-          const int v = a.col[e];
+      for (int fb = warp * VPW; fb < f; fb += nwarps * VPW) {
+        const int idx = fb + sub;
+        const bool has = idx < f;
+        const int u = has ? __ldcg(&F[idx]) : 0;
+        const unsigned du = has ? __ldcg(&dvm[(size_t)u * LANES + sl]) : INF;
+        const int e0 = has ? a.ro[u] : 0;
+        const int deg = has ? a.ro[u + 1] - e0 : 0;
+        int maxdeg = deg;
+        if (VPW == 2) maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
+        for (int e = 0; e < maxdeg; e++) {
           bool imp = false;
-          if (du < INF) {
-            const unsigned cand =
-                Dist<T>::bits(Dist<T>::add(Dist<T>::from_bits(du), Dist<T>::from_bits(wb[e])));
-            unsigned *p = &dvm[(size_t)v * 32 + lane];
-            if (cand < __ldcg(p)) imp = cand < atomicMin(p, cand);
+          int v = 0;
+          if (e < deg) {
+            v = a.col[e0 + e];
+            if (du < INF) {
+              const unsigned cand =
+                  Dist<T>::bits(Dist<T>::add(Dist<T>::from_bits(du), Dist<T>::from_bits(wb[e0 + e])));
+              unsigned *p = &dvm[(size_t)v * LANES + sl];
+              if (cand < __ldcg(p)) imp = cand < atomicMin(p, cand);
+            }
           }
-          if (__any_sync(0xffffffffu, imp) && lane == 0) {
+          const unsigned bal = __ballot_sync(0xffffffffu, imp) & group_mask;
+          if (bal != 0u && sl == 0) {
             if (atomicExch(&stamp[v], epoch) != epoch) {
               const int pos = atomicAdd(&s_count[cur ^ 1], 1);
               N[pos] = v;
@@ -130,13 +144,13 @@ __global__ void __launch_bounds__(kSsspThreads)
 
     // Predecessors and transposed output, 32 vertices at a time.
     for (int v0 = 0; v0 < n; v0 += 32) {
-      for (int vi = warp; vi < 32; vi += nwarps) {
+      for (int vi = warp * VPW + sub; vi < 32; vi += nwarps * VPW) {
         const int v = v0 + vi;
         unsigned dv = INF;
         int32_t p = -1;
         if (v < n) {
-          dv = __ldcg(&dvm[(size_t)v * 32 + lane]);
-          if (PRED && lane < cnt && dv < INF) {
+          dv = __ldcg(&dvm[(size_t)v * LANES + sl]);
+          if (PRED && sl < cnt && dv < INF) {
             if (v == my_src) {
               p = v;
             } else {
@@ -144,7 +158,7 @@ __global__ void __launch_bounds__(kSsspThreads)
               int bu = -1;
               for (int e = a.iro[v]; e < a.iro[v + 1]; e++) {
                 const int u = a.icol[e];
-                const unsigned du = __ldcg(&dvm[(size_t)u * 32 + lane]);
+                const unsigned du = __ldcg(&dvm[(size_t)u * LANES + sl]);
                 if (du >= INF) continue;
                 const unsigned s =
                     Dist<T>::bits(Dist<T>::add(Dist<T>::from_bits(du), Dist<T>::from_bits(iwb[e])));
@@ -157,9 +171,9 @@ __global__ void __launch_bounds__(kSsspThreads)
             }
           }
         }
-        if (lane < cnt && dv < INF) local_max = max(local_max, dv);
-        tile_d[vi][lane] = dv;
-        tile_p[vi][lane] = p;
+        if (sl < cnt && dv < INF) local_max = max(local_max, dv);
+        tile_d[vi][sl] = dv;
+        tile_p[vi][sl] = p;
       }
       __syncthreads();
       const int col = v0 + lane;
@@ -180,6 +194,12 @@ __global__ void __launch_bounds__(kSsspThreads)
   }
 }
 
+template <typename T, bool PRED>
+void launch_t(const SsspArgs &a, cudaStream_t st) {
+  if (a.lanes == 16) sssp_lanes_kernel<T, PRED, 16><<<a.slots, kSsspThreads, 0, st>>>(a);
+  else sssp_lanes_kernel<T, PRED, 32><<<a.slots, kSsspThreads, 0, st>>>(a);
+}
+
 }  // namespace
 
 size_t sssp_slot_bytes(int32_t n) { return slot_bytes(n); }
@@ -187,15 +207,21 @@ int sssp_threads() { return kSsspThreads; }
 
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st) {
   if (a.nbatches <= 0 || a.slots <= 0) return cudaSuccess;
+  if (a.lanes != 16 && a.lanes != 32) return cudaErrorInvalidValue;
   const bool pred = a.pred != nullptr;
   if (f32) {
-    if (pred) sssp_lanes_kernel<float, true><<<a.slots, kSsspThreads, 0, st>>>(a);
-    else sssp_lanes_kernel<float, false><<<a.slots, kSsspThreads, 0, st>>>(a);
+    if (pred) launch_t<float, true>(a, st); else launch_t<float, false>(a, st);
   } else {
-    if (pred) sssp_lanes_kernel<uint32_t, true><<<a.slots, kSsspThreads, 0, st>>>(a);
-    else sssp_lanes_kernel<uint32_t, false><<<a.slots, kSsspThreads, 0, st>>>(a);
+    if (pred) launch_t<uint32_t, true>(a, st); else launch_t<uint32_t, false>(a, st);
   }
   return cudaGetLastError();
+}
+
+int sssp_lanes_for(int64_t sources_total, int64_t batches32, int sm_count) {
+  // Half-warp batches double the CTA count and the frontier vertices a warp
+  // relaxes at once; worth it while 32-source batches leave SMs idle.
+  (void)sources_total;
+  return batches32 < 2LL * sm_count ? 16 : 32;
 }
 
 }  // namespace fapk
