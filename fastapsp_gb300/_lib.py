@@ -25,6 +25,9 @@ DTYPE_I32 = 1
 MODE_PLAIN = 0
 MODE_BATCHED = 1
 MAXVALUE_F32 = 1e8
+OPT_SSSP_FP64 = 1
+OPT_SSSP_DELTA = 2
+OPT_AUTOTUNE = 3
 INF_I32 = 1 << 30
 
 _i32 = C.c_int32
@@ -61,6 +64,8 @@ SIGNATURES = {
     "fap_backward": (C.c_int, [_p, _p, _i32, _p, _p, _p, _p, _p]),
     "fap_backward_dense": (C.c_int, [_p, _i32, _p, _p, _p, _p, _i32, _p, _p, _p, _p, _p]),
     "fap_addmin_peak": (C.c_int, [_p, _i32, C.POINTER(C.c_double)]),
+    "fap_set_option": (C.c_int, [_p, _i32, C.c_double]),
+    "fap_get_option": (C.c_int, [_p, _i32, C.POINTER(C.c_double)]),
     "fap_sssp_noalloc": (C.c_int, [_i32, _i32, _i64, _p, _p, _p, _p, _p, _p, _p, _i32, _p, _p, _i64,
                                    _p]),
 }

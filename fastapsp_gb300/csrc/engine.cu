@@ -162,6 +162,13 @@ struct fap_engine {
   std::vector<int32_t> ro, col, graph_id, st2ed, ed2st, ver_num, ver_offset, bdy_num, bdy_offset;
   std::vector<float> w;
   uint32_t wmax = 0;  // largest weight (int32 mode)
+  double wmean = 1.0; // mean weight (sets the SSSP near-far step)
+  // SSSP options (fap_set_option)
+  int sssp_fp64 = 0;       // FP32 engines: search in FP64
+  double sssp_delta = 0;   // near-far threshold step; 0 = auto (tuned on first solve)
+  int autotune = 1;        // tune the SSSP step on the first solve
+  double delta_try = 0;    // step under trial while tuning
+  double tuned_ms = 0;     // SSSP time of the chosen step during tuning
   // device graph
   int32_t *d_ro = nullptr, *d_col = nullptr, *d_iro = nullptr, *d_icol = nullptr;
   int32_t *d_gid = nullptr, *d_st2ed = nullptr, *d_ed2st = nullptr;
@@ -185,10 +192,18 @@ struct fap_engine {
 
 namespace {
 
+double sssp_delta_of(const fap_engine *e) {
+  if (e->delta_try > 0) return e->delta_try;
+  if (e->sssp_delta > 0) return e->sssp_delta;
+  // a few mean edge weights per near-far step (at least one unit for int32)
+  double d = 8.0 * e->wmean;
+  return e->f32() ? std::max(d, 1e-30) : std::max(1.0, std::floor(d));
+}
+
 int max_sssp_slots(fap_engine *e) {
   // Two 512-thread CTAs per SM, bounded by a 16 GiB scratch budget.
   int slots = std::max(1, 2 * e->sm_count);
-  size_t per = fapk::sssp_slot_bytes(e->n) + (size_t)e->n * 4;
+  size_t per = fapk::sssp_slot_bytes(e->n) + (size_t)e->n * 8;
   size_t budget = (size_t)16 << 30;
   slots = (int)std::max<size_t>(1, std::min<size_t>((size_t)slots, budget / std::max<size_t>(per, 1)));
   return slots;
@@ -198,9 +213,9 @@ int ensure_sssp_scratch(fap_engine *e, int slots) {
   if (slots <= e->sssp_slots_alloc) return FAP_OK;
   int st;
   if ((st = e->sssp_scratch.ensure(fapk::sssp_slot_bytes(e->n) * slots)) != FAP_OK) return st;
-  if ((st = e->sssp_stamps.ensure((size_t)e->n * 4 * slots)) != FAP_OK) return st;
+  if ((st = e->sssp_stamps.ensure((size_t)e->n * 8 * slots)) != FAP_OK) return st;
   if ((st = e->sssp_epoch.ensure((size_t)4 * slots)) != FAP_OK) return st;
-  FAP_CUDA(cudaMemset(e->sssp_stamps.p, 0, (size_t)e->n * 4 * slots));
+  FAP_CUDA(cudaMemset(e->sssp_stamps.p, 0, (size_t)e->n * 8 * slots));
   FAP_CUDA(cudaMemset(e->sssp_epoch.p, 0, (size_t)4 * slots));
   e->sssp_slots_alloc = slots;
   return FAP_OK;
@@ -534,8 +549,10 @@ struct Issuer {
     sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
     sa.status = e->d_status;
     sa.maxd = e->f32() ? nullptr : e->d_status + 1;
-    sa.iter_cap = 2 * e->n + 8;
+    sa.iter_cap = 8 * e->n + 64;
     sa.lanes = pl.sssp_lanes;
+    sa.acc64 = e->f32() && e->sssp_fp64;
+    sa.delta = sssp_delta_of(e);
     FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
     return FAP_OK;
   }
@@ -571,6 +588,55 @@ struct Issuer {
     return FAP_OK;
   }
 };
+
+int check_status(fap_engine *e);
+std::vector<const void *> buffer_signature(const fap_engine *e);
+
+// SSSP step autotuner: times the plan's SSSP phase (every group) with a few
+// near-far steps -- multiples of the mean edge weight, and plain frontier
+// Bellman-Ford -- and keeps the fastest.  The step only orders the work, so
+// every candidate produces the same rows.  Runs once per engine, on the first
+// run of a plan, when the step was left automatic.
+int autotune_sssp(fap_engine *e, Plan &pl, cudaStream_t st) {
+  const double unit = e->f32() ? e->wmean : std::max(1.0, e->wmean);
+  const double factors[] = {2.0, 8.0, 32.0, 128.0, 0.0};
+  double best = 0, best_ms = 1e300;
+  cudaEvent_t t0 = e->ev_sync[0], t1 = e->ev_sync[1];
+  cudaEvent_t a, b;
+  FAP_CUDA(cudaEventCreate(&a));
+  FAP_CUDA(cudaEventCreate(&b));
+  (void)t0;
+  (void)t1;
+  int rc = FAP_OK;
+  for (double f : factors) {
+    double d = f > 0 ? f * unit : fapk::kSsspNoDelta;
+    if (!e->f32()) d = std::max(1.0, std::floor(d));
+    e->delta_try = d;
+    Issuer is{e, pl, st, false};
+    if (cudaEventRecord(a, st) != cudaSuccess) { rc = FAP_ERR_CUDA; break; }
+    for (size_t g = 0; g < pl.groups.size() && rc == FAP_OK; g++) rc = is.sssp(g);
+    if (rc != FAP_OK) break;
+    if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) {
+      rc = set_error(FAP_ERR_CUDA, "autotune: event failed");
+      break;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = d;
+    }
+  }
+  e->delta_try = 0;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc != FAP_OK) return rc;
+  if ((rc = check_status(e)) != FAP_OK) return rc;
+  e->sssp_delta = best;
+  e->tuned_ms = best_ms;
+  pl.sig = buffer_signature(e);
+  return FAP_OK;
+}
 
 // Decides the packed int32 form for a plan on its first run: runs every
 // group's SSSP, reads back the largest finite SSSP distance, and checks the
@@ -613,8 +679,13 @@ int check_status(fap_engine *e) {
 }
 
 std::vector<const void *> buffer_signature(const fap_engine *e) {
+  double d = sssp_delta_of(e);
+  intptr_t dbits;
+  std::memcpy(&dbits, &d, sizeof(dbits));
   return {e->fw_d.p, e->fw_p.p, e->sssp_scratch.p, e->sssp_stamps.p, e->sssp_epoch.p,
-          reinterpret_cast<const void *>((intptr_t)e->sssp_slots_alloc)};
+          reinterpret_cast<const void *>((intptr_t)e->sssp_slots_alloc),
+          reinterpret_cast<const void *>((intptr_t)e->sssp_fp64),
+          reinterpret_cast<const void *>(dbits)};
 }
 
 Plan *find_plan(fap_engine *e, int mode, void *dist, int32_t *pred,
@@ -640,7 +711,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     batches32 += (e->bdy_num[p] + 31) / 32;
     sources += e->bdy_num[p];
   }
-  const int lanes = fapk::sssp_lanes_for(sources, batches32, e->sm_count);
+  const int lanes = (e->f32() && e->sssp_fp64) ? 16 : fapk::sssp_lanes_for(sources, batches32, e->sm_count);
   int max_batches = 0;
   for (int p : parts) max_batches += (e->bdy_num[p] + lanes - 1) / lanes;
   if ((rc = e->fw_d.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
@@ -663,7 +734,10 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
   }
-  if (pl->pack < 0) return first_run(e, *pl, st);
+  if (pl->pack < 0) {
+    if (e->autotune && e->sssp_delta <= 0 && (rc = autotune_sssp(e, *pl, st)) != FAP_OK) return rc;
+    return first_run(e, *pl, st);
+  }
   if (mode == FAP_MODE_BATCHED) {
     if (!pl->exec) {
       cudaGraph_t graph = nullptr;
@@ -743,6 +817,7 @@ int init_device(fap_engine *e, int device) {
   FAP_CUDA(cudaMalloc(&e->d_status, 4 * sizeof(unsigned)));
   FAP_CUDA(cudaMemset(e->d_status, 0, 4 * sizeof(unsigned)));
   FAP_CUDA(fapk::init_minplus_kernels());
+  FAP_CUDA(fapk::init_sssp_kernels());
   return FAP_OK;
 }
 
@@ -938,6 +1013,11 @@ int fap_create(int32_t n, int64_t m, const int32_t *row_offset, const int32_t *c
     return rc;
   }
   E->wmax = dtype == FAP_DTYPE_I32 ? (uint32_t)wmax : 0u;
+  {
+    double sum = 0;
+    for (int64_t j = 0; j < m; j++) sum += weight[j];
+    E->wmean = m > 0 ? std::max(sum / (double)m, 1e-30) : 1.0;
+  }
   E->has_graph = true;
   *out = e.release();
   return FAP_OK;
@@ -1210,7 +1290,9 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   std::lock_guard<std::mutex> lk(e->mu);
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
-  const int lanes = fapk::sssp_lanes_for(num_sources, (num_sources + 31) / 32, e->sm_count);
+  const int lanes = (e->f32() && e->sssp_fp64)
+                        ? 16
+                        : fapk::sssp_lanes_for(num_sources, (num_sources + 31) / 32, e->sm_count);
   std::vector<SsspBatch> batches;
   for (int b0 = 0; b0 < num_sources; b0 += lanes) {
     SsspBatch sb{};
@@ -1245,8 +1327,10 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
   sa.status = e->d_status;
   sa.maxd = nullptr;
-  sa.iter_cap = 2 * e->n + 8;
+  sa.iter_cap = 8 * e->n + 64;
   sa.lanes = lanes;
+  sa.acc64 = e->f32() && e->sssp_fp64;
+  sa.delta = sssp_delta_of(e);
   FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);
@@ -1298,6 +1382,35 @@ int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s) {
   DeviceGuard dg(e->device);
   FAP_CUDA(fapk::measure_addmin_peak(mode, e->sm_count, ops_per_s));
   return FAP_OK;
+}
+
+int fap_set_option(fap_engine *e, int32_t option, double value) {
+  if (!e) return set_error(FAP_ERR_INVALID, "null engine");
+  std::lock_guard<std::mutex> lk(e->mu);
+  switch (option) {
+    case FAP_OPT_SSSP_FP64:
+      e->sssp_fp64 = value != 0.0 ? 1 : 0;
+      return FAP_OK;
+    case FAP_OPT_SSSP_DELTA:
+      if (!(value >= 0.0) || std::isinf(value)) return set_error(FAP_ERR_INVALID, "SSSP delta must be >= 0");
+      e->sssp_delta = (!e->f32() && value > 0.0) ? std::max(1.0, std::floor(value)) : value;
+      return FAP_OK;
+    case FAP_OPT_AUTOTUNE:
+      e->autotune = value != 0.0 ? 1 : 0;
+      return FAP_OK;
+    default:
+      return set_error(FAP_ERR_INVALID, "unknown option");
+  }
+}
+
+int fap_get_option(const fap_engine *e, int32_t option, double *value) {
+  if (!e || !value) return set_error(FAP_ERR_INVALID, "null argument");
+  switch (option) {
+    case FAP_OPT_SSSP_FP64: *value = e->sssp_fp64; return FAP_OK;
+    case FAP_OPT_SSSP_DELTA: *value = sssp_delta_of(e); return FAP_OK;
+    case FAP_OPT_AUTOTUNE: *value = e->autotune; return FAP_OK;
+    default: return set_error(FAP_ERR_INVALID, "unknown option");
+  }
 }
 
 }  // extern "C"

@@ -38,13 +38,18 @@ struct SsspArgs {
   int32_t *pred;              // may be null
   void *scratch;              // per-slot scratch, sssp_slot_bytes(n) each
   int32_t slots;              // number of CTAs (= scratch slots)
-  int32_t *stamps;            // slots * n ints, zeroed once at allocation
+  int32_t *stamps;            // slots * 2n ints (near and far stamps), zeroed at allocation
   int32_t *slot_epoch;        // slots ints, zeroed once at allocation
   unsigned *status;           // device status word (error flags are or-ed in)
   unsigned *maxd;             // largest finite int32 distance written (atomicMax), may be null
-  int32_t iter_cap;
+  int32_t iter_cap;           // steps (near-frontier sweeps + far splits) per batch
   int32_t lanes;              // sources per batch: 16 or 32 (batches hold <= lanes)
+  int32_t acc64;              // FP32 weights searched in FP64 (lanes must be 16)
+  double delta;               // near-far threshold step (> 0; huge = plain Bellman-Ford)
 };
+// delta value that puts every vertex in the near frontier (plain frontier BF)
+constexpr double kSsspNoDelta = 2147483647.0;
+cudaError_t init_sssp_kernels();
 size_t sssp_slot_bytes(int32_t n);
 // Batch width to use given the number of 32-source batches the work needs.
 int sssp_lanes_for(int64_t sources_total, int64_t batches32, int sm_count);  // bytes of one slot's scratch (excluding stamps)

@@ -88,13 +88,13 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   if (num_sources == 0) return FAP_OK;
 
   // Layout of the static array: status words | batch list | slot epochs |
-  // stamps (slots x n) | per-slot scratch (slots x sssp_slot_bytes(n)).
+  // stamps (slots x 2n) | per-slot scratch (slots x sssp_slot_bytes(n)).
   const int nb = (num_sources + 31) / 32;
   const size_t o_status = 0;
   const size_t o_batches = 256;
   const size_t batch_bytes = round_up((size_t)nb * sizeof(fapk::SsspBatch), 256);
   const size_t o_epoch = o_batches + batch_bytes;
-  const size_t per_slot = fapk::sssp_slot_bytes(n) + round_up((size_t)n * 4, 256);
+  const size_t per_slot = fapk::sssp_slot_bytes(n) + round_up((size_t)n * 8, 256);
   if (o_epoch + 256 + per_slot > kNoAllocBytes)
     return set_error(FAP_ERR_RANGE,
                      "fap_sssp_noalloc: n = " + std::to_string(n) + " with " +
@@ -110,7 +110,7 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   if (rc != FAP_OK) return rc;
   // Largest slot count (one CTA per slot, at most two per SM) that fits.
   auto end_of = [&](size_t k) {
-    return o_epoch + round_up(k * 4, 256) + round_up(k * (size_t)n * 4, 256) +
+    return o_epoch + round_up(k * 4, 256) + round_up(k * (size_t)n * 8, 256) +
            k * fapk::sssp_slot_bytes(n);
   };
   int slots = std::min(nb, std::max(1, 2 * sms));
@@ -118,7 +118,7 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   if (end_of((size_t)slots) > kNoAllocBytes)
     return set_error(FAP_ERR_RANGE, "fap_sssp_noalloc: graph too large for the static scratch");
   const size_t o_stamps = o_epoch + round_up((size_t)slots * 4, 256);
-  const size_t o_slots = o_stamps + round_up((size_t)slots * n * 4, 256);
+  const size_t o_slots = o_stamps + round_up((size_t)slots * n * 8, 256);
 
   std::vector<fapk::SsspBatch> batches(nb);
   for (int b = 0; b < nb; b++) {
@@ -134,7 +134,7 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   // Clear what must start at zero: status, slot epochs and stamps.
   if ((ce = cudaMemsetAsync(base + o_status, 0, 256, st)) != cudaSuccess ||
       (ce = cudaMemsetAsync(base + o_epoch, 0, (size_t)slots * 4, st)) != cudaSuccess ||
-      (ce = cudaMemsetAsync(base + o_stamps, 0, (size_t)slots * n * 4, st)) != cudaSuccess ||
+      (ce = cudaMemsetAsync(base + o_stamps, 0, (size_t)slots * n * 8, st)) != cudaSuccess ||
       (ce = cudaMemcpyAsync(base + o_batches, batches.data(), (size_t)nb * sizeof(fapk::SsspBatch),
                             cudaMemcpyHostToDevice, st)) != cudaSuccess)
     return set_error(FAP_ERR_CUDA, std::string("fap_sssp_noalloc: ") + cudaGetErrorString(ce));
@@ -156,8 +156,10 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   sa.slot_epoch = reinterpret_cast<int32_t *>(base + o_epoch);
   sa.status = reinterpret_cast<unsigned *>(base + o_status);
   sa.maxd = nullptr;
-  sa.iter_cap = 2 * n + 8;
+  sa.iter_cap = 8 * n + 64;
   sa.lanes = 32;
+  sa.acc64 = 0;
+  sa.delta = fapk::kSsspNoDelta;
   if ((ce = fapk::launch_sssp(dtype == FAP_DTYPE_F32, sa, st)) != cudaSuccess)
     return set_error(FAP_ERR_CUDA, std::string("fap_sssp_noalloc: ") + cudaGetErrorString(ce));
   unsigned status = 0;

@@ -146,6 +146,14 @@ class Engine:
         check(lib().fap_last_times(self._h, t), "fap_last_times")
         return dict(zip(["sssp", "floyd", "min_plus", "data", "total"], list(t)))
 
+    def set_option(self, option: int, value: float):
+        check(lib().fap_set_option(self._h, int(option), float(value)), "fap_set_option")
+
+    def get_option(self, option: int) -> float:
+        v = C.c_double(0)
+        check(lib().fap_get_option(self._h, int(option), C.byref(v)), "fap_get_option")
+        return float(v.value)
+
     def sssp(self, sources, dist, pred=None, ld=None, stream=None):
         src = _i32(sources)
         check(lib().fap_sssp(self._h, ptr(src), int(src.shape[0]), ptr(dist), ptr(pred),

@@ -147,6 +147,26 @@ int fap_solve_part(fap_engine *e, int32_t part, void *dist, int32_t *pred,
 int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode,
               void *stream);
 
+/* Engine options (no reference counterpart).
+ *   FAP_OPT_SSSP_FP64  (FP32 engines) 1 = run the boundary SSSP in FP64 and
+ *                      round once, which keeps FP32 results within an ulp or
+ *                      two of FP64 shortest distances on long paths; 0
+ *                      (default) = FP32 arithmetic, bit-identical to the
+ *                      reference's FP32 Dijkstra.
+ *   FAP_OPT_SSSP_DELTA near-far threshold step of the SSSP in distance units
+ *                      (0 = automatic).  Changes speed only, never results.
+ *   FAP_OPT_AUTOTUNE   1 (default) = while the step is automatic, the first
+ *                      run of a solve times the SSSP phase with a few steps
+ *                      (multiples of the mean edge weight, and plain
+ *                      Bellman-Ford) and keeps the fastest; fap_get_option
+ *                      then reports the chosen step.  0 = 8 x the mean weight.
+ * Setting an option takes effect from the next solve. */
+#define FAP_OPT_SSSP_FP64 1
+#define FAP_OPT_SSSP_DELTA 2
+#define FAP_OPT_AUTOTUNE 3
+int fap_set_option(fap_engine *e, int32_t option, double value);
+int fap_get_option(const fap_engine *e, int32_t option, double *value);
+
 /* Device time of the last solve's phases in milliseconds:
  * [sssp, floyd, min_plus, data, total] (the getTime* counters of
  * fap/fap.cpp:622-639, measured with CUDA events). */
@@ -220,7 +240,7 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes,
  * sources in host memory, and device rows dist/pred of num_sources x ld.
  * All scratch comes from one static device array of FAP_NOALLOC_SCRATCH_BYTES
  * (64 MiB) that every GPU loading this library holds until exit; graphs whose
- * scratch does not fit (about n > 450,000 vertices) are rejected with
+ * scratch does not fit (about n > 440,000 vertices) are rejected with
  * FAP_ERR_RANGE.  No allocation: neither cudaMalloc/cudaFree nor an
  * allocating library call.  The first call on a device looks up the array's
  * device address (so make that first call before any stream capture).  Calls

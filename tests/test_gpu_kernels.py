@@ -131,3 +131,73 @@ def test_sssp_matches_dijkstra_bit_for_bit(gpu, oracle_lib, kind):
         rd, rp = oracle_lib.dijkstra_path(int(s), g.row_offset, g.col_val, g.weight)
         assert np.array_equal(d[i].view(np.int32), rd.view(np.int32)), f"row {i}"
         assert np.array_equal(p[i], rp), f"pred row {i}"
+
+
+@pytest.mark.parametrize("kind", ["grid", "road_f32"])
+def test_sssp_result_independent_of_near_far_step(gpu, oracle_lib, kind):
+    """The near-far step only orders the work: any step gives the reference
+    Dijkstra's distances and predecessors."""
+    if kind == "grid":
+        g, dtype = graphs.grid_graph(30, 30, seed=2), gpu.DTYPE_I32
+    else:
+        g, dtype = graphs.road_like(3000, seed=5), gpu.DTYPE_F32
+    src = np.random.default_rng(3).choice(g.n, size=40, replace=False).astype(np.int32)
+    dt = torch.int32 if dtype == gpu.DTYPE_I32 else torch.float32
+    outs = []
+    with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=dtype) as eng:
+        for delta in (1e-3 if dtype == gpu.DTYPE_F32 else 1, 0.0, 1e9):
+            eng.set_option(gpu._lib.OPT_SSSP_DELTA, delta)
+            d = torch.empty((len(src), g.n), dtype=dt, device="cuda")
+            p = torch.empty((len(src), g.n), dtype=torch.int32, device="cuda")
+            eng.sssp(src, d, p)
+            torch.cuda.synchronize()
+            outs.append((d.cpu().numpy(), p.cpu().numpy()))
+    for d, p in outs[1:]:
+        assert np.array_equal(d, outs[0][0]) and np.array_equal(p, outs[0][1])
+    for i, s in enumerate(src):
+        rd, rp = oracle_lib.dijkstra_path(int(s), g.row_offset, g.col_val, g.weight)
+        assert np.array_equal(as_oracle(outs[0][0][i]).view(np.int32), rd.view(np.int32))
+        assert np.array_equal(outs[0][1][i], rp)
+
+
+def test_sssp_fp64_option_rounds_once(gpu, oracle_lib):
+    """With FP64 search the FP32 output is the FP64 distance rounded once."""
+    g = graphs.road_like(4000, seed=8)
+    src = np.random.default_rng(2).choice(g.n, size=33, replace=False).astype(np.int32)
+    with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=gpu.DTYPE_F32) as eng:
+        eng.set_option(gpu._lib.OPT_SSSP_FP64, 1)
+        d = torch.empty((len(src), g.n), dtype=torch.float32, device="cuda")
+        p = torch.empty((len(src), g.n), dtype=torch.int32, device="cuda")
+        eng.sssp(src, d, p)
+        torch.cuda.synchronize()
+        d = d.cpu().numpy()
+        p = p.cpu().numpy()
+    for i, s in enumerate(src):
+        d64 = oracle_lib.dijkstra_f64(int(s), g.row_offset, g.col_val, g.weight)
+        f = d64 < 1e299
+        assert np.array_equal(f, d[i] < 1e8)
+        assert np.array_equal(d[i][f], d64[f].astype(np.float32))  # round-to-nearest of FP64
+    n = g.n
+    check_pred_tight(d.astype(np.float64), p, src, n, g.row_offset, g.col_val, g.weight, rtol=1e-6)
+
+
+def test_engine_fp64_sssp_option_meets_1e6_on_road_graph(gpu, oracle_lib):
+    g = graphs.road_like(6000, seed=12)
+    K = 8
+    with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, K, dtype=gpu.DTYPE_F32) as eng:
+        eng.set_option(gpu._lib.OPT_SSSP_FP64, 1)
+        n = g.n
+        d = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        p = torch.empty((n, n), dtype=torch.int32, device="cuda")
+        eng.solve(d, p, gpu.MODE_BATCHED)
+        torch.cuda.synchronize()
+        mapping = eng.mapping()
+        rows = np.arange(0, n, 97)
+        dd = d[torch.from_numpy(rows).cuda()].cpu().numpy()
+    worst = 0.0
+    for i, r in enumerate(rows):
+        d64 = oracle_lib.dijkstra_f64(int(mapping[r]), g.row_offset, g.col_val, g.weight)
+        f = d64 < 1e299
+        assert np.array_equal(f, dd[i] < 1e8)
+        worst = max(worst, float(np.max(np.abs(dd[i][f] - d64[f]) / np.maximum(d64[f], 1e-30))))
+    assert worst <= 1e-6, worst
