@@ -53,6 +53,7 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_2() { asm volatile("cp.async.wait_group 2;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
 // Block index of list entry g when block `skip` is left out of 0..nblocks-1.
@@ -161,15 +162,46 @@ __device__ __forceinline__ bool fw_column(const MpSegment &s, int col, int64_t &
   return true;
 }
 
+// Whether the output rows allow 16-byte stores of 4 consecutive columns.
+template <bool PRED>
+__device__ __forceinline__ bool vec_stores_ok(const MpSegment &s) {
+  bool ok = (s.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(s.C) & 15) == 0;
+  if (PRED) ok = ok && (s.ldcp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Cp) & 15) == 0;
+  return ok;
+}
+
+// Stores the 4 outputs of columns col0..col0+3 of `row` (those < N), after
+// the part-column override; one 16-byte store per array when all 4 are in
+// range and the rows are aligned.
 template <typename T, bool PRED>
-__device__ __forceinline__ void store_out(const MpSegment &s, int row, int col, T d, int32_t p) {
-  int64_t j;
-  if (fw_column(s, col, j)) {
-    d = static_cast<const T *>(s.F)[(int64_t)row * s.ldf + j];
-    if (PRED) p = s.Fp[(int64_t)row * s.ldf + j];
+__device__ __forceinline__ void store_quad(const MpSegment &s, int row, int col0, T d[4],
+                                           int32_t p[4], bool vec) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    int64_t j;
+    if (col0 + q < s.N && fw_column(s, col0 + q, j)) {
+      d[q] = static_cast<const T *>(s.F)[(int64_t)row * s.ldf + j];
+      if (PRED) p[q] = s.Fp[(int64_t)row * s.ldf + j];
+    }
   }
-  static_cast<T *>(s.C)[(int64_t)row * s.ldc + col] = d;
-  if (PRED) s.Cp[(int64_t)row * s.ldcp + col] = p;
+  T *crow = static_cast<T *>(s.C) + (int64_t)row * s.ldc;
+  int32_t *prow = PRED ? s.Cp + (int64_t)row * s.ldcp : nullptr;
+  if (vec && col0 + 3 < s.N) {
+    uint4 dv;
+    dv.x = Dist<T>::bits(d[0]);
+    dv.y = Dist<T>::bits(d[1]);
+    dv.z = Dist<T>::bits(d[2]);
+    dv.w = Dist<T>::bits(d[3]);
+    *reinterpret_cast<uint4 *>(crow + col0) = dv;
+    if (PRED) *reinterpret_cast<int4 *>(prow + col0) = make_int4(p[0], p[1], p[2], p[3]);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    if (col0 + q < s.N) {
+      crow[col0 + q] = d[q];
+      if (PRED) prow[col0 + q] = p[q];
+    }
 }
 
 // Wide form: add, compare, and two selects per add-min; the argmin is the
@@ -235,15 +267,24 @@ __device__ __forceinline__ void tile_wide(MpSmem<T> &sm, const MpSegment &s, con
     __syncthreads();
   }
   cp_async_wait_0();
+  const bool vec = vec_stores_ok<PRED>(s);
 #pragma unroll
   for (int r = 0; r < 8; r++) {
     const int row = out_row(g, r);
     if (row < 0 || row >= s.M) continue;
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const int col = out_col(g, c);
-      if (col < 0 || col >= s.N) continue;
-      store_out<T, PRED>(s, row, col, acc[r][c], pred[r][c]);
+    for (int h = 0; h < 2; h++) {
+      if (g.cbase[h] < 0) continue;
+      const int col0 = g.cbase[h] + g.tx * 4;
+      if (col0 >= s.N) continue;
+      T d[4];
+      int32_t p[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        d[q] = acc[r][h * 4 + q];
+        p[q] = pred[r][h * 4 + q];
+      }
+      store_quad<T, PRED>(s, row, col0, d, p, vec);
     }
   }
 }
@@ -263,10 +304,34 @@ constexpr unsigned kIdxBits = 7;
 constexpr unsigned kIdxMask = (1u << kIdxBits) - 1;
 constexpr int kMaxPackedK = 127;
 
+constexpr int kStagedBpRows = 64;  // B-predecessor rows kept in shared memory
+
 struct KeySmem {
   unsigned A[2][kTile][kApad];
   unsigned B[2][kBK][kTile];
+  int32_t Bp[kStagedBpRows][kTile];  // rows k of B's predecessors when K <= 64
+  int32_t fwcol[kTile];  // FW-matrix column of each tile column of the own part, else -1
 };
+
+// Stages B-predecessor rows [k0, k0+32) into Bp[k0..] (not double-buffered:
+// every row of the whole K range keeps its own slot), same thread mapping as
+// the B loads of load_chunk.
+__device__ __forceinline__ void load_bp_rows(KeySmem &sm, const MpSegment &s, const int cbase[2],
+                                             int k0) {
+  const int t = threadIdx.x;
+  const int j = t & 127;
+  const int cb = cbase[j >> 6];
+  const int col = cb + (j & 63);
+  const bool colok = cb >= 0 && col < s.N;
+#pragma unroll 4
+  for (int it = 0; it < kBK / 2; it++) {
+    const int kk = (t >> 7) + 2 * it;
+    const int kg = k0 + kk;
+    int32_t *dst = &sm.Bp[kg][j];
+    if (colok && kg < s.K) cp_async4(dst, s.Bp + (int64_t)kg * s.ldbp + col);
+    else *dst = -1;
+  }
+}
 
 // After this thread's copies of a chunk have landed, turns the elements it
 // loaded (same index mapping as load_chunk) into keys.
@@ -314,14 +379,32 @@ __global__ void __launch_bounds__(kThreads, 2)
         acc[r][c] = min(static_cast<const unsigned *>(s.C)[(int64_t)row * s.ldc + col], kPackH) << kIdxBits;
     }
   }
+  // Own-part columns of the tile (min-plus of inner rows): FW column or -1.
+  if (threadIdx.x < kTile) {
+    const int j = threadIdx.x;
+    const int cb = g.cbase[j >> 6];
+    const int col = cb + (j & 63);
+    int32_t f = -1;
+    if (s.col_part != nullptr && cb >= 0 && col < s.N && s.col_part[col] == s.part)
+      f = s.col_local[col] - s.local0;
+    sm.fwcol[j] = f;
+  }
   const int nchunks = (s.K + kBK - 1) / kBK;
+  // B's predecessor rows (K <= 64) go to shared memory in their own cp.async
+  // group, waited for only before the epilogue, so their latency hides under
+  // the DPX loop.  Groups: chunk 0 | predecessor rows | chunk 1 | ...
+  const bool stage_bp = PRED && s.K <= kStagedBpRows;
   if (nchunks > 0) load_chunk<uint32_t, false>(sm, 0, s, g.rbase, g.cbase, 0);
   cp_async_commit();
+  if (stage_bp) {
+    for (int k0 = 0; k0 < s.K; k0 += kBK) load_bp_rows(sm, s, g.cbase, k0);
+    cp_async_commit();
+  }
   for (int ch = 0; ch < nchunks; ch++) {
     const int buf = ch & 1;
     if (ch + 1 < nchunks) load_chunk<uint32_t, false>(sm, buf ^ 1, s, g.rbase, g.cbase, (ch + 1) * kBK);
     cp_async_commit();
-    cp_async_wait_1();
+    if (ch == 0 && stage_bp) cp_async_wait_2(); else cp_async_wait_1();
     keys_from_values(sm, buf, ch * kBK);
     __syncthreads();
 #pragma unroll 2
@@ -339,26 +422,71 @@ __global__ void __launch_bounds__(kThreads, 2)
     __syncthreads();
   }
   cp_async_wait_0();
+  __syncthreads();  // staged predecessor rows and column flags visible to every thread
+  if (s.init_from_c) {
+    // Accumulating product (FW phases): idx 0 means the output kept its value,
+    // so neither its distance nor its predecessor is stored again.
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const int row = out_row(g, r);
+      if (row < 0 || row >= s.M) continue;
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        const int col = out_col(g, c);
+        if (col < 0 || col >= s.N) continue;
+        const unsigned key = acc[r][c];
+        const unsigned idx = key & kIdxMask;
+        if (idx == 0) continue;
+        static_cast<unsigned *>(s.C)[(int64_t)row * s.ldc + col] = key >> kIdxBits;
+        if (PRED)
+          s.Cp[(int64_t)row * s.ldcp + col] =
+              stage_bp ? sm.Bp[idx - 1][smem_col(g, c)] : s.Bp[(int64_t)(idx - 1) * s.ldbp + col];
+      }
+    }
+    return;
+  }
+  const bool vec = vec_stores_ok<PRED>(s);
 #pragma unroll
   for (int r = 0; r < 8; r++) {
     const int row = out_row(g, r);
     if (row < 0 || row >= s.M) continue;
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const int col = out_col(g, c);
-      if (col < 0 || col >= s.N) continue;
-      const unsigned key = acc[r][c];
-      const unsigned d = key >> kIdxBits;
-      const unsigned idx = key & kIdxMask;
-      int32_t p = -1;
-      if (PRED) {
-        if (d >= kPackH || idx == 0) {
-          if (s.init_from_c) p = s.Cp[(int64_t)row * s.ldcp + col];
-        } else {
-          p = s.Bp[(int64_t)(idx - 1) * s.ldbp + col];
+    for (int h = 0; h < 2; h++) {
+      if (g.cbase[h] < 0) continue;
+      const int col0 = g.cbase[h] + g.tx * 4;
+      if (col0 >= s.N) continue;
+      unsigned d[4];
+      int32_t p[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int col = col0 + q;
+        const int sc = smem_col(g, h * 4 + q);
+        const unsigned key = acc[r][h * 4 + q];
+        const unsigned dist = key >> kIdxBits;
+        const unsigned idx = key & kIdxMask;
+        d[q] = dist >= kPackH ? Dist<uint32_t>::inf() : dist;
+        p[q] = -1;
+        if (PRED && col < s.N && dist < kPackH && idx != 0)
+          p[q] = stage_bp ? sm.Bp[idx - 1][sc] : s.Bp[(int64_t)(idx - 1) * s.ldbp + col];
+        const int fj = sm.fwcol[sc];
+        if (fj >= 0) {  // own-part column: the FW value (the decode of this row)
+          d[q] = static_cast<const unsigned *>(s.F)[(int64_t)row * s.ldf + fj];
+          if (PRED) p[q] = s.Fp[(int64_t)row * s.ldf + fj];
         }
       }
-      store_out<uint32_t, PRED>(s, row, col, d >= kPackH ? Dist<uint32_t>::inf() : d, p);
+      unsigned *crow = static_cast<unsigned *>(s.C) + (int64_t)row * s.ldc;
+      int32_t *prow = PRED ? s.Cp + (int64_t)row * s.ldcp : nullptr;
+      if (vec && col0 + 3 < s.N) {
+        *reinterpret_cast<uint4 *>(crow + col0) = make_uint4(d[0], d[1], d[2], d[3]);
+        if (PRED) *reinterpret_cast<int4 *>(prow + col0) = make_int4(p[0], p[1], p[2], p[3]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (col0 + q < s.N) {
+            crow[col0 + q] = d[q];
+            if (PRED) prow[col0 + q] = p[q];
+          }
+      }
     }
   }
 }
