@@ -187,6 +187,7 @@ def run_ours(args, rank, world, local_rank):
 
     # phase times (device events inside the captured graph)
     ph = {k: statistics.mean(p[k] for p in phase) for k in phase[0]}
+    sssp_stats = eng.sssp_stats()
     # roofline of the dominant kernel (min-plus) against the add-min issue peak
     peak_dpx = eng_ctx_peak(fap, dev, 0)
     peak_arg = eng_ctx_peak(fap, dev, 2)
@@ -281,6 +282,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline_sssp": {"bound": "hbm", "achieved": sssp_gbs, "peak": hbm, "unit": "GB/s",
                           "frac": sssp_gbs / hbm, "algorithmic_bytes": sssp_bytes, "peak_source": peak_src},
         "phase_ms": ph,
+        "sssp_stats": sssp_stats,
         "plain_form": {"ms_per_step": plain_ms, "batched_speedup": plain_ms / ms_per_step},
         "clocks": clocks,
     }
@@ -409,7 +411,8 @@ def run_c1(args):
             "ms_per_step": ms, "dtype": "int32", "n": g.n, "m": g.m, "K": 16, "edge_cut": cut,
             "plain_ms": plain_ms, "batched_speedup": plain_ms / ms,
             "parity": f"64 sampled rows bit-exact vs the reference's Dijkstra: {exact}",
-            "phase_ms": eng.last_times()}
+            "phase_ms": eng.last_times(), "sssp_stats": eng.sssp_stats(),
+            "sssp_delta": eng.get_option(fap._lib.OPT_SSSP_DELTA)}
 
 
 def run_c3(args):
@@ -487,6 +490,8 @@ def run_c4(args):
         fap, torch, g, 128, fap.DTYPE_F32, args.steps, args.warmup,
         options={fap._lib.OPT_SSSP_FP64: fp64})
     phase = eng.last_times()
+    stats = eng.sssp_stats()
+    delta = eng.get_option(fap._lib.OPT_SSSP_DELTA)
     mapping = eng.mapping()
     inv = np.empty_like(mapping)
     inv[mapping] = np.arange(g.n)
@@ -511,7 +516,8 @@ def run_c4(args):
             "ms_per_step": ms, "dtype": "f32", "n": g.n, "m": g.m, "K": 128, "edge_cut": cut,
             "sssp": "FP64 search, rounded once" if fp64 else "FP32 (reference arithmetic)",
             "sampled_sources": len(srcs), "max_rel_err_vs_fp64": max(errs),
-            "mean_of_row_max_rel_err": float(np.mean(errs)), "phase_ms": phase}
+            "mean_of_row_max_rel_err": float(np.mean(errs)), "phase_ms": phase,
+            "sssp_stats": stats, "sssp_delta": delta}
 
 
 def run_c5(args):

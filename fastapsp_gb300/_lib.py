@@ -65,6 +65,7 @@ SIGNATURES = {
     "fap_backward_dense": (C.c_int, [_p, _i32, _p, _p, _p, _p, _i32, _p, _p, _p, _p, _p]),
     "fap_addmin_peak": (C.c_int, [_p, _i32, C.POINTER(C.c_double)]),
     "fap_set_option": (C.c_int, [_p, _i32, C.c_double]),
+    "fap_sssp_stats": (C.c_int, [_p, C.POINTER(C.c_uint64)]),
     "fap_get_option": (C.c_int, [_p, _i32, C.POINTER(C.c_double)]),
     "fap_sssp_noalloc": (C.c_int, [_i32, _i32, _i64, _p, _p, _p, _p, _p, _p, _p, _i32, _p, _p, _i64,
                                    _p]),

@@ -174,6 +174,7 @@ struct fap_engine {
   int32_t *d_gid = nullptr, *d_st2ed = nullptr, *d_ed2st = nullptr;
   void *d_w = nullptr, *d_iw = nullptr;
   unsigned *d_status = nullptr;
+  unsigned long long *d_stats = nullptr;  // SSSP counters of the last solve
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[6] = {};
   cudaEvent_t ev_sync[2] = {};
@@ -553,6 +554,8 @@ struct Issuer {
     sa.lanes = pl.sssp_lanes;
     sa.acc64 = e->f32() && e->sssp_fp64;
     sa.delta = sssp_delta_of(e);
+    sa.stats = e->d_stats;
+    if (g == 0) FAP_CUDA(cudaMemsetAsync(e->d_stats, 0, 8 * sizeof(unsigned long long), st));
     FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
     return FAP_OK;
   }
@@ -816,6 +819,8 @@ int init_device(fap_engine *e, int device) {
   // status words: [0] error flags, [1]/[2] maxima for the packed-form bound
   FAP_CUDA(cudaMalloc(&e->d_status, 4 * sizeof(unsigned)));
   FAP_CUDA(cudaMemset(e->d_status, 0, 4 * sizeof(unsigned)));
+  FAP_CUDA(cudaMalloc(&e->d_stats, 8 * sizeof(unsigned long long)));
+  FAP_CUDA(cudaMemset(e->d_stats, 0, 8 * sizeof(unsigned long long)));
   FAP_CUDA(fapk::init_minplus_kernels());
   FAP_CUDA(fapk::init_sssp_kernels());
   return FAP_OK;
@@ -1038,7 +1043,7 @@ int fap_destroy(fap_engine *e) {
     e->res_p.release();
     e->small.release();
     void *ptrs[] = {e->d_ro, e->d_col, e->d_iro, e->d_icol, e->d_gid, e->d_st2ed, e->d_ed2st,
-                    e->d_w, e->d_iw, e->d_status};
+                    e->d_w, e->d_iw, e->d_status, e->d_stats};
     for (void *p : ptrs)
       if (p) cudaFree(p);
     for (auto &ev : e->ev)
@@ -1411,6 +1416,16 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_AUTOTUNE: *value = e->autotune; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");
   }
+}
+
+int fap_sssp_stats(fap_engine *e, uint64_t *out5) {
+  if (!e || !out5) return set_error(FAP_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard dg(e->device);
+  unsigned long long h[8];
+  FAP_CUDA(cudaMemcpy(h, e->d_stats, sizeof(h), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 5; i++) out5[i] = h[i];
+  return FAP_OK;
 }
 
 }  // extern "C"

@@ -46,6 +46,8 @@ struct SsspArgs {
   int32_t lanes;              // sources per batch: 16 or 32 (batches hold <= lanes)
   int32_t acc64;              // FP32 weights searched in FP64 (lanes must be 16)
   double delta;               // near-far threshold step (> 0; huge = plain Bellman-Ford)
+  unsigned long long *stats;  // may be null: [near steps, far splits, frontier
+                              // vertices relaxed, far entries scanned, batches]
 };
 // delta value that puts every vertex in the near frontier (plain frontier BF)
 constexpr double kSsspNoDelta = 2147483647.0;

@@ -204,12 +204,17 @@ __device__ __forceinline__ void store_quad(const MpSegment &s, int row, int col0
     }
 }
 
-// Wide form: add, compare, and two selects per add-min; the argmin is the
-// chunk-local k of the last strict improvement.
+// Wide form (FP32, and int32 outside the packed range).  Distances are kept
+// as their bit patterns, which order like the values (non-negative floats and
+// the int32 encoding), so one __vibmin_u32 gives both the new minimum and
+// whether the current value was kept (ties keep it: strict improvement).  An
+// add-min is then add + vibmin + select; the argmin is the chunk-local k of
+// the last strict improvement, resolved against the staged predecessor tile
+// after each chunk.
 template <typename T, bool PRED>
 __device__ __forceinline__ void tile_wide(MpSmem<T> &sm, const MpSegment &s, const TileGeom &g) {
-  const T INF = Dist<T>::inf();
-  T acc[8][8];
+  const unsigned INF = Dist<T>::bits(Dist<T>::inf());
+  unsigned acc[8][8];
   int32_t pred[8][8];
   int arg[8][8];
 #pragma unroll
@@ -222,7 +227,7 @@ __device__ __forceinline__ void tile_wide(MpSmem<T> &sm, const MpSegment &s, con
       pred[r][c] = -1;
       arg[r][c] = -1;
       if (s.init_from_c && row >= 0 && row < s.M && col >= 0 && col < s.N) {
-        acc[r][c] = static_cast<const T *>(s.C)[(int64_t)row * s.ldc + col];
+        acc[r][c] = static_cast<const unsigned *>(s.C)[(int64_t)row * s.ldc + col];
         if (PRED) pred[r][c] = s.Cp[(int64_t)row * s.ldcp + col];
       }
     }
@@ -247,10 +252,13 @@ __device__ __forceinline__ void tile_wide(MpSmem<T> &sm, const MpSegment &s, con
       for (int r = 0; r < 8; r++)
 #pragma unroll
         for (int c = 0; c < 8; c++) {
-          const T v = Dist<T>::add(a[r], b[c]);
-          if (v < acc[r][c]) {
-            acc[r][c] = v;
-            if (PRED) arg[r][c] = kk;
+          const unsigned v = Dist<T>::bits(Dist<T>::add(a[r], b[c]));
+          if (PRED) {
+            bool keep;
+            acc[r][c] = __vibmin_u32(acc[r][c], v, &keep);
+            arg[r][c] = keep ? arg[r][c] : kk;
+          } else {
+            acc[r][c] = min(acc[r][c], v);
           }
         }
     }
@@ -281,7 +289,7 @@ __device__ __forceinline__ void tile_wide(MpSmem<T> &sm, const MpSegment &s, con
       int32_t p[4];
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        d[q] = acc[r][h * 4 + q];
+        d[q] = Dist<T>::from_bits(acc[r][h * 4 + q]);
         p[q] = pred[r][h * 4 + q];
       }
       store_quad<T, PRED>(s, row, col0, d, p, vec);

@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(kSsspThreads)
   // so that no stamp left by an earlier launch can equal a new epoch.
   int epoch = a.slot_epoch[blockIdx.x];
   unsigned local_max = 0;  // largest finite int32 distance this thread wrote
+  unsigned long long st_steps = 0, st_splits = 0, st_relaxed = 0, st_scanned = 0, st_batches = 0;
   for (int b = blockIdx.x; b < a.nbatches; b += gridDim.x) {
     int steps = 0;  // BF steps + far splits of this batch (capped)
     const int cnt = a.batches[b].count;
@@ -163,6 +164,8 @@ __global__ void __launch_bounds__(kSsspThreads)
           capped = true;
           break;
         }
+        st_steps++;
+        st_relaxed += (unsigned long long)f;
         epoch++;
         const int32_t *F = nearq[cur];
         int32_t *N = nearq[cur ^ 1];
@@ -230,6 +233,8 @@ __global__ void __launch_bounds__(kSsspThreads)
         break;
       }
       thr += delta;
+      st_splits++;
+      st_scanned += (unsigned long long)nf;
       epoch++;
       const int new_far_epoch = ++epoch;
       if (threadIdx.x == 0) s_minfar = INF;
@@ -316,8 +321,18 @@ __global__ void __launch_bounds__(kSsspThreads)
       __syncwarp();
     }
     __syncthreads();  // dvm and the frontiers are reset by the next batch
+    st_batches++;
   }
-  if (threadIdx.x == 0) a.slot_epoch[blockIdx.x] = epoch;
+  if (threadIdx.x == 0) {
+    a.slot_epoch[blockIdx.x] = epoch;
+    if (a.stats != nullptr) {
+      atomicAdd(&a.stats[0], st_steps);
+      atomicAdd(&a.stats[1], st_splits);
+      atomicAdd(&a.stats[2], st_relaxed);
+      atomicAdd(&a.stats[3], st_scanned);
+      atomicAdd(&a.stats[4], st_batches);
+    }
+  }
   if (a.maxd != nullptr) {
     local_max = __reduce_max_sync(0xffffffffu, local_max);
     if (lane == 0 && local_max) atomicMax(a.maxd, local_max);

@@ -146,6 +146,12 @@ class Engine:
         check(lib().fap_last_times(self._h, t), "fap_last_times")
         return dict(zip(["sssp", "floyd", "min_plus", "data", "total"], list(t)))
 
+    def sssp_stats(self):
+        """Counters of the last solve's SSSP phase."""
+        v = (C.c_uint64 * 5)()
+        check(lib().fap_sssp_stats(self._h, v), "fap_sssp_stats")
+        return dict(zip(["steps", "far_splits", "relaxed", "far_scanned", "batches"], list(v)))
+
     def set_option(self, option: int, value: float):
         check(lib().fap_set_option(self._h, int(option), float(value)), "fap_set_option")
 

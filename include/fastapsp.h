@@ -257,6 +257,11 @@ int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m,
 
 /* ---- diagnostics -------------------------------------------------------- */
 
+/* Counters of the SSSP phase of the last solve (no reference counterpart):
+ * [near-frontier steps, far-list splits, frontier vertices relaxed, far
+ * entries scanned, batches], summed over all batches. */
+int fap_sssp_stats(fap_engine *e, uint64_t *out5);
+
 /* Add-min operations per second that the GPU issues from registers alone
  * (no reference counterpart; the roofline denominator of the FW and min-plus
  * phases).  mode 0: int32 DPX add-min (__viaddmin_u32); 1: FP32
