@@ -120,6 +120,9 @@ struct Plan {
     // min-plus
     const MpSegment *mp = nullptr;
     int mp_nseg = 0, mp_tiles = 0;
+    // strip form: the first mp_strip_nseg segments (mp_strip_tiles tiles in
+    // the tile numbering), their CTAs and their largest K
+    int mp_strip_nseg = 0, mp_strip_tiles = 0, mp_strips = 0, mp_max_k = 0;
     int max_sub = 0;  // largest part of the group (bound of the packed form)
   };
   std::vector<Group> groups;
@@ -180,7 +183,7 @@ struct fap_engine {
   cudaEvent_t ev_sync[2] = {};
   // work buffers
   DevBuf fw_d, fw_p;           // FW matrices arena
-  DevBuf sssp_scratch, sssp_stamps, sssp_epoch;
+  DevBuf sssp_scratch, sssp_bits;
   int sssp_slots_alloc = 0;
   DevBuf res_d, res_p;         // device results when the caller passes host memory
   DevBuf small;                // tables of standalone calls
@@ -204,7 +207,7 @@ double sssp_delta_of(const fap_engine *e) {
 int max_sssp_slots(fap_engine *e) {
   // Two 512-thread CTAs per SM, bounded by a 16 GiB scratch budget.
   int slots = std::max(1, 2 * e->sm_count);
-  size_t per = fapk::sssp_slot_bytes(e->n) + (size_t)e->n * 8;
+  size_t per = fapk::sssp_slot_bytes(e->n) + fapk::sssp_bits_bytes(e->n);
   size_t budget = (size_t)16 << 30;
   slots = (int)std::max<size_t>(1, std::min<size_t>((size_t)slots, budget / std::max<size_t>(per, 1)));
   return slots;
@@ -214,10 +217,8 @@ int ensure_sssp_scratch(fap_engine *e, int slots) {
   if (slots <= e->sssp_slots_alloc) return FAP_OK;
   int st;
   if ((st = e->sssp_scratch.ensure(fapk::sssp_slot_bytes(e->n) * slots)) != FAP_OK) return st;
-  if ((st = e->sssp_stamps.ensure((size_t)e->n * 8 * slots)) != FAP_OK) return st;
-  if ((st = e->sssp_epoch.ensure((size_t)4 * slots)) != FAP_OK) return st;
-  FAP_CUDA(cudaMemset(e->sssp_stamps.p, 0, (size_t)e->n * 8 * slots));
-  FAP_CUDA(cudaMemset(e->sssp_epoch.p, 0, (size_t)4 * slots));
+  if ((st = e->sssp_bits.ensure(std::max<size_t>(fapk::sssp_bits_bytes(e->n) * slots, 4))) != FAP_OK)
+    return st;
   e->sssp_slots_alloc = slots;
   return FAP_OK;
 }
@@ -308,6 +309,18 @@ MpSegment mp_segment(const void *A, int64_t lda, const void *B, int64_t ldb, con
   return s;
 }
 
+// CTAs of a segment in the tile form of the min-plus (no skipped blocks).
+int mp_tiles_of(const MpSegment &s) {
+  const int T = fapk::minplus_tile_rows();
+  return ((s.M + T - 1) / T) * s.tiles_x;
+}
+
+// CTAs of a segment in the strip form of the min-plus.
+int mp_strips_of(const MpSegment &s) {
+  const int T = fapk::minplus_tile_rows(), S = fapk::minplus_strip_tiles();
+  return ((s.M + T - 1) / T) * ((s.tiles_x + S - 1) / S);
+}
+
 // Builds the plan for `parts` (row offsets into dist/pred given per part),
 // grouped one part per group (plain) or all in one group (batched).
 int build_plan(fap_engine *e, Plan &pl) {
@@ -353,8 +366,9 @@ int build_plan(fap_engine *e, Plan &pl) {
     std::vector<SsspBatch> batches;
     std::vector<PartDesc> pdesc;
     std::vector<int64_t> row_begin(1, 0), dec_begin(1, 0);
-    std::vector<MpSegment> mps;
-    int mp_tiles = 0;
+    // min-plus segments: those the strip form can take (K <= its limit)
+    // first, then the rest; tiles are numbered over all of them
+    std::vector<MpSegment> mps, mps_wide;
     int maxnb = 0;
     for (int idx : groups[g]) {
       int p = pl.parts[idx];
@@ -403,9 +417,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         s.Fp = pred ? fwp + mat_off[idx] + (int64_t)bdy * d.ld : nullptr;
         s.ldf = d.ld;
         pl.max_mp_k = std::max(pl.max_mp_k, bdy);
-        s.tile_begin = mp_tiles;
-        mp_tiles += tiles;
-        mps.push_back(s);
+        (bdy <= fapk::minplus_strip_max_k() ? mps : mps_wide).push_back(s);
       }
     }
     G.nbatches = (int)batches.size();
@@ -416,8 +428,23 @@ int build_plan(fap_engine *e, Plan &pl) {
     O.pdesc = tb.add(pdesc.data(), pdesc.size());
     O.row_begin = tb.add(row_begin.data(), row_begin.size());
     O.dec_begin = tb.add(dec_begin.data(), dec_begin.size());
+    int mp_tiles = 0, mp_strips = 0, mp_max_k = 0;
+    for (MpSegment &s : mps) {
+      s.strip_begin = mp_strips;
+      mp_strips += mp_strips_of(s);
+      mp_max_k = std::max(mp_max_k, s.K);
+    }
+    G.mp_strip_nseg = (int)mps.size();
+    mps.insert(mps.end(), mps_wide.begin(), mps_wide.end());
+    for (MpSegment &s : mps) {
+      s.tile_begin = mp_tiles;
+      mp_tiles += mp_tiles_of(s);
+      if (&s - mps.data() + 1 == G.mp_strip_nseg) G.mp_strip_tiles = mp_tiles;
+    }
     G.mp_nseg = (int)mps.size();
     G.mp_tiles = mp_tiles;
+    G.mp_strips = mp_strips;
+    G.mp_max_k = mp_max_k;
     O.mp = tb.add(mps.data(), mps.size());
     // FW rounds
     G.diag_cnt.assign(maxnb, 0);
@@ -546,8 +573,7 @@ struct Issuer {
     sa.pred = pl.pred;
     sa.scratch = e->sssp_scratch.p;
     sa.slots = std::min(G.nbatches, e->sssp_slots_alloc);
-    sa.stamps = static_cast<int32_t *>(e->sssp_stamps.p);
-    sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
+    sa.bits = e->sssp_bits.p;
     sa.status = e->d_status;
     sa.maxd = e->f32() ? nullptr : e->d_status + 1;
     sa.iter_cap = 8 * e->n + 64;
@@ -573,7 +599,13 @@ struct Issuer {
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
     }
     if (last) FAP_CUDA(rec(3));
-    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, packed, st));
+    if (packed) {  // strip form for the small-K segments, tiles for the rest
+      FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp, G.mp_strip_nseg, G.mp_strips, G.mp_max_k, st));
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles - G.mp_strip_tiles,
+                                          packed, st, G.mp_strip_tiles));
+    } else {
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, packed, st));
+    }
     if (last) FAP_CUDA(rec(4));
     FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, st));
     if (last) FAP_CUDA(rec(5));
@@ -685,7 +717,7 @@ std::vector<const void *> buffer_signature(const fap_engine *e) {
   double d = sssp_delta_of(e);
   intptr_t dbits;
   std::memcpy(&dbits, &d, sizeof(dbits));
-  return {e->fw_d.p, e->fw_p.p, e->sssp_scratch.p, e->sssp_stamps.p, e->sssp_epoch.p,
+  return {e->fw_d.p, e->fw_p.p, e->sssp_scratch.p, e->sssp_bits.p,
           reinterpret_cast<const void *>((intptr_t)e->sssp_slots_alloc),
           reinterpret_cast<const void *>((intptr_t)e->sssp_fp64),
           reinterpret_cast<const void *>(dbits)};
@@ -1037,8 +1069,7 @@ int fap_destroy(fap_engine *e) {
     e->fw_d.release();
     e->fw_p.release();
     e->sssp_scratch.release();
-    e->sssp_stamps.release();
-    e->sssp_epoch.release();
+    e->sssp_bits.release();
     e->res_d.release();
     e->res_p.release();
     e->small.release();
@@ -1162,6 +1193,7 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
   int tiles = 0;
   MpSegment s = mp_segment(A, lda, B, ldb, Bpath, ldbp, C, ldc, Cpath, ldcp, M, N, K, tiles);
   s.tile_begin = 0;
+  s.strip_begin = 0;
   int rc;
   const bool i32 = dtype == FAP_DTYPE_I32;
   TableBuilder tb;
@@ -1184,9 +1216,11 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
     packed = (unsigned long long)mx[0] + mx[1] < fapk::pack_limit() &&
              (Cpath == nullptr || K <= fapk::max_packed_k());
   }
-  FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr,
-                                      reinterpret_cast<const MpSegment *>(base + o_seg), 1, tiles,
-                                      packed, st));
+  const MpSegment *dseg = reinterpret_cast<const MpSegment *>(base + o_seg);
+  if (packed && K <= fapk::minplus_strip_max_k())
+    FAP_CUDA(fapk::launch_minplus_strips(Cpath != nullptr, dseg, 1, mp_strips_of(s), K, st));
+  else
+    FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr, dseg, 1, tiles, packed, st));
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);
 }
@@ -1328,8 +1362,7 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   sa.pred = pred;
   sa.scratch = e->sssp_scratch.p;
   sa.slots = std::min(sa.nbatches, e->sssp_slots_alloc);
-  sa.stamps = static_cast<int32_t *>(e->sssp_stamps.p);
-  sa.slot_epoch = static_cast<int32_t *>(e->sssp_epoch.p);
+  sa.bits = e->sssp_bits.p;
   sa.status = e->d_status;
   sa.maxd = nullptr;
   sa.iter_cap = 8 * e->n + 64;

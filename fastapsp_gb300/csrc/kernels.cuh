@@ -60,6 +60,7 @@ struct MpSegment {
   int32_t init_from_c; // 1: start from C/Cp (keep on ties); 0: start unreached/-1
   int32_t tiles_x;     // CTA tiles along columns
   int32_t tile_begin;  // first global CTA index of this segment
+  int32_t strip_begin; // first global CTA index in the strip form (min-plus)
   // Optional Floyd-Warshall override of the part's own columns (min-plus of
   // a part's inner rows): where col_part[col] == part, the output takes
   // F[row][col_local[col] - local0] (and Fp) instead of the product.

@@ -13,8 +13,17 @@ namespace fapk {
 // caller must have checked that every finite result stays below
 // pack_limit() and, with predecessors, that every segment has K <=
 // max_packed_k().
+// CTAs take tiles tile0 .. tile0 + tiles - 1 of the segments' numbering.
 cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, int nseg,
-                                 int total_tiles, bool packed, cudaStream_t st);
+                                 int tiles, bool packed, cudaStream_t st, int tile0 = 0);
+// Strip form of the packed min-plus: segments that do not accumulate into C
+// (init_from_c = 0), every K <= max_k <= minplus_strip_max_k(), CTAs numbered by
+// MpSegment::strip_begin (ceil(M / 128) x ceil(tiles_x / minplus_strip_tiles())
+// strips per segment).  Same preconditions as the packed tile form.
+cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
+                                  int max_k, cudaStream_t st);
+int minplus_strip_tiles();
+int minplus_strip_max_k();
 // Largest finite int32 entry of the matrices, atomicMax-ed into *out.
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st);
 unsigned pack_limit();
@@ -38,8 +47,8 @@ struct SsspArgs {
   int32_t *pred;              // may be null
   void *scratch;              // per-slot scratch, sssp_slot_bytes(n) each
   int32_t slots;              // number of CTAs (= scratch slots)
-  int32_t *stamps;            // slots * 2n ints (near and far stamps), zeroed at allocation
-  int32_t *slot_epoch;        // slots ints, zeroed once at allocation
+  void *bits;                 // slots * sssp_bits_bytes(n): frontier bitmaps that do
+                              // not fit in shared memory (null when that is 0)
   unsigned *status;           // device status word (error flags are or-ed in)
   unsigned *maxd;             // largest finite int32 distance written (atomicMax), may be null
   int32_t iter_cap;           // steps (near-frontier sweeps + far splits) per batch
@@ -53,8 +62,9 @@ struct SsspArgs {
 constexpr double kSsspNoDelta = 2147483647.0;
 cudaError_t init_sssp_kernels();
 size_t sssp_slot_bytes(int32_t n);
+size_t sssp_bits_bytes(int32_t n);  // per slot; 0 when the bitmaps fit in shared memory
 // Batch width to use given the number of 32-source batches the work needs.
-int sssp_lanes_for(int64_t sources_total, int64_t batches32, int sm_count);  // bytes of one slot's scratch (excluding stamps)
+int sssp_lanes_for(int64_t sources_total, int64_t batches32, int sm_count);
 int sssp_threads();
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st);
 

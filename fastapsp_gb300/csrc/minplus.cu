@@ -51,6 +51,10 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
   unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
 }
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_2() { asm volatile("cp.async.wait_group 2;\n" ::); }
@@ -366,11 +370,11 @@ __device__ __forceinline__ void keys_from_values(KeySmem &sm, int buf, int k0) {
 
 template <bool PRED>
 __global__ void __launch_bounds__(kThreads, 2)
-    mp_tile_packed_kernel(const MpSegment *__restrict__ segs, int nseg) {
+    mp_tile_packed_kernel(const MpSegment *__restrict__ segs, int nseg, int tile0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   KeySmem &sm = *reinterpret_cast<KeySmem *>(smem_raw);
   __shared__ MpSegment seg;
-  const int tile = blockIdx.x;
+  const int tile = tile0 + blockIdx.x;
   if (threadIdx.x == 0) seg = find_segment(segs, nseg, tile);
   __syncthreads();
   const MpSegment &s = seg;
@@ -499,15 +503,232 @@ __global__ void __launch_bounds__(kThreads, 2)
   }
 }
 
+// Strip form of the packed min-plus for products that do not accumulate into
+// C (the inner rows of every part) with K <= kStripMaxK.  One CTA owns a
+// strip: one 128-row tile of a segment and up to kStripTiles consecutive
+// 128-column tiles.  A's 128 x K block is staged once per strip; B's K x 128
+// tiles are double-buffered, so the next tile's copy is in flight while the
+// current one is multiplied; B's predecessor rows and the own-part column
+// flags of the next tile are staged right after each epilogue, behind the
+// next tile's DPX loop.  The descriptor search, the staging of A and the
+// pipeline fill of the tile kernel are paid once per strip instead of once
+// per tile.  Shared memory (ks = K rounded up to 4):
+//   B[2][ks][128] | Bp[ks][128] | colp[128] | coll[128] | A[128][ks + 1]
+constexpr int kStripTiles = 16;
+constexpr int kStripMaxK = 48;
+
+__host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
+  return (size_t)3 * ks * kTile * 4 + (size_t)2 * kTile * 4 + (size_t)kTile * (ks + 1) * 4;
+}
+
+__device__ __forceinline__ const MpSegment &find_strip_segment(const MpSegment *__restrict__ segs,
+                                                               int nseg, int strip) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (segs[mid].strip_begin <= strip) lo = mid; else hi = mid - 1;
+  }
+  return segs[lo];
+}
+
+// Copies a ks x 128 tile of a row-major 4-byte matrix (rows < K, columns
+// [col0, col0 + 128) < N) into dst[ks][128]; each thread moves 4 consecutive
+// columns of a row per pass (one 16-byte copy when `vec`), and writes `fill`
+// where the source is outside the matrix.
+__device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *src, int64_t ld,
+                                                int K, int N, int ks, int col0, bool vec,
+                                                unsigned fill) {
+  const int t = threadIdx.x;
+  const int j = (t & 31) * 4;
+  const int col = col0 + j;
+  for (int kk = t >> 5; kk < ks; kk += kThreads / 32) {
+    unsigned *d = dst + kk * kTile + j;
+    const unsigned *g = src + (int64_t)kk * ld + col;
+    if (kk < K && vec && col + 3 < N) {
+      cp_async16(d, g);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (kk < K && col + q < N) cp_async4(d + q, g + q);
+        else d[q] = fill;
+      }
+    }
+  }
+}
+
+// Turns the B values this thread copied (same mapping as strip_load_rows)
+// into keys (d << 7) | (k + 1).
+__device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks) {
+  const int t = threadIdx.x;
+  const int j = (t & 31) * 4;
+  for (int kk = t >> 5; kk < ks; kk += kThreads / 32) {
+    uint4 *p = reinterpret_cast<uint4 *>(Bs + kk * kTile + j);
+    const unsigned idx = (unsigned)(kk & kMaxPackedK) + 1u;
+    uint4 v = *p;
+    v.x = (min(v.x, kPackH) << kIdxBits) | idx;
+    v.y = (min(v.y, kPackH) << kIdxBits) | idx;
+    v.z = (min(v.z, kPackH) << kIdxBits) | idx;
+    v.w = (min(v.w, kPackH) << kIdxBits) | idx;
+    *p = v;
+  }
+}
+
+template <bool PRED>
+__global__ void __launch_bounds__(kThreads, 2)
+    mp_strip_kernel(const MpSegment *__restrict__ segs, int nseg, int ks) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned *Bs = reinterpret_cast<unsigned *>(smem_raw);  // [2][ks][128]
+  int32_t *Bps = reinterpret_cast<int32_t *>(Bs + 2 * ks * kTile);  // [ks][128]
+  int32_t *colp = Bps + ks * kTile;  // col_part of the tile's columns
+  int32_t *coll = colp + kTile;      // col_local of the tile's columns
+  unsigned *As = reinterpret_cast<unsigned *>(coll + kTile);  // [128][ks + 1]
+  const int apitch = ks + 1;
+  __shared__ MpSegment seg;
+  if (threadIdx.x == 0) seg = find_strip_segment(segs, nseg, blockIdx.x);
+  __syncthreads();
+  const MpSegment &s = seg;
+  const int strips_x = (s.tiles_x + kStripTiles - 1) / kStripTiles;
+  const int local = blockIdx.x - s.strip_begin;
+  const int rt = local / strips_x;
+  const int jt0 = (local - rt * strips_x) * kStripTiles;
+  const int jt1 = min(jt0 + kStripTiles, s.tiles_x);
+  const int row0 = rt * kTile;
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  const unsigned INF = Dist<uint32_t>::inf();
+  const int kseg = (s.K + 3) & ~3;  // this segment's K rounded up to 4 (<= ks)
+  const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
+  const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
+  const bool vec_c = vec_stores_ok<PRED>(s);
+
+  auto load_side = [&](int col0) {  // B's predecessor rows and column flags of a tile
+    if (PRED)
+      strip_load_rows(reinterpret_cast<unsigned *>(Bps), reinterpret_cast<const unsigned *>(s.Bp),
+                      s.ldbp, s.K, s.N, kseg, col0, vec_bp, 0xffffffffu);
+    if (threadIdx.x < kTile) {
+      const int j = threadIdx.x, col = col0 + j;
+      if (s.col_part != nullptr && col < s.N) {
+        cp_async4(&colp[j], s.col_part + col);
+        cp_async4(&coll[j], s.col_local + col);
+      } else {
+        colp[j] = -1;
+      }
+    }
+  };
+
+  // Prologue: A and B of the first tile | side data of the first tile.
+  for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
+    const int m = idx / kseg, kk = idx - m * kseg;
+    unsigned *d = &As[m * apitch + kk];
+    if (row0 + m < s.M && kk < s.K) cp_async4(d, static_cast<const unsigned *>(s.A) + (int64_t)(row0 + m) * s.lda + kk);
+    else *d = INF;
+  }
+  strip_load_rows(Bs, static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, kseg, jt0 * kTile, vec_b, INF);
+  cp_async_commit();
+  load_side(jt0 * kTile);
+  cp_async_commit();
+
+  for (int jt = jt0; jt < jt1; jt++) {
+    const int buf = (jt - jt0) & 1;
+    unsigned *Bcur = Bs + buf * ks * kTile;
+    if (jt + 1 < jt1)
+      strip_load_rows(Bs + (buf ^ 1) * ks * kTile, static_cast<const unsigned *>(s.B), s.ldb, s.K,
+                      s.N, kseg, (jt + 1) * kTile, vec_b, INF);
+    cp_async_commit();
+    cp_async_wait_1();  // all but the next tile's B have landed
+    if (jt == jt0)
+      for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
+        const int m = idx / kseg, kk = idx - m * kseg;
+        As[m * apitch + kk] = min(As[m * apitch + kk], kPackH) << kIdxBits;
+      }
+    strip_keys_b(Bcur, kseg);
+    __syncthreads();
+
+    unsigned acc[8][8];
+#pragma unroll
+    for (int r = 0; r < 8; r++)
+#pragma unroll
+      for (int c = 0; c < 8; c++) acc[r][c] = kPackH << kIdxBits;
+    const unsigned *arow[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) arow[r] = As + ((r >> 2) * kBlk + ty * 4 + (r & 3)) * apitch;
+    const unsigned *bcol = Bcur + tx * 4;
+    for (int k0 = 0; k0 < kseg; k0 += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int kk = k0 + u;
+        unsigned a[8], b[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) a[r] = arow[r][kk];
+        const uint4 b0 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile);
+        const uint4 b1 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile + kBlk);
+        b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
+        b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+#pragma unroll
+          for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+      }
+    }
+
+    // Epilogue: distances, predecessors from the staged rows, own-part
+    // columns from the part's Floyd-Warshall matrix.
+    const int colbase = jt * kTile;
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const int row = row0 + (r >> 2) * kBlk + ty * 4 + (r & 3);
+      if (row >= s.M) continue;
+      unsigned *crow = static_cast<unsigned *>(s.C) + (int64_t)row * s.ldc;
+      int32_t *prow = PRED ? s.Cp + (int64_t)row * s.ldcp : nullptr;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int sc0 = h * kBlk + tx * 4;
+        const int col0 = colbase + sc0;
+        if (col0 >= s.N) continue;
+        unsigned d[4];
+        int32_t p[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const unsigned key = acc[r][h * 4 + q];
+          const unsigned dist = key >> kIdxBits;
+          const unsigned idx = key & kIdxMask;
+          d[q] = dist >= kPackH ? INF : dist;
+          p[q] = -1;
+          if (PRED && dist < kPackH && idx != 0) p[q] = Bps[(idx - 1) * kTile + sc0 + q];
+          if (colp[sc0 + q] == s.part) {  // own-part column: the FW value
+            const int64_t fj = coll[sc0 + q] - s.local0;
+            d[q] = static_cast<const unsigned *>(s.F)[(int64_t)row * s.ldf + fj];
+            if (PRED) p[q] = s.Fp[(int64_t)row * s.ldf + fj];
+          }
+        }
+        if (vec_c && col0 + 3 < s.N) {
+          *reinterpret_cast<uint4 *>(crow + col0) = make_uint4(d[0], d[1], d[2], d[3]);
+          if (PRED) *reinterpret_cast<int4 *>(prow + col0) = make_int4(p[0], p[1], p[2], p[3]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            if (col0 + q < s.N) {
+              crow[col0 + q] = d[q];
+              if (PRED) prow[col0 + q] = p[q];
+            }
+        }
+      }
+    }
+    __syncthreads();  // B[buf], Bp and the column flags are free again
+    if (jt + 1 < jt1) load_side((jt + 1) * kTile);
+    cp_async_commit();
+  }
+  cp_async_wait_0();
+}
+
 template <typename T, bool PRED>
 __global__ void __launch_bounds__(kThreads, 1)
-    mp_tile_kernel(const MpSegment *__restrict__ segs, int nseg) {
+    mp_tile_kernel(const MpSegment *__restrict__ segs, int nseg, int tile0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MpSmem<T> &sm = *reinterpret_cast<MpSmem<T> *>(smem_raw);
   // The segment descriptor stays in shared memory (read where needed) so that
   // the accumulators, argmins and predecessors keep the registers.
   __shared__ MpSegment seg;
-  const int tile = blockIdx.x;
+  const int tile = tile0 + blockIdx.x;
   if (threadIdx.x == 0) seg = find_segment(segs, nseg, tile);
   __syncthreads();
   const MpSegment &s = seg;
@@ -585,16 +806,23 @@ __global__ void __launch_bounds__(256)
 }
 
 template <typename T, bool PRED>
-cudaError_t launch_mp_t(const MpSegment *d_segs, int nseg, int total_tiles, cudaStream_t st) {
-  if (total_tiles <= 0 || nseg <= 0) return cudaSuccess;
-  mp_tile_kernel<T, PRED><<<total_tiles, kThreads, sizeof(MpSmem<T>), st>>>(d_segs, nseg);
+cudaError_t launch_mp_t(const MpSegment *d_segs, int nseg, int tiles, int tile0, cudaStream_t st) {
+  if (tiles <= 0 || nseg <= 0) return cudaSuccess;
+  mp_tile_kernel<T, PRED><<<tiles, kThreads, sizeof(MpSmem<T>), st>>>(d_segs, nseg, tile0);
   return cudaGetLastError();
 }
 
 template <bool PRED>
-cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int total_tiles, cudaStream_t st) {
-  if (total_tiles <= 0 || nseg <= 0) return cudaSuccess;
-  mp_tile_packed_kernel<PRED><<<total_tiles, kThreads, sizeof(KeySmem), st>>>(d_segs, nseg);
+cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int tiles, int tile0, cudaStream_t st) {
+  if (tiles <= 0 || nseg <= 0) return cudaSuccess;
+  mp_tile_packed_kernel<PRED><<<tiles, kThreads, sizeof(KeySmem), st>>>(d_segs, nseg, tile0);
+  return cudaGetLastError();
+}
+
+template <bool PRED>
+cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks, cudaStream_t st) {
+  if (strips <= 0 || nseg <= 0) return cudaSuccess;
+  mp_strip_kernel<PRED><<<strips, kThreads, strip_smem_bytes(ks), st>>>(d_segs, nseg, ks);
   return cudaGetLastError();
 }
 
@@ -613,14 +841,25 @@ cudaError_t set_packed_attr() {
 }  // namespace
 
 cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, int nseg,
-                                 int total_tiles, bool packed, cudaStream_t st) {
-  if (f32) return pred ? launch_mp_t<float, true>(d_segs, nseg, total_tiles, st)
-                       : launch_mp_t<float, false>(d_segs, nseg, total_tiles, st);
-  if (packed) return pred ? launch_packed_t<true>(d_segs, nseg, total_tiles, st)
-                          : launch_packed_t<false>(d_segs, nseg, total_tiles, st);
-  return pred ? launch_mp_t<uint32_t, true>(d_segs, nseg, total_tiles, st)
-              : launch_mp_t<uint32_t, false>(d_segs, nseg, total_tiles, st);
+                                 int tiles, bool packed, cudaStream_t st, int tile0) {
+  if (f32) return pred ? launch_mp_t<float, true>(d_segs, nseg, tiles, tile0, st)
+                       : launch_mp_t<float, false>(d_segs, nseg, tiles, tile0, st);
+  if (packed) return pred ? launch_packed_t<true>(d_segs, nseg, tiles, tile0, st)
+                          : launch_packed_t<false>(d_segs, nseg, tiles, tile0, st);
+  return pred ? launch_mp_t<uint32_t, true>(d_segs, nseg, tiles, tile0, st)
+              : launch_mp_t<uint32_t, false>(d_segs, nseg, tiles, tile0, st);
 }
+
+cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
+                                  int max_k, cudaStream_t st) {
+  if (max_k < 0 || max_k > kStripMaxK) return cudaErrorInvalidValue;
+  const int ks = (max_k + 3) & ~3;
+  return pred ? launch_strip_t<true>(d_segs, nseg, strips, ks, st)
+              : launch_strip_t<false>(d_segs, nseg, strips, ks, st);
+}
+
+int minplus_strip_tiles() { return kStripTiles; }
+int minplus_strip_max_k() { return kStripMaxK; }
 
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st) {
   if (nmats <= 0) return cudaSuccess;
@@ -651,7 +890,12 @@ cudaError_t init_minplus_kernels() {
   if ((e = set_mp_attr<uint32_t, true>()) != cudaSuccess) return e;
   if ((e = set_mp_attr<uint32_t, false>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<true>()) != cudaSuccess) return e;
-  return set_packed_attr<false>();
+  if ((e = set_packed_attr<false>()) != cudaSuccess) return e;
+  const int smax = (int)strip_smem_bytes((kStripMaxK + 3) & ~3);
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                smax)) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(mp_strip_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
 }
 
 int minplus_tile_rows() { return kTile; }

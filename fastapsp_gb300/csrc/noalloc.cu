@@ -7,8 +7,8 @@
 // inside a request, or real-time paths where an allocation (and the device
 // synchronization it can imply) is not acceptable.  fap_sssp_noalloc gives
 // them the SSSP kernel of fap_sssp with every piece of scratch -- the
-// per-batch distance table, frontiers, dedup stamps, the batch list and the
-// status word -- taken from one file-scope device array of fixed size,
+// per-batch distance table, frontiers, frontier bitmaps, the batch list and
+// the status word -- taken from one file-scope device array of fixed size,
 // kNoAllocBytes.  The caller passes the graph and the output rows in device
 // memory it owns.  Every GPU that loads this library holds the array until
 // the process exits.
@@ -18,7 +18,8 @@
 // device current) on the first call there.  That first call should therefore
 // come before any stream capture.  All calls on a device share the array and
 // it keeps the last call's contents, so every call clears the parts that
-// must start at zero; calls whose work overlaps on the GPU (different
+// must start at zero (the status words; the kernel clears its own tables);
+// calls whose work overlaps on the GPU (different
 // streams, or different host threads) race on the array and must be
 // serialized by the caller.
 
@@ -87,15 +88,16 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
       return set_error(FAP_ERR_INVALID, "fap_sssp_noalloc: source out of range");
   if (num_sources == 0) return FAP_OK;
 
-  // Layout of the static array: status words | batch list | slot epochs |
-  // stamps (slots x 2n) | per-slot scratch (slots x sssp_slot_bytes(n)).
+  // Layout of the static array: status words | batch list | frontier bitmaps
+  // (slots x sssp_bits_bytes(n), none when they fit in shared memory) |
+  // per-slot scratch (slots x sssp_slot_bytes(n)).
   const int nb = (num_sources + 31) / 32;
   const size_t o_status = 0;
   const size_t o_batches = 256;
   const size_t batch_bytes = round_up((size_t)nb * sizeof(fapk::SsspBatch), 256);
-  const size_t o_epoch = o_batches + batch_bytes;
-  const size_t per_slot = fapk::sssp_slot_bytes(n) + round_up((size_t)n * 8, 256);
-  if (o_epoch + 256 + per_slot > kNoAllocBytes)
+  const size_t o_bits = o_batches + batch_bytes;
+  const size_t per_slot = fapk::sssp_slot_bytes(n) + round_up(fapk::sssp_bits_bytes(n), 256);
+  if (o_bits + per_slot > kNoAllocBytes)
     return set_error(FAP_ERR_RANGE,
                      "fap_sssp_noalloc: n = " + std::to_string(n) + " with " +
                          std::to_string(num_sources) + " sources needs more than the " +
@@ -110,15 +112,13 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   if (rc != FAP_OK) return rc;
   // Largest slot count (one CTA per slot, at most two per SM) that fits.
   auto end_of = [&](size_t k) {
-    return o_epoch + round_up(k * 4, 256) + round_up(k * (size_t)n * 8, 256) +
-           k * fapk::sssp_slot_bytes(n);
+    return o_bits + round_up(k * fapk::sssp_bits_bytes(n), 256) + k * fapk::sssp_slot_bytes(n);
   };
   int slots = std::min(nb, std::max(1, 2 * sms));
   while (slots > 1 && end_of((size_t)slots) > kNoAllocBytes) slots--;
   if (end_of((size_t)slots) > kNoAllocBytes)
     return set_error(FAP_ERR_RANGE, "fap_sssp_noalloc: graph too large for the static scratch");
-  const size_t o_stamps = o_epoch + round_up((size_t)slots * 4, 256);
-  const size_t o_slots = o_stamps + round_up((size_t)slots * n * 8, 256);
+  const size_t o_slots = o_bits + round_up((size_t)slots * fapk::sssp_bits_bytes(n), 256);
 
   std::vector<fapk::SsspBatch> batches(nb);
   for (int b = 0; b < nb; b++) {
@@ -131,10 +131,9 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
     }
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // Clear what must start at zero: status, slot epochs and stamps.
+  // Clear what must start at zero: the status words (the kernel clears its
+  // own distance tables and bitmaps at the start of every batch).
   if ((ce = cudaMemsetAsync(base + o_status, 0, 256, st)) != cudaSuccess ||
-      (ce = cudaMemsetAsync(base + o_epoch, 0, (size_t)slots * 4, st)) != cudaSuccess ||
-      (ce = cudaMemsetAsync(base + o_stamps, 0, (size_t)slots * n * 8, st)) != cudaSuccess ||
       (ce = cudaMemcpyAsync(base + o_batches, batches.data(), (size_t)nb * sizeof(fapk::SsspBatch),
                             cudaMemcpyHostToDevice, st)) != cudaSuccess)
     return set_error(FAP_ERR_CUDA, std::string("fap_sssp_noalloc: ") + cudaGetErrorString(ce));
@@ -152,8 +151,7 @@ extern "C" int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m, const int32
   sa.pred = pred;
   sa.scratch = base + o_slots;
   sa.slots = slots;
-  sa.stamps = reinterpret_cast<int32_t *>(base + o_stamps);
-  sa.slot_epoch = reinterpret_cast<int32_t *>(base + o_epoch);
+  sa.bits = base + o_bits;
   sa.status = reinterpret_cast<unsigned *>(base + o_status);
   sa.maxd = nullptr;
   sa.iter_cap = 8 * n + 64;

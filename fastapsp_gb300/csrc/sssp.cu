@@ -18,7 +18,7 @@
 // keeps the re-relaxations of plain Bellman-Ford on long weighted paths (road
 // networks) down while every phase stays data-parallel.  Relaxation is an
 // atomicMin on the distance bits (non-negative floats, doubles and the int32
-// encoding all order like their bits); per-vertex stamps let a vertex enter a
+// encoding all order like their bits); frontier bitmaps let a vertex enter a
 // frontier once per step.  No host round trip: the loop ends when both
 // frontiers are empty, or at a step cap that sets an error flag instead of
 // spinning.  The result is the fixpoint dist[v] = min_u fl(dist[u] + w(u,v)),
@@ -38,6 +38,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "kernels.cuh"
@@ -51,8 +52,7 @@ constexpr int kSsspThreads = 512;
 constexpr int kSsspWarps = kSsspThreads / 32;
 
 // dvm (n x 32 four-byte or n x 16 eight-byte entries) + near/far frontiers
-// (2 + 2), n ints each.  The near and far stamps (2n ints per slot) live in
-// SsspArgs::stamps, which is zeroed when it is allocated.
+// (2 + 2), n ints each.
 __host__ __device__ inline size_t slot_bytes(int32_t n) {
   size_t b = (size_t)n * 32 * 4 + (size_t)n * 4 * 4;
   return (b + 255) & ~(size_t)255;
@@ -94,26 +94,40 @@ struct Acc<float, true> {  // FP32 weights, FP64 search
   static __device__ __forceinline__ V from_double(double x) { return x; }
 };
 
+// Frontier membership bitmaps: near[2] (entry of the next near frontier,
+// alternating per step) and far (entry of the far list), ceil(n / 32) words
+// each.  They live in the dynamic shared memory (overlaid on the output
+// tiles, which are only used after the search) when they fit there, else in
+// the slot's part of SsspArgs::bits.
+__host__ __device__ inline size_t bitmap_bytes(int32_t n) { return (size_t)3 * ((n + 31) / 32) * 4; }
+constexpr size_t kBitmapSmemMax = 160 * 1024;
+
+__device__ __forceinline__ bool set_bit(unsigned *bits, int v) {
+  const unsigned m = 1u << (v & 31);
+  return (atomicOr(&bits[v >> 5], m) & m) == 0u;
+}
+__device__ __forceinline__ void clear_bit(unsigned *bits, int v) {
+  atomicAnd(&bits[v >> 5], ~(1u << (v & 31)));
+}
+
 template <typename T, bool PRED, int LANES, bool ACC64>
 __global__ void __launch_bounds__(kSsspThreads)
     sssp_kernel(SsspArgs a) {
   using A = Acc<T, ACC64>;
   using V = typename A::V;
   using K = typename A::K;
-  constexpr int VPW = 32 / LANES;
+  constexpr int VPW = 32 / LANES;  // lane groups (frontier vertices) per warp
+  constexpr int R = 4;             // frontier vertices per lane group per sweep
+  constexpr int G = 8;             // edges per lane group in flight
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / LANES, sl = lane % LANES;
   const unsigned group_mask = LANES == 32 ? 0xffffffffu : (0xffffu << (16 * sub));
   const int32_t n = a.n;
   unsigned char *base = static_cast<unsigned char *>(a.scratch) + (size_t)blockIdx.x * slot_bytes(n);
   K *dvm = reinterpret_cast<K *>(base);
-  int32_t *nearq[2], *farq[2];
-  nearq[0] = reinterpret_cast<int32_t *>(base + (size_t)n * 32 * 4);
-  nearq[1] = nearq[0] + n;
-  farq[0] = nearq[1] + n;
-  farq[1] = farq[0] + n;
-  int32_t *stamp = a.stamps + (size_t)blockIdx.x * 2 * n;
-  int32_t *fstamp = stamp + n;
+  // near frontiers at nearq0 + {0, n}, far lists at farq0 + {0, n}
+  int32_t *const nearq0 = reinterpret_cast<int32_t *>(base + (size_t)n * 32 * 4);
+  int32_t *const farq0 = nearq0 + 2 * (size_t)n;
   const unsigned *wb = static_cast<const unsigned *>(a.w);
   const unsigned *iwb = static_cast<const unsigned *>(a.iw);
   const K INF = A::inf();
@@ -121,12 +135,14 @@ __global__ void __launch_bounds__(kSsspThreads)
 
   extern __shared__ __align__(16) unsigned char sssp_smem[];
   OutTile<LANES> &tile = reinterpret_cast<OutTile<LANES> *>(sssp_smem)[warp];
+  const int words = (n + 31) / 32;
+  unsigned *bits = bitmap_bytes(n) <= kBitmapSmemMax
+                       ? reinterpret_cast<unsigned *>(sssp_smem)
+                       : reinterpret_cast<unsigned *>(a.bits) + (size_t)blockIdx.x * 3 * words;
+  unsigned *const farbits = bits + 2 * words;  // near bitmaps at bits + {0, words}
   __shared__ int s_near[2], s_far[2];
   __shared__ K s_minfar;
 
-  // Stamps persist across launches; each slot continues its own epoch count
-  // so that no stamp left by an earlier launch can equal a new epoch.
-  int epoch = a.slot_epoch[blockIdx.x];
   unsigned local_max = 0;  // largest finite int32 distance this thread wrote
   unsigned long long st_steps = 0, st_splits = 0, st_relaxed = 0, st_scanned = 0, st_batches = 0;
   for (int b = blockIdx.x; b < a.nbatches; b += gridDim.x) {
@@ -134,19 +150,15 @@ __global__ void __launch_bounds__(kSsspThreads)
     const int cnt = a.batches[b].count;
     const int my_src = sl < cnt ? a.batches[b].src[sl] : -1;
     for (size_t i = threadIdx.x; i < (size_t)n * LANES; i += blockDim.x) dvm[i] = INF;
+    for (int i = threadIdx.x; i < 3 * words; i += blockDim.x) bits[i] = 0u;
     if (threadIdx.x == 0) {
       s_near[0] = s_near[1] = 0;
       s_far[0] = s_far[1] = 0;
     }
-    epoch++;
-    int far_epoch = ++epoch;
     __syncthreads();
     if (threadIdx.x < LANES && my_src >= 0 && my_src < n) {
       dvm[(size_t)my_src * LANES + sl] = A::key((V)0);
-      if (atomicExch(&stamp[my_src], epoch) != epoch) {
-        const int pos = atomicAdd(&s_near[0], 1);
-        nearq[0][pos] = my_src;
-      }
+      if (set_bit(bits, my_src)) nearq0[atomicAdd(&s_near[0], 1)] = my_src;
     } else if (threadIdx.x < LANES && my_src >= n) {
       atomicOr(a.status, kErrBadInput);
     }
@@ -166,53 +178,79 @@ __global__ void __launch_bounds__(kSsspThreads)
         }
         st_steps++;
         st_relaxed += (unsigned long long)f;
-        epoch++;
-        const int32_t *F = nearq[cur];
-        int32_t *N = nearq[cur ^ 1];
-        int32_t *FAR = farq[fcur];
-        for (int fb = warp * VPW; fb < f; fb += kSsspWarps * VPW) {
-          const int idx = fb + sub;
-          const bool has = idx < f;
-          const int u = has ? __ldcg(&F[idx]) : 0;
-          const K duk = has ? __ldcg(&dvm[(size_t)u * LANES + sl]) : INF;
-          const V du = A::val(duk);
-          const int e0 = has ? a.ro[u] : 0;
-          const int deg = has ? a.ro[u + 1] - e0 : 0;
-          int maxdeg = deg;
-          if (VPW == 2) maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
-          // Edges in groups of 4: the neighbour ids, weights and current
-          // distances of a group are loaded before any atomic, so a vertex
-          // costs a few dependent round trips rather than a few per edge.
-          constexpr int G = 4;
-          for (int e = 0; e < maxdeg; e += G) {
+        const int32_t *F = nearq0 + (size_t)cur * n;
+        int32_t *N = nearq0 + (size_t)(cur ^ 1) * n;
+        int32_t *FAR = farq0 + (size_t)fcur * n;
+        unsigned *fbits = bits + cur * words, *nbits = bits + (cur ^ 1) * words;
+        // A lane group takes R frontier vertices per sweep and walks their
+        // concatenated out-edge lists G edges at a time: the loads of a
+        // sweep's vertices, of G edges and the G atomics are each issued
+        // together, so a sweep costs four dependent round trips.
+        for (int fb = warp * VPW * R; fb < f; fb += kSsspWarps * VPW * R) {
+          int u[R];
+#pragma unroll
+          for (int i = 0; i < R; i++) {
+            const int idx = fb + i * VPW + sub;
+            u[i] = idx < f ? __ldcg(&F[idx]) : -1;
+          }
+          V du[R];
+          bool ok[R];
+          int eb[R], pre[R + 1];
+          pre[0] = 0;
+#pragma unroll
+          for (int i = 0; i < R; i++) {
+            K k = INF;
+            int e0 = 0, deg = 0;
+            if (u[i] >= 0) {
+              k = __ldcg(&dvm[(size_t)u[i] * LANES + sl]);
+              e0 = a.ro[u[i]];
+              deg = a.ro[u[i] + 1] - e0;
+              if (sl == 0) clear_bit(fbits, u[i]);
+            }
+            du[i] = A::val(k);
+            ok[i] = k < INF;
+            pre[i + 1] = pre[i] + deg;
+            eb[i] = e0 - pre[i];
+          }
+          const int tot = pre[R];
+          int tmax = tot;
+          if (VPW == 2) tmax = max(tot, __shfl_xor_sync(0xffffffffu, tot, 16));
+          for (int t0 = 0; t0 < tmax; t0 += G) {
             int v[G];
-            K cur_k[G], ck[G];
             V c[G];
             bool live[G];
 #pragma unroll
             for (int q = 0; q < G; q++) {
-              live[q] = e + q < deg;
-              v[q] = live[q] ? a.col[e0 + e + q] : 0;
-              c[q] = live[q] ? du + A::weight(wb[e0 + e + q]) : (V)0;
+              const int t = t0 + q;
+              V d = du[0];
+              int e = eb[0] + t;
+              bool o = ok[0];
+#pragma unroll
+              for (int i = 1; i < R; i++)
+                if (t >= pre[i]) {
+                  d = du[i];
+                  e = eb[i] + t;
+                  o = ok[i];
+                }
+              const bool in = t < tot;
+              v[q] = in ? a.col[e] : 0;
+              live[q] = in && o;
+              c[q] = live[q] ? d + A::weight(wb[e]) : (V)0;
             }
+            K old[G];
+#pragma unroll
+            for (int q = 0; q < G; q++)
+              old[q] = live[q] ? atomicMin(&dvm[(size_t)v[q] * LANES + sl], A::key(c[q])) : (K)0;
 #pragma unroll
             for (int q = 0; q < G; q++) {
-              ck[q] = A::key(c[q]);
-              cur_k[q] = (live[q] && duk < INF) ? __ldcg(&dvm[(size_t)v[q] * LANES + sl]) : (K)0;
-            }
-#pragma unroll
-            for (int q = 0; q < G; q++) {
-              bool imp = false, nearv = false;
-              if (live[q] && duk < INF && ck[q] < cur_k[q]) {
-                imp = ck[q] < atomicMin(&dvm[(size_t)v[q] * LANES + sl], ck[q]);
-                nearv = imp && c[q] < thr;
-              }
+              const bool imp = live[q] && A::key(c[q]) < old[q];
+              const bool nearv = imp && c[q] < thr;
               const unsigned bi = __ballot_sync(0xffffffffu, imp) & group_mask;
               const unsigned bn = __ballot_sync(0xffffffffu, nearv) & group_mask;
               if (bi != 0u && sl == 0) {
                 if (bn != 0u) {
-                  if (atomicExch(&stamp[v[q]], epoch) != epoch) N[atomicAdd(&s_near[cur ^ 1], 1)] = v[q];
-                } else if (atomicExch(&fstamp[v[q]], far_epoch) != far_epoch) {
+                  if (set_bit(nbits, v[q])) N[atomicAdd(&s_near[cur ^ 1], 1)] = v[q];
+                } else if (set_bit(farbits, v[q])) {
                   FAR[atomicAdd(&s_far[fcur], 1)] = v[q];
                 }
               }
@@ -235,28 +273,38 @@ __global__ void __launch_bounds__(kSsspThreads)
       thr += delta;
       st_splits++;
       st_scanned += (unsigned long long)nf;
-      epoch++;
-      const int new_far_epoch = ++epoch;
       if (threadIdx.x == 0) s_minfar = INF;
       __syncthreads();
-      const int32_t *FAR = farq[fcur];
-      int32_t *NFAR = farq[fcur ^ 1];
-      for (int fb = warp * VPW; fb < nf; fb += kSsspWarps * VPW) {
-        const int idx = fb + sub;
-        const bool has = idx < nf;
-        const int v = has ? __ldcg(&FAR[idx]) : 0;
-        K m = has ? __ldcg(&dvm[(size_t)v * LANES + sl]) : INF;
+      const int32_t *FAR = farq0 + (size_t)fcur * n;
+      int32_t *NFAR = farq0 + (size_t)(fcur ^ 1) * n;
+      int32_t *NEAR = nearq0 + (size_t)cur * n;
+      unsigned *nearbits = bits + cur * words;
+      for (int fb = warp * VPW * R; fb < nf; fb += kSsspWarps * VPW * R) {
+        int v[R];
+        K m[R];
 #pragma unroll
-        for (int o = LANES / 2; o >= 1; o >>= 1) {
-          const K other = __shfl_xor_sync(0xffffffffu, m, o);
-          m = other < m ? other : m;
+        for (int i = 0; i < R; i++) {
+          const int idx = fb + i * VPW + sub;
+          v[i] = idx < nf ? __ldcg(&FAR[idx]) : -1;
         }
-        if (has && sl == 0) {
-          if (A::val(m) < thr) {
-            if (atomicExch(&stamp[v], epoch) != epoch) nearq[cur][atomicAdd(&s_near[cur], 1)] = v;
-          } else if (atomicExch(&fstamp[v], new_far_epoch) != new_far_epoch) {
-            NFAR[atomicAdd(&s_far[fcur ^ 1], 1)] = v;
-            atomicMin(&s_minfar, m);
+#pragma unroll
+        for (int i = 0; i < R; i++) m[i] = v[i] >= 0 ? __ldcg(&dvm[(size_t)v[i] * LANES + sl]) : INF;
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+#pragma unroll
+          for (int o = LANES / 2; o >= 1; o >>= 1) {
+            const K other = __shfl_xor_sync(0xffffffffu, m[i], o);
+            m[i] = other < m[i] ? other : m[i];
+          }
+          if (v[i] >= 0 && sl == 0) {
+            if (A::val(m[i]) < thr) {
+              // leaves the far list (its bit is cleared) for the near frontier
+              clear_bit(farbits, v[i]);
+              if (set_bit(nearbits, v[i])) NEAR[atomicAdd(&s_near[cur], 1)] = v[i];
+            } else {
+              NFAR[atomicAdd(&s_far[fcur ^ 1], 1)] = v[i];  // stays, bit kept
+              atomicMin(&s_minfar, m[i]);
+            }
           }
         }
       }
@@ -265,7 +313,6 @@ __global__ void __launch_bounds__(kSsspThreads)
       // nothing below the new threshold: jump it to the far minimum
       if (s_near[cur] == 0 && s_minfar < INF) thr = A::val(s_minfar) + delta;
       fcur ^= 1;
-      far_epoch = new_far_epoch;
       __syncthreads();
     }
     if (capped) {
@@ -274,40 +321,81 @@ __global__ void __launch_bounds__(kSsspThreads)
     }
 
     // ---- predecessors and transposed output: warps work on their own
-    // 32-vertex blocks and synchronize only within the warp ----
+    // 32-vertex blocks and synchronize only within the warp.  A lane group
+    // takes R vertices at a time and scans their concatenated in-edge lists
+    // G edges at a time. ----
     for (int v0 = warp * 32; v0 < n; v0 += kSsspWarps * 32) {
-      for (int vi = sub; vi < 32; vi += VPW) {
-        const int v = v0 + vi;
-        unsigned dv_out = Dist<T>::bits(Dist<T>::inf());
-        int32_t p = -1;
-        if (v < n && sl < cnt) {
-          const K dvk = __ldcg(&dvm[(size_t)v * LANES + sl]);
-          dv_out = A::out(dvk);
-          if (dvk < INF) {
-            if (!std::is_same<T, float>::value) local_max = max(local_max, dv_out);
-            if (PRED) {
-              if (v == my_src) {
-                p = v;
-              } else {
-                K bdu = ~(K)0;
-                int bu = -1;
-                const V dv = A::val(dvk);
-                for (int e = a.iro[v]; e < a.iro[v + 1]; e++) {
-                  const int u = a.icol[e];
-                  const K duk = __ldcg(&dvm[(size_t)u * LANES + sl]);
-                  if (duk >= INF) continue;
-                  if (A::val(duk) + A::weight(iwb[e]) == dv && (duk < bdu || (duk == bdu && u < bu))) {
-                    bdu = duk;
-                    bu = u;
-                  }
+      for (int vb = 0; vb < 32; vb += VPW * R) {
+        int vv[R], ib[R], pre[R + 1];
+        K dk[R], bdu[R];
+        int bu[R];
+        pre[0] = 0;
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+          vv[i] = v0 + vb + i * VPW + sub;
+          const bool in = vv[i] < n;
+          dk[i] = (in && sl < cnt) ? __ldcg(&dvm[(size_t)vv[i] * LANES + sl]) : INF;
+          int e0 = 0, deg = 0;
+          if (PRED && in) {
+            e0 = a.iro[vv[i]];
+            deg = a.iro[vv[i] + 1] - e0;
+          }
+          pre[i + 1] = pre[i] + deg;
+          ib[i] = e0 - pre[i];
+          bdu[i] = ~(K)0;
+          bu[i] = -1;
+        }
+        if (PRED) {
+          const int tot = pre[R];
+          int tmax = tot;
+          if (VPW == 2) tmax = max(tot, __shfl_xor_sync(0xffffffffu, tot, 16));
+          for (int t0 = 0; t0 < tmax; t0 += G) {
+            int uu[G], own[G];
+            unsigned wq[G];
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+              const int t = t0 + q;
+              int e = ib[0] + t, o = 0;
+#pragma unroll
+              for (int i = 1; i < R; i++)
+                if (t >= pre[i]) {
+                  e = ib[i] + t;
+                  o = i;
                 }
-                p = bu;
+              const bool in = t < tot;
+              uu[q] = in ? a.icol[e] : -1;
+              wq[q] = in ? iwb[e] : 0u;
+              own[q] = o;
+            }
+            K duk[G];
+#pragma unroll
+            for (int q = 0; q < G; q++) duk[q] = uu[q] >= 0 ? __ldcg(&dvm[(size_t)uu[q] * LANES + sl]) : INF;
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+              const V cand = A::val(duk[q]) + A::weight(wq[q]);
+              const bool reached = duk[q] < INF;
+#pragma unroll
+              for (int i = 0; i < R; i++) {
+                const bool better = reached && own[q] == i && cand == A::val(dk[i]) &&
+                                    (duk[q] < bdu[i] || (duk[q] == bdu[i] && uu[q] < bu[i]));
+                bdu[i] = better ? duk[q] : bdu[i];
+                bu[i] = better ? uu[q] : bu[i];
               }
             }
           }
         }
-        tile.d[vi][sl] = dv_out;
-        tile.p[vi][sl] = p;
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+          unsigned dv_out = Dist<T>::bits(Dist<T>::inf());
+          int32_t p = -1;
+          if (dk[i] < INF) {
+            dv_out = A::out(dk[i]);
+            if (!std::is_same<T, float>::value) local_max = max(local_max, dv_out);
+            if (PRED) p = vv[i] == my_src ? vv[i] : bu[i];
+          }
+          tile.d[vb + i * VPW + sub][sl] = dv_out;
+          tile.p[vb + i * VPW + sub][sl] = p;
+        }
       }
       __syncwarp();
       const int col = v0 + lane;
@@ -320,18 +408,15 @@ __global__ void __launch_bounds__(kSsspThreads)
       }
       __syncwarp();
     }
-    __syncthreads();  // dvm and the frontiers are reset by the next batch
+    __syncthreads();  // dvm, the frontiers and the bitmaps are reset by the next batch
     st_batches++;
   }
-  if (threadIdx.x == 0) {
-    a.slot_epoch[blockIdx.x] = epoch;
-    if (a.stats != nullptr) {
-      atomicAdd(&a.stats[0], st_steps);
-      atomicAdd(&a.stats[1], st_splits);
-      atomicAdd(&a.stats[2], st_relaxed);
-      atomicAdd(&a.stats[3], st_scanned);
-      atomicAdd(&a.stats[4], st_batches);
-    }
+  if (threadIdx.x == 0 && a.stats != nullptr) {
+    atomicAdd(&a.stats[0], st_steps);
+    atomicAdd(&a.stats[1], st_splits);
+    atomicAdd(&a.stats[2], st_relaxed);
+    atomicAdd(&a.stats[3], st_scanned);
+    atomicAdd(&a.stats[4], st_batches);
   }
   if (a.maxd != nullptr) {
     local_max = __reduce_max_sync(0xffffffffu, local_max);
@@ -341,7 +426,9 @@ __global__ void __launch_bounds__(kSsspThreads)
 
 template <typename T, bool PRED, int LANES, bool ACC64>
 cudaError_t launch_one(const SsspArgs &a, cudaStream_t st) {
-  sssp_kernel<T, PRED, LANES, ACC64><<<a.slots, kSsspThreads, out_smem<LANES>(), st>>>(a);
+  size_t smem = out_smem<LANES>();
+  if (bitmap_bytes(a.n) <= kBitmapSmemMax) smem = std::max(smem, bitmap_bytes(a.n));
+  sssp_kernel<T, PRED, LANES, ACC64><<<a.slots, kSsspThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -358,12 +445,14 @@ cudaError_t launch_t(const SsspArgs &a, cudaStream_t st) {
 template <typename T, bool PRED, int LANES, bool ACC64>
 cudaError_t set_attr() {
   return cudaFuncSetAttribute(sssp_kernel<T, PRED, LANES, ACC64>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)out_smem<LANES>());
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)std::max(out_smem<LANES>(), kBitmapSmemMax));
 }
 
 }  // namespace
 
 size_t sssp_slot_bytes(int32_t n) { return slot_bytes(n); }
+size_t sssp_bits_bytes(int32_t n) { return bitmap_bytes(n) <= kBitmapSmemMax ? 0 : bitmap_bytes(n); }
 int sssp_threads() { return kSsspThreads; }
 
 cudaError_t init_sssp_kernels() {

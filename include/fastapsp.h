@@ -240,7 +240,7 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes,
  * sources in host memory, and device rows dist/pred of num_sources x ld.
  * All scratch comes from one static device array of FAP_NOALLOC_SCRATCH_BYTES
  * (64 MiB) that every GPU loading this library holds until exit; graphs whose
- * scratch does not fit (about n > 440,000 vertices) are rejected with
+ * scratch does not fit (about n > 460,000 vertices) are rejected with
  * FAP_ERR_RANGE.  No allocation: neither cudaMalloc/cudaFree nor an
  * allocating library call.  The first call on a device looks up the array's
  * device address (so make that first call before any stream capture).  Calls

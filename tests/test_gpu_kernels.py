@@ -37,7 +37,8 @@ def as_oracle(a):
 
 @pytest.mark.parametrize("f32", [False, True])
 @pytest.mark.parametrize("M,N,K", [(1, 1, 1), (31, 33, 7), (64, 64, 64), (65, 129, 33), (200, 300, 130),
-                                   (130, 70, 0), (5, 1000, 257)])
+                                   (130, 70, 0), (5, 1000, 257), (300, 2100, 29), (129, 2053, 48),
+                                   (257, 4100, 49)])
 def test_minplus_matches_oracle(ctx, oracle_lib, f32, M, N, K):
     rng = np.random.default_rng(M * 1000 + N * 10 + K)
     A = rand_dist(rng, (M, K), 0.2, f32)
@@ -158,6 +159,26 @@ def test_sssp_result_independent_of_near_far_step(gpu, oracle_lib, kind):
         rd, rp = oracle_lib.dijkstra_path(int(s), g.row_offset, g.col_val, g.weight)
         assert np.array_equal(as_oracle(outs[0][0][i]).view(np.int32), rd.view(np.int32))
         assert np.array_equal(outs[0][1][i], rp)
+
+
+def test_sssp_large_graph_bitmaps_in_global_memory(gpu, oracle_lib):
+    """n = 450,000: the frontier bitmaps (3 x n bits) exceed the shared-memory
+    budget and live in device memory; results stay bit-exact."""
+    g = graphs.road_like(450_000, seed=21)
+    n = g.n
+    gid = np.where(np.arange(n) < n // 2, 1, 2).astype(np.int32)
+    src = np.random.default_rng(9).choice(n, size=24, replace=False).astype(np.int32)
+    with gpu.Engine(n, g.row_offset, g.col_val, g.weight, 2, graph_id=gid, dtype=gpu.DTYPE_F32) as eng:
+        d = torch.empty((len(src), n), dtype=torch.float32, device="cuda")
+        p = torch.empty((len(src), n), dtype=torch.int32, device="cuda")
+        eng.sssp(src, d, p)
+        torch.cuda.synchronize()
+        d = d.cpu().numpy()
+        p = p.cpu().numpy()
+    for i in (0, 7, 23):
+        rd, rp = oracle_lib.dijkstra_path(int(src[i]), g.row_offset, g.col_val, g.weight)
+        assert np.array_equal(d[i].view(np.int32), rd.view(np.int32)), f"row {i}"
+        assert np.array_equal(p[i], rp), f"pred row {i}"
 
 
 def test_sssp_fp64_option_rounds_once(gpu, oracle_lib):
