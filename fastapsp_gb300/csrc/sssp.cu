@@ -117,8 +117,8 @@ __global__ void __launch_bounds__(kSsspThreads)
   using V = typename A::V;
   using K = typename A::K;
   constexpr int VPW = 32 / LANES;  // lane groups (frontier vertices) per warp
-  constexpr int R = 4;             // frontier vertices per lane group per sweep
-  constexpr int G = 8;             // edges per lane group in flight
+  constexpr int R = 2;             // frontier vertices per lane group per sweep
+  constexpr int G = 8;             // edges per lane group in flight (<= LANES)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / LANES, sl = lane % LANES;
   const unsigned group_mask = LANES == 32 ? 0xffffffffu : (0xffffu << (16 * sub));
@@ -185,7 +185,9 @@ __global__ void __launch_bounds__(kSsspThreads)
         // A lane group takes R frontier vertices per sweep and walks their
         // concatenated out-edge lists G edges at a time: the loads of a
         // sweep's vertices, of G edges and the G atomics are each issued
-        // together, so a sweep costs four dependent round trips.
+        // together, so a sweep costs four dependent round trips.  Two
+        // vertices of one group can push the same target: the bitmap keeps
+        // one copy.
         for (int fb = warp * VPW * R; fb < f; fb += kSsspWarps * VPW * R) {
           int u[R];
 #pragma unroll
@@ -241,18 +243,30 @@ __global__ void __launch_bounds__(kSsspThreads)
 #pragma unroll
             for (int q = 0; q < G; q++)
               old[q] = live[q] ? atomicMin(&dvm[(size_t)v[q] * LANES + sl], A::key(c[q])) : (K)0;
+            // Which edge targets improved (for any source of the group) and
+            // whether below the threshold; then lane q of the group files
+            // target q, so the G pushes run side by side.
+            unsigned bi[G], bn[G];
 #pragma unroll
             for (int q = 0; q < G; q++) {
               const bool imp = live[q] && A::key(c[q]) < old[q];
-              const bool nearv = imp && c[q] < thr;
-              const unsigned bi = __ballot_sync(0xffffffffu, imp) & group_mask;
-              const unsigned bn = __ballot_sync(0xffffffffu, nearv) & group_mask;
-              if (bi != 0u && sl == 0) {
-                if (bn != 0u) {
-                  if (set_bit(nbits, v[q])) N[atomicAdd(&s_near[cur ^ 1], 1)] = v[q];
-                } else if (set_bit(farbits, v[q])) {
-                  FAR[atomicAdd(&s_far[fcur], 1)] = v[q];
-                }
+              bi[q] = __ballot_sync(0xffffffffu, imp) & group_mask;
+              bn[q] = __ballot_sync(0xffffffffu, imp && c[q] < thr) & group_mask;
+            }
+            int mv = v[0];
+            unsigned mi = bi[0], mn = bn[0];
+#pragma unroll
+            for (int q = 1; q < G; q++)
+              if (sl == q) {
+                mv = v[q];
+                mi = bi[q];
+                mn = bn[q];
+              }
+            if (sl < G && mi != 0u) {
+              if (mn != 0u) {
+                if (set_bit(nbits, mv)) N[atomicAdd(&s_near[cur ^ 1], 1)] = mv;
+              } else if (set_bit(farbits, mv)) {
+                FAR[atomicAdd(&s_far[fcur], 1)] = mv;
               }
             }
           }
@@ -322,70 +336,49 @@ __global__ void __launch_bounds__(kSsspThreads)
 
     // ---- predecessors and transposed output: warps work on their own
     // 32-vertex blocks and synchronize only within the warp.  A lane group
-    // takes R vertices at a time and scans their concatenated in-edge lists
-    // G edges at a time. ----
+    // takes two vertices at a time and scans their in-edge lists side by
+    // side (edge j of both per iteration), so their loads overlap. ----
     for (int v0 = warp * 32; v0 < n; v0 += kSsspWarps * 32) {
-      for (int vb = 0; vb < 32; vb += VPW * R) {
-        int vv[R], ib[R], pre[R + 1];
-        K dk[R], bdu[R];
-        int bu[R];
-        pre[0] = 0;
+      for (int vb = 0; vb < 32; vb += 2 * VPW) {
+        int vv[2], e0[2], deg[2], bu[2];
+        K dk[2], bdu[2];
+        V dvv[2];
 #pragma unroll
-        for (int i = 0; i < R; i++) {
+        for (int i = 0; i < 2; i++) {
           vv[i] = v0 + vb + i * VPW + sub;
           const bool in = vv[i] < n;
           dk[i] = (in && sl < cnt) ? __ldcg(&dvm[(size_t)vv[i] * LANES + sl]) : INF;
-          int e0 = 0, deg = 0;
-          if (PRED && in) {
-            e0 = a.iro[vv[i]];
-            deg = a.iro[vv[i] + 1] - e0;
-          }
-          pre[i + 1] = pre[i] + deg;
-          ib[i] = e0 - pre[i];
+          dvv[i] = A::val(dk[i]);
+          e0[i] = (PRED && in) ? a.iro[vv[i]] : 0;
+          deg[i] = (PRED && in) ? a.iro[vv[i] + 1] - e0[i] : 0;
           bdu[i] = ~(K)0;
           bu[i] = -1;
         }
         if (PRED) {
-          const int tot = pre[R];
-          int tmax = tot;
-          if (VPW == 2) tmax = max(tot, __shfl_xor_sync(0xffffffffu, tot, 16));
-          for (int t0 = 0; t0 < tmax; t0 += G) {
-            int uu[G], own[G];
-            unsigned wq[G];
+          int dmax = max(deg[0], deg[1]);
+          if (VPW == 2) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, 16));
+          for (int j = 0; j < dmax; j++) {
+            int u[2];
+            unsigned wq[2];
+            K duk[2];
 #pragma unroll
-            for (int q = 0; q < G; q++) {
-              const int t = t0 + q;
-              int e = ib[0] + t, o = 0;
-#pragma unroll
-              for (int i = 1; i < R; i++)
-                if (t >= pre[i]) {
-                  e = ib[i] + t;
-                  o = i;
-                }
-              const bool in = t < tot;
-              uu[q] = in ? a.icol[e] : -1;
-              wq[q] = in ? iwb[e] : 0u;
-              own[q] = o;
+            for (int i = 0; i < 2; i++) {
+              const bool has = j < deg[i];
+              u[i] = has ? a.icol[e0[i] + j] : 0;
+              wq[i] = has ? iwb[e0[i] + j] : 0u;
+              duk[i] = (has && dk[i] < INF) ? __ldcg(&dvm[(size_t)u[i] * LANES + sl]) : INF;
             }
-            K duk[G];
 #pragma unroll
-            for (int q = 0; q < G; q++) duk[q] = uu[q] >= 0 ? __ldcg(&dvm[(size_t)uu[q] * LANES + sl]) : INF;
-#pragma unroll
-            for (int q = 0; q < G; q++) {
-              const V cand = A::val(duk[q]) + A::weight(wq[q]);
-              const bool reached = duk[q] < INF;
-#pragma unroll
-              for (int i = 0; i < R; i++) {
-                const bool better = reached && own[q] == i && cand == A::val(dk[i]) &&
-                                    (duk[q] < bdu[i] || (duk[q] == bdu[i] && uu[q] < bu[i]));
-                bdu[i] = better ? duk[q] : bdu[i];
-                bu[i] = better ? uu[q] : bu[i];
-              }
+            for (int i = 0; i < 2; i++) {
+              const bool better = duk[i] < INF && A::val(duk[i]) + A::weight(wq[i]) == dvv[i] &&
+                                  (duk[i] < bdu[i] || (duk[i] == bdu[i] && u[i] < bu[i]));
+              bdu[i] = better ? duk[i] : bdu[i];
+              bu[i] = better ? u[i] : bu[i];
             }
           }
         }
 #pragma unroll
-        for (int i = 0; i < R; i++) {
+        for (int i = 0; i < 2; i++) {
           unsigned dv_out = Dist<T>::bits(Dist<T>::inf());
           int32_t p = -1;
           if (dk[i] < INF) {
