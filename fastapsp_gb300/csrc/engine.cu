@@ -116,7 +116,7 @@ struct Plan {
     std::vector<const MpSegment *> panel;
     std::vector<int> panel_nseg, panel_tiles;
     std::vector<const MpSegment *> rest;
-    std::vector<int> rest_nseg, rest_tiles;
+    std::vector<int> rest_nseg, rest_tiles, rest_strips;
     // min-plus
     const MpSegment *mp = nullptr;
     int mp_nseg = 0, mp_tiles = 0;
@@ -452,13 +452,14 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.panel_tiles.assign(maxnb, 0);
     G.rest_nseg.assign(maxnb, 0);
     G.rest_tiles.assign(maxnb, 0);
+    G.rest_strips.assign(maxnb, 0);
     O.diag.assign(maxnb, 0);
     O.panel.assign(maxnb, 0);
     O.rest.assign(maxnb, 0);
     for (int r = 0; r < maxnb; r++) {
       std::vector<FwDiagJob> dj;
       std::vector<MpSegment> ps, rs;
-      int pt = 0, rt = 0;
+      int pt = 0, rt = 0, rstrips = 0;
       for (const PartDesc &d : pdesc) {
         int nb = d.ld / B;
         if (r >= nb) continue;
@@ -483,6 +484,8 @@ int build_plan(fap_engine *e, Plan &pl) {
           ps.push_back(cp);
           rest.tile_begin = rt;
           rt += a3;
+          rest.strip_begin = rstrips;
+          rstrips += rest.tiles_x * ((rest.tiles_x + fapk::fw_strip_tiles() - 1) / fapk::fw_strip_tiles());
           rs.push_back(rest);
         }
       }
@@ -493,6 +496,7 @@ int build_plan(fap_engine *e, Plan &pl) {
       O.panel[r] = tb.add(ps.data(), ps.size());
       G.rest_nseg[r] = (int)rs.size();
       G.rest_tiles[r] = rt;
+      G.rest_strips[r] = rstrips;
       O.rest[r] = tb.add(rs.data(), rs.size());
     }
   }
@@ -596,7 +600,10 @@ struct Issuer {
     for (size_t r = 0; r < G.diag.size(); r++) {
       FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
-      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
+      if (packed)  // remaining tiles: strip form (rows x columns of the pivot-free lists)
+        FAP_CUDA(fapk::launch_fw_strips(pred, G.rest[r], G.rest_nseg[r], G.rest_strips[r], st));
+      else
+        FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
     }
     if (last) FAP_CUDA(rec(3));
     if (packed) {  // strip form for the small-K segments, tiles for the rest
@@ -1244,11 +1251,11 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   cudaStream_t st = pick_stream(e, stream);
   TableBuilder tb;
   std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb);
-  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb);
+  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), sr(maxnb);
   for (int r = 0; r < maxnb; r++) {
     std::vector<FwDiagJob> dj;
     std::vector<MpSegment> ps, rs;
-    int pt = 0, rt = 0;
+    int pt = 0, rt = 0, rstrips = 0;
     for (int32_t b = 0; b < count; b++) {
       int nb = (sizes[b] + Bk - 1) / Bk;
       if (r >= nb) continue;
@@ -1272,9 +1279,12 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
         ps.push_back(c);
         rest.tile_begin = rt;
         rt += t3;
+        rest.strip_begin = rstrips;
+        rstrips += rest.tiles_x * ((rest.tiles_x + fapk::fw_strip_tiles() - 1) / fapk::fw_strip_tiles());
         rs.push_back(rest);
       }
     }
+    sr[r] = rstrips;
     nd[r] = (int)dj.size();
     od[r] = tb.add(dj.data(), dj.size());
     np[r] = (int)ps.size();
@@ -1311,7 +1321,9 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   for (int r = 0; r < maxnb; r++) {
     FAP_CUDA(fapk::launch_fw_diag(f32, pred, reinterpret_cast<const FwDiagJob *>(base + od[r]), nd[r], st));
     FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], packed, st));
-    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]), nr[r], tr[r], packed, st));
+    const MpSegment *rseg = reinterpret_cast<const MpSegment *>(base + orr[r]);
+    if (packed) FAP_CUDA(fapk::launch_fw_strips(pred, rseg, nr[r], sr[r], st));
+    else FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, rseg, nr[r], tr[r], packed, st));
   }
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);
@@ -1415,7 +1427,7 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes, int32
 }
 
 int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s) {
-  if (!e || !ops_per_s || mode < 0 || mode > 3) return set_error(FAP_ERR_INVALID, "fap_addmin_peak: bad arguments");
+  if (!e || !ops_per_s || mode < 0 || mode > 5) return set_error(FAP_ERR_INVALID, "fap_addmin_peak: bad arguments");
   std::lock_guard<std::mutex> lk(e->mu);
   DeviceGuard dg(e->device);
   FAP_CUDA(fapk::measure_addmin_peak(mode, e->sm_count, ops_per_s));

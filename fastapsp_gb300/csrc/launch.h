@@ -23,6 +23,12 @@ cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, i
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
                                   int max_k, cudaStream_t st);
 int minplus_strip_tiles();
+// Strip form of the FW remaining-tile phase (packed int32, init_from_c = 1,
+// K <= 64): CTAs numbered by MpSegment::strip_begin, tiles_y x
+// ceil(tiles_x / fw_strip_tiles()) strips per segment.
+cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
+                             cudaStream_t st);
+int fw_strip_tiles();
 int minplus_strip_max_k();
 // Largest finite int32 entry of the matrices, atomicMax-ed into *out.
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st);

@@ -506,19 +506,28 @@ __global__ void __launch_bounds__(kThreads, 2)
 // Strip form of the packed min-plus for products that do not accumulate into
 // C (the inner rows of every part) with K <= kStripMaxK.  One CTA owns a
 // strip: one 128-row tile of a segment and up to kStripTiles consecutive
-// 128-column tiles.  A's 128 x K block is staged once per strip; B's K x 128
-// tiles are double-buffered, so the next tile's copy is in flight while the
-// current one is multiplied; B's predecessor rows and the own-part column
-// flags of the next tile are staged right after each epilogue, behind the
-// next tile's DPX loop.  The descriptor search, the staging of A and the
-// pipeline fill of the tile kernel are paid once per strip instead of once
-// per tile.  Shared memory (ks = K rounded up to 4):
-//   B[2][ks][128] | Bp[ks][128] | colp[128] | coll[128] | A[128][ks + 1]
+// 128-column tiles, two CTAs per SM.  A's 128 x K block is staged once per
+// strip (transposed, so that a thread's 8 row operands of one k are two
+// 16-byte loads); B's K x 128 tiles are double-buffered, so the next tile's
+// copy is in flight while the current one is multiplied; B's predecessor
+// rows and the own-part column flags of the next tile are staged right after
+// each epilogue, behind the next tile's DPX loop.  The part's own columns of
+// a tile (the Floyd-Warshall values replace the product there) are listed
+// when the tile's column flags land, and the FW values of up to kOwnCap of
+// them are staged with cp.async behind the DPX loop; further own columns are
+// read from global memory in the epilogue.  The descriptor search, the
+// staging of A and the pipeline fill of the tile kernel are paid once per
+// strip instead of once per tile.  Shared memory (ks = K rounded up to 4):
+//   B[2][ks][128] | Bp[1 + ks][128] | colp[128] | coll[128] | ownidx[128] |
+//   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
+// Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
+// with the key's idx as it is (0 when unreached).
 constexpr int kStripTiles = 16;
 constexpr int kStripMaxK = 48;
+constexpr int kOwnCap = 12;
 
 __host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
-  return (size_t)3 * ks * kTile * 4 + (size_t)2 * kTile * 4 + (size_t)kTile * (ks + 1) * 4;
+  return (size_t)4 * ks * kTile * 4 + (size_t)4 * kTile * 4 + (size_t)2 * kOwnCap * kTile * 4;
 }
 
 __device__ __forceinline__ const MpSegment &find_strip_segment(const MpSegment *__restrict__ segs,
@@ -578,13 +587,21 @@ __global__ void __launch_bounds__(kThreads, 2)
     mp_strip_kernel(const MpSegment *__restrict__ segs, int nseg, int ks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned *Bs = reinterpret_cast<unsigned *>(smem_raw);  // [2][ks][128]
-  int32_t *Bps = reinterpret_cast<int32_t *>(Bs + 2 * ks * kTile);  // [ks][128]
-  int32_t *colp = Bps + ks * kTile;  // col_part of the tile's columns
-  int32_t *coll = colp + kTile;      // col_local of the tile's columns
-  unsigned *As = reinterpret_cast<unsigned *>(coll + kTile);  // [128][ks + 1]
-  const int apitch = ks + 1;
+  int32_t *Bps = reinterpret_cast<int32_t *>(Bs + 2 * ks * kTile);  // [1 + ks][128]
+  int32_t *colp = Bps + (ks + 1) * kTile;  // col_part of the tile's columns
+  int32_t *coll = colp + kTile;            // col_local of the tile's columns
+  int32_t *ownidx = coll + kTile;          // own column: staging slot, or -2 (not staged); else -1
+  unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + kTile);  // [kOwnCap][128]
+  int32_t *Fpst = reinterpret_cast<int32_t *>(Fst + kOwnCap * kTile);  // [kOwnCap][128]
+  unsigned *As = reinterpret_cast<unsigned *>(Fpst + kOwnCap * kTile);  // A^T [ks][128]
   __shared__ MpSegment seg;
-  if (threadIdx.x == 0) seg = find_strip_segment(segs, nseg, blockIdx.x);
+  __shared__ int s_own[2];                   // own columns of the tile (per tile parity)
+  __shared__ int16_t s_ownlist[2][kOwnCap];  // their tile columns, by slot
+  if (threadIdx.x == 0) {
+    seg = find_strip_segment(segs, nseg, blockIdx.x);
+    s_own[0] = s_own[1] = 0;
+  }
+  if (threadIdx.x < kTile) Bps[threadIdx.x] = -1;  // predecessor of idx 0
   __syncthreads();
   const MpSegment &s = seg;
   const int strips_x = (s.tiles_x + kStripTiles - 1) / kStripTiles;
@@ -602,7 +619,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 
   auto load_side = [&](int col0) {  // B's predecessor rows and column flags of a tile
     if (PRED)
-      strip_load_rows(reinterpret_cast<unsigned *>(Bps), reinterpret_cast<const unsigned *>(s.Bp),
+      strip_load_rows(reinterpret_cast<unsigned *>(Bps + kTile), reinterpret_cast<const unsigned *>(s.Bp),
                       s.ldbp, s.K, s.N, kseg, col0, vec_bp, 0xffffffffu);
     if (threadIdx.x < kTile) {
       const int j = threadIdx.x, col = col0 + j;
@@ -617,10 +634,12 @@ __global__ void __launch_bounds__(kThreads, 2)
 
   // Prologue: A and B of the first tile | side data of the first tile.
   for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
-    const int m = idx / kseg, kk = idx - m * kseg;
-    unsigned *d = &As[m * apitch + kk];
-    if (row0 + m < s.M && kk < s.K) cp_async4(d, static_cast<const unsigned *>(s.A) + (int64_t)(row0 + m) * s.lda + kk);
-    else *d = INF;
+    const int kk = idx >> 7, m = idx & (kTile - 1);
+    unsigned *d = &As[idx];
+    if (row0 + m < s.M && kk < s.K)
+      cp_async4(d, static_cast<const unsigned *>(s.A) + (int64_t)(row0 + m) * s.lda + kk);
+    else
+      *d = INF;
   }
   strip_load_rows(Bs, static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, kseg, jt0 * kTile, vec_b, INF);
   cp_async_commit();
@@ -636,33 +655,63 @@ __global__ void __launch_bounds__(kThreads, 2)
     cp_async_commit();
     cp_async_wait_1();  // all but the next tile's B have landed
     if (jt == jt0)
-      for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
-        const int m = idx / kseg, kk = idx - m * kseg;
-        As[m * apitch + kk] = min(As[m * apitch + kk], kPackH) << kIdxBits;
-      }
+      for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads)
+        As[idx] = min(As[idx], kPackH) << kIdxBits;
     strip_keys_b(Bcur, kseg);
+    // List the tile's own columns (threads 0..127 copied their column's flags;
+    // slots are taken in any order through a counter).
+    if (threadIdx.x == 0) s_own[buf ^ 1] = 0;  // used by the next tile
+    if (threadIdx.x < kTile) {
+      const int j = threadIdx.x;
+      const bool own = colp[j] == s.part;
+      const unsigned bal = __ballot_sync(0xffffffffu, own);
+      int base = 0;
+      if ((threadIdx.x & 31) == 0 && bal) base = atomicAdd(&s_own[buf], __popc(bal));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      int slot = -1;
+      if (own) {
+        slot = base + __popc(bal & ((1u << (threadIdx.x & 31)) - 1u));
+        if (slot < kOwnCap) s_ownlist[buf][slot] = (int16_t)j;
+        else slot = -2;
+      }
+      ownidx[j] = slot;
+    }
     __syncthreads();
+    const int nown = min(s_own[buf], kOwnCap);
+    if (nown > 0) {  // stage the FW values of the own columns (rows of this tile)
+      for (int it = threadIdx.x; it < nown * kTile; it += kThreads) {
+        const int sl = it / kTile, m = it - sl * kTile;
+        if (row0 + m < s.M) {
+          const int64_t off = (int64_t)(row0 + m) * s.ldf + (coll[s_ownlist[buf][sl]] - s.local0);
+          cp_async4(&Fst[sl * kTile + m], static_cast<const unsigned *>(s.F) + off);
+          if (PRED) cp_async4(&Fpst[sl * kTile + m], s.Fp + off);
+        }
+      }
+      cp_async_commit();
+    }
 
     unsigned acc[8][8];
 #pragma unroll
     for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 8; c++) acc[r][c] = kPackH << kIdxBits;
-    const unsigned *arow[8];
-#pragma unroll
-    for (int r = 0; r < 8; r++) arow[r] = As + ((r >> 2) * kBlk + ty * 4 + (r & 3)) * apitch;
-    const unsigned *bcol = Bcur + tx * 4;
-    for (int k0 = 0; k0 < kseg; k0 += 4) {
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int kk = k0 + u;
-        unsigned a[8], b[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) a[r] = arow[r][kk];
-        const uint4 b0 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile);
-        const uint4 b1 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile + kBlk);
-        b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
-        b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+    // Operands of step k + 1 are loaded while step k's 64 add-mins issue.
+    if (kseg > 0) {
+      const unsigned *acol = As + ty * 4;
+      const unsigned *bcol = Bcur + tx * 4;
+      uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
+      uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
+      uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
+      uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kBlk);
+#pragma unroll 2
+      for (int kk = 0; kk < kseg; kk++) {
+        const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
+        const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
+        const int kn = (kk + 1 < kseg ? kk + 1 : kk) * kTile;
+        na0 = *reinterpret_cast<const uint4 *>(acol + kn);
+        na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
+        nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
+        nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
 #pragma unroll
         for (int r = 0; r < 8; r++)
 #pragma unroll
@@ -670,9 +719,20 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
     }
 
+    if (nown > 0) {  // staged FW values visible to every thread
+      cp_async_wait_0();
+      __syncthreads();
+    }
     // Epilogue: distances, predecessors from the staged rows, own-part
-    // columns from the part's Floyd-Warshall matrix.
+    // columns from the part's Floyd-Warshall matrix (only when the tile has
+    // any; the test is uniform over the CTA).
     const int colbase = jt * kTile;
+    unsigned ownmask = 0;  // bit h * 4 + q: this thread's column sc0 + q of half h is the part's own
+    if (nown > 0) {
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        if (ownidx[(c >> 2) * kBlk + tx * 4 + (c & 3)] != -1) ownmask |= 1u << c;
+    }
 #pragma unroll
     for (int r = 0; r < 8; r++) {
       const int row = row0 + (r >> 2) * kBlk + ty * 4 + (r & 3);
@@ -690,14 +750,22 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int q = 0; q < 4; q++) {
           const unsigned key = acc[r][h * 4 + q];
           const unsigned dist = key >> kIdxBits;
-          const unsigned idx = key & kIdxMask;
           d[q] = dist >= kPackH ? INF : dist;
-          p[q] = -1;
-          if (PRED && dist < kPackH && idx != 0) p[q] = Bps[(idx - 1) * kTile + sc0 + q];
-          if (colp[sc0 + q] == s.part) {  // own-part column: the FW value
-            const int64_t fj = coll[sc0 + q] - s.local0;
-            d[q] = static_cast<const unsigned *>(s.F)[(int64_t)row * s.ldf + fj];
-            if (PRED) p[q] = s.Fp[(int64_t)row * s.ldf + fj];
+          if (PRED) p[q] = Bps[(key & kIdxMask) * kTile + sc0 + q];
+        }
+        if ((ownmask >> (h * 4)) & 0xfu) {
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            if (!((ownmask >> (h * 4 + q)) & 1u)) continue;
+            const int oi = ownidx[sc0 + q];
+            if (oi >= 0) {  // own-part column: the FW value, staged
+              d[q] = Fst[oi * kTile + row - row0];
+              if (PRED) p[q] = Fpst[oi * kTile + row - row0];
+            } else if (oi == -2) {  // own-part column beyond the staging slots
+              const int64_t fj = coll[sc0 + q] - s.local0;
+              d[q] = static_cast<const unsigned *>(s.F)[(int64_t)row * s.ldf + fj];
+              if (PRED) p[q] = s.Fp[(int64_t)row * s.ldf + fj];
+            }
           }
         }
         if (vec_c && col0 + 3 < s.N) {
@@ -715,6 +783,215 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     __syncthreads();  // B[buf], Bp and the column flags are free again
     if (jt + 1 < jt1) load_side((jt + 1) * kTile);
+    cp_async_commit();
+  }
+  cp_async_wait_0();
+}
+
+// Strip form of the accumulating packed product of the Floyd-Warshall
+// remaining-tile phase: D_ij = min(D_ij, D_ir (x) D_rj) with K <= 64 (one
+// pivot block), ties keeping D_ij.  One CTA per SM (197 KB of shared memory)
+// owns a strip: one row tile of the segment's row list (A = D_ir resident)
+// and up to kFwStripTiles column tiles of its column list.  Everything a tile
+// needs is in flight before it is needed: B (= D_rj) double-buffered, the
+// current tile's C staged behind its DPX loop, B's predecessors staged behind
+// the next tile's loop.  The product starts from "unreached" and C joins in
+// the epilogue with index 0, which gives the same minimum and tie rule as
+// starting from C.
+constexpr int kFwStripTiles = 4;
+
+struct FwStripSmem {
+  unsigned A[kBlk][kTile];       // A keys, transposed: pivot block x strip rows
+  unsigned B[2][kBlk][kTile];    // B keys of the current / next tile
+  int32_t Bp[kBlk][kTile];       // B's predecessors of the current tile
+  unsigned C[kTile][kTile];      // C of the current tile
+};
+
+__device__ __forceinline__ int fw_strips_x(const MpSegment &s) {
+  return (s.tiles_x + kFwStripTiles - 1) / kFwStripTiles;
+}
+
+// Copies rows [0, 64) of B-like data (row k at src + k * ld, columns of the
+// two 64-column blocks starting at cbase.x / cbase.y, -1 for none) into
+// dst[64][128]; 16-byte copies of 4 columns where aligned, `fill` outside the
+// matrix.
+__device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, int64_t ld, int K,
+                                          int N, int2 cbase, bool vec, unsigned fill) {
+  const int t = threadIdx.x;
+  const int j = (t & 31) * 4;
+  const int cb = (j >> 6) ? cbase.y : cbase.x;
+  const int col = cb + (j & 63);
+  for (int kk = t >> 5; kk < kBlk; kk += kThreads / 32) {
+    unsigned *d = dst + kk * kTile + j;
+    const unsigned *g = src + (int64_t)kk * ld + col;
+    if (cb >= 0 && kk < K && vec && col + 3 < N) {
+      cp_async16(d, g);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (cb >= 0 && kk < K && col + q < N) cp_async4(d + q, g + q);
+        else d[q] = fill;
+      }
+    }
+  }
+}
+
+template <bool PRED>
+__global__ void __launch_bounds__(kThreads, 1)
+    mp_fwstrip_kernel(const MpSegment *__restrict__ segs, int nseg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FwStripSmem &sm = *reinterpret_cast<FwStripSmem *>(smem_raw);
+  __shared__ MpSegment seg;
+  if (threadIdx.x == 0) seg = find_strip_segment(segs, nseg, blockIdx.x);
+  __syncthreads();
+  const MpSegment &s = seg;
+  const int sx = fw_strips_x(s);
+  const int local = blockIdx.x - s.strip_begin;
+  const int tyt = local / sx;
+  const int jt0 = (local - tyt * sx) * kFwStripTiles;
+  const int jt1 = min(jt0 + kFwStripTiles, s.tiles_x);
+  const int nbr = (s.M + kBlk - 1) / kBlk, nbc = (s.N + kBlk - 1) / kBlk;
+  const int rl0 = list_block(2 * tyt, s.row_skip, s.row_fix, nbr);
+  const int rl1 = list_block(2 * tyt + 1, s.row_skip, s.row_fix, nbr);
+  const int rbase0 = rl0 >= 0 ? rl0 * kBlk : -1, rbase1 = rl1 >= 0 ? rl1 * kBlk : -1;
+  auto col_bases = [&](int jt) {  // first columns of the tile's two blocks (-1: none)
+    const int b0 = list_block(2 * jt, s.col_skip, s.col_fix, nbc);
+    const int b1 = list_block(2 * jt + 1, s.col_skip, s.col_fix, nbc);
+    return make_int2(b0 >= 0 ? b0 * kBlk : -1, b1 >= 0 ? b1 * kBlk : -1);
+  };
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  const unsigned INF = Dist<uint32_t>::inf();
+  const int kseg = (s.K + 3) & ~3;
+  const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
+  const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
+  const bool vec_c = (s.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(s.C) & 15) == 0;
+
+  // Prologue: A (transposed) and the first B | the first B's predecessors.
+  for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads) {
+    const int kk = idx >> 7, m = idx & (kTile - 1);
+    const int rb = (m >> 6) ? rbase1 : rbase0;
+    const int row = rb + (m & 63);
+    unsigned *d = &sm.A[kk][m];
+    if (rb >= 0 && row < s.M && kk < s.K)
+      cp_async4(d, static_cast<const unsigned *>(s.A) + (int64_t)row * s.lda + kk);
+    else
+      *d = INF;
+  }
+  int2 cb = col_bases(jt0);
+  fw_load_b(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
+  cp_async_commit();
+  if (PRED)
+    fw_load_b(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
+              s.ldbp, s.K, s.N, cb, vec_bp, 0xffffffffu);
+  cp_async_commit();
+
+  for (int jt = jt0; jt < jt1; jt++) {
+    const int buf = (jt - jt0) & 1;
+    cb = col_bases(jt);
+    if (jt + 1 < jt1)
+      fw_load_b(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
+                col_bases(jt + 1), vec_b, INF);
+    cp_async_commit();
+    cp_async_wait_1();  // A, this tile's B and its predecessors have landed
+    if (jt == jt0)
+      for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads)
+        (&sm.A[0][0])[idx] = min((&sm.A[0][0])[idx], kPackH) << kIdxBits;
+    {
+      const int j = (threadIdx.x & 31) * 4;
+      for (int kk = threadIdx.x >> 5; kk < kBlk; kk += kThreads / 32) {
+        uint4 *p = reinterpret_cast<uint4 *>(&sm.B[buf][kk][j]);
+        const unsigned idx = (unsigned)kk + 1u;
+        uint4 v = *p;
+        v.x = (min(v.x, kPackH) << kIdxBits) | idx;
+        v.y = (min(v.y, kPackH) << kIdxBits) | idx;
+        v.z = (min(v.z, kPackH) << kIdxBits) | idx;
+        v.w = (min(v.w, kPackH) << kIdxBits) | idx;
+        *p = v;
+      }
+    }
+    __syncthreads();
+    // Stage this tile's C behind the DPX loop.
+    {
+      const int j = (threadIdx.x & 31) * 4;
+      const int cbj = (j >> 6) ? cb.y : cb.x;
+      const int col = cbj + (j & 63);
+      for (int m = threadIdx.x >> 5; m < kTile; m += kThreads / 32) {
+        const int rb = (m >> 6) ? rbase1 : rbase0;
+        const int row = rb + (m & 63);
+        unsigned *d = &sm.C[m][j];
+        const unsigned *g = static_cast<const unsigned *>(s.C) + (int64_t)row * s.ldc + col;
+        if (rb >= 0 && row < s.M && cbj >= 0 && vec_c && col + 3 < s.N) {
+          cp_async16(d, g);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            if (rb >= 0 && row < s.M && cbj >= 0 && col + q < s.N) cp_async4(d + q, g + q);
+            else d[q] = INF;
+          }
+        }
+      }
+      cp_async_commit();
+    }
+
+    unsigned acc[8][8];
+#pragma unroll
+    for (int r = 0; r < 8; r++)
+#pragma unroll
+      for (int c = 0; c < 8; c++) acc[r][c] = kPackH << kIdxBits;
+    if (kseg > 0) {  // operands of step k + 1 load while step k issues
+      const unsigned *acol = &sm.A[0][ty * 4];
+      const unsigned *bcol = &sm.B[buf][0][tx * 4];
+      uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
+      uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
+      uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
+      uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kBlk);
+#pragma unroll 2
+      for (int kk = 0; kk < kseg; kk++) {
+        const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
+        const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
+        const int kn = (kk + 1 < kseg ? kk + 1 : kk) * kTile;
+        na0 = *reinterpret_cast<const uint4 *>(acol + kn);
+        na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
+        nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
+        nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+#pragma unroll
+          for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+      }
+    }
+    cp_async_wait_0();
+    __syncthreads();  // C staged by every thread
+
+    // Epilogue: C joins with index 0; only strict improvements are stored.
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const int m = (r >> 2) * kBlk + ty * 4 + (r & 3);
+      const int rb = (r >> 2) ? rbase1 : rbase0;
+      const int row = rb + ty * 4 + (r & 3);
+      if (rb < 0 || row >= s.M) continue;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int cbh = h ? cb.y : cb.x;
+        if (cbh < 0) continue;
+        const int sc0 = h * kBlk + tx * 4;
+        const uint4 cv = *reinterpret_cast<const uint4 *>(&sm.C[m][sc0]);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int col = cbh + tx * 4 + q;
+          const unsigned cq = q == 0 ? cv.x : q == 1 ? cv.y : q == 2 ? cv.z : cv.w;
+          const unsigned key = min(min(cq, kPackH) << kIdxBits, acc[r][h * 4 + q]);
+          const unsigned idx = key & kIdxMask;
+          if (idx == 0 || col >= s.N) continue;
+          static_cast<unsigned *>(s.C)[(int64_t)row * s.ldc + col] = key >> kIdxBits;
+          if (PRED) s.Cp[(int64_t)row * s.ldcp + col] = sm.Bp[idx - 1][sc0 + q];
+        }
+      }
+    }
+    __syncthreads();  // C, B[buf] and the predecessors are free again
+    if (PRED && jt + 1 < jt1)
+      fw_load_b(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
+                s.ldbp, s.K, s.N, col_bases(jt + 1), vec_bp, 0xffffffffu);
     cp_async_commit();
   }
   cp_async_wait_0();
@@ -826,6 +1103,13 @@ cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks
   return cudaGetLastError();
 }
 
+template <bool PRED>
+cudaError_t launch_fwstrip_t(const MpSegment *d_segs, int nseg, int strips, cudaStream_t st) {
+  if (strips <= 0 || nseg <= 0) return cudaSuccess;
+  mp_fwstrip_kernel<PRED><<<strips, kThreads, sizeof(FwStripSmem), st>>>(d_segs, nseg);
+  return cudaGetLastError();
+}
+
 template <typename T, bool PRED>
 cudaError_t set_mp_attr() {
   return cudaFuncSetAttribute(mp_tile_kernel<T, PRED>,
@@ -859,6 +1143,13 @@ cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, 
 }
 
 int minplus_strip_tiles() { return kStripTiles; }
+
+cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
+                             cudaStream_t st) {
+  return pred ? launch_fwstrip_t<true>(d_segs, nseg, strips, st)
+              : launch_fwstrip_t<false>(d_segs, nseg, strips, st);
+}
+int fw_strip_tiles() { return kFwStripTiles; }
 int minplus_strip_max_k() { return kStripMaxK; }
 
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st) {
@@ -895,7 +1186,14 @@ cudaError_t init_minplus_kernels() {
   if ((e = cudaFuncSetAttribute(mp_strip_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smax)) != cudaSuccess)
     return e;
-  return cudaFuncSetAttribute(mp_strip_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                smax)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(mp_fwstrip_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(FwStripSmem))) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(mp_fwstrip_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(FwStripSmem));
 }
 
 int minplus_tile_rows() { return kTile; }

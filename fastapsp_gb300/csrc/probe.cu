@@ -12,6 +12,9 @@
 //   mode 1: FP32 add-min        acc = fminf(a + b, acc)
 //   mode 2: int32 add-min keeping the argmin (the tile kernel's inner step)
 //   mode 3: FP32 add-min keeping the argmin
+//   mode 4: int32, two add-mins per step: two adds and one 3-input min (DPX)
+//   mode 5: FP32, two add-mins per step: one paired add (add.f32x2) and one
+//           3-input min
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -22,10 +25,26 @@ namespace fapk {
 
 namespace {
 
+__device__ __forceinline__ unsigned min3_u32(unsigned a, unsigned b, unsigned c) {
+  return __vimin3_u32(a, b, c);
+}
+__device__ __forceinline__ float min3_f32(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float2 add_f32x2(float2 a, float2 b) {
+  unsigned long long x, y, z;
+  x = (unsigned long long)__float_as_uint(a.x) | ((unsigned long long)__float_as_uint(a.y) << 32);
+  y = (unsigned long long)__float_as_uint(b.x) | ((unsigned long long)__float_as_uint(b.y) << 32);
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(z) : "l"(x), "l"(y));
+  return make_float2(__uint_as_float((unsigned)z), __uint_as_float((unsigned)(z >> 32)));
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int iters, unsigned seed) {
-  constexpr bool F = (MODE == 1 || MODE == 3);
-  constexpr bool ARG = (MODE >= 2);
+  constexpr bool F = (MODE == 1 || MODE == 3 || MODE == 5);
+  constexpr bool ARG = (MODE == 2 || MODE == 3);
   using T = typename std::conditional<F, float, unsigned>::type;
   T a[4][4], b[4][16], acc[4][16];
   int arg[4][16];
@@ -45,6 +64,26 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
       arg[r][c] = 0;
     }
   for (int it = 0; it < iters; it++) {
+    if (MODE == 4 || MODE == 5) {
+#pragma unroll
+      for (int s = 0; s < 4; s += 2)
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            if (MODE == 4) {
+              acc[r][c] = (T)min3_u32((unsigned)acc[r][c], (unsigned)a[s][r] + (unsigned)b[s][c],
+                                      (unsigned)a[s + 1][r] + (unsigned)b[s + 1][c]);
+            } else {
+              const float2 v = add_f32x2(make_float2((float)a[s][r], (float)a[s + 1][r]),
+                                         make_float2((float)b[s][c], (float)b[s + 1][c]));
+              acc[r][c] = (T)min3_f32((float)acc[r][c], v.x, v.y);
+            }
+          }
+#pragma unroll
+      for (int i = 0; i < 16; i++) b[it & 3][i] = b[it & 3][i] - (T)1;
+      continue;
+    }
 #pragma unroll
     for (int s = 0; s < 4; s++) {
 #pragma unroll
@@ -105,7 +144,9 @@ cudaError_t measure_addmin_peak(int mode, int sm_count, double *ops_per_s) {
       case 0: e = run_mode<0>(buf, blocks, iters, 0); break;
       case 1: e = run_mode<1>(buf, blocks, iters, 0); break;
       case 2: e = run_mode<2>(buf, blocks, iters, 0); break;
-      default: e = run_mode<3>(buf, blocks, iters, 0); break;
+      case 3: e = run_mode<3>(buf, blocks, iters, 0); break;
+      case 4: e = run_mode<4>(buf, blocks, iters, 0); break;
+      default: e = run_mode<5>(buf, blocks, iters, 0); break;
     }
     cudaEventRecord(b, 0);
     if (e != cudaSuccess) break;

@@ -266,7 +266,9 @@ int fap_sssp_stats(fap_engine *e, uint64_t *out5);
  * (no reference counterpart; the roofline denominator of the FW and min-plus
  * phases).  mode 0: int32 DPX add-min (__viaddmin_u32); 1: FP32
  * fminf(a + b, c); 2: int32 add-min keeping the argmin; 3: FP32 add-min
- * keeping the argmin. */
+ * keeping the argmin; 4: int32, two add-mins as two adds and one 3-input
+ * min; 5: FP32, two add-mins as one paired add (add.f32x2) and one 3-input
+ * min. */
 int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s);
 
 #ifdef __cplusplus
