@@ -35,6 +35,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+MP_TRAFFIC_PER_OUTPUT_BYTE = 1.184  # DRAM read+write per output byte of the min-plus launch (ncu)
 METRIC = "APSP distances/s"
 UNIT = "distances/s"
 HBM_PEAK_FALLBACK = 6800.0
@@ -253,12 +254,12 @@ def run_ours(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": {
-            "workload": "directed 3-NN geometric graph, n=65536, int weights U[1,1000], K=64 parts, "
-                        "all parts solved (solveSubGraph 1..64 rows), int32 dist + pred",
+            "workload": f"directed 3-NN geometric graph, n={n}, int weights U[1,1000], K={K} parts, "
+                        f"all parts solved (solveSubGraph 1..{K} rows), int32 dist + pred",
             "n": n, "m": int(g.m), "K": K, "edge_cut": cut, "boundary_vertices": srcs,
             "mode": "batched (one launch per phase, CUDA graph)",
             "sssp_delta": tuned_delta,
-            "l2": "L2 flushed (256 MiB write) before every timed step; outputs 34 GB >> L2",
+            "l2": f"L2 flushed (256 MiB write) before every timed step; outputs {n * n * 8 / 1e9:.1f} GB",
             "parallelism": f"replicas x{world}",
         },
         "e2e": {"value": world * float(n) * n / (e2e_ms_step / 1e3), "unit": UNIT,
@@ -268,9 +269,15 @@ def run_ours(args, rank, world, local_rank):
                     " (SSSP step set to the value tuned on this graph)"},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {
-            "kernel": "mp_tile_kernel (min-plus, inner rows)", "bound": "alu",
+            "kernel": "mp_strip_kernel (min-plus of the inner rows; parts with more than 48 boundary "
+                      "vertices: mp_tile_packed_kernel)", "bound": "alu",
             "achieved": mp_rate / 1e9, "peak": peak_dpx / 1e9, "unit": "Gaddmin/s",
-            "frac": mp_rate / peak_dpx, "traffic": None,
+            "frac": mp_rate / peak_dpx,
+            # DRAM bytes per launch: an ncu capture of the same launch at n=24,576 read + wrote
+            # 1.184x its output bytes; the output grows with n^2 like the work, so the full
+            # launch is scaled by its output bytes.
+            "traffic": MP_TRAFFIC_PER_OUTPUT_BYTE * mp_bytes,
+            "traffic_source": "ncu capture at n=24,576 (1.184 DRAM bytes per output byte), scaled",
             "peak_source": "fap_addmin_peak mode 0 (int32 DPX add-min from registers), measured in this run",
             "peak_with_argmin": peak_arg / 1e9,
             "algorithmic_addmins_per_launch": addmin_mp,
@@ -349,7 +356,7 @@ def run_reference(args):
         "ms_per_step": statistics.mean(meas) * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (reference arithmetic; integer weights exact)",
         "data": "synthetic",
-        "config": {"workload": "directed 3-NN geometric graph, n=65536, int weights U[1,1000], K=64 parts",
+        "config": {"workload": f"directed 3-NN geometric graph, n={g.n}, int weights U[1,1000], K={K} parts",
                    "n": g.n, "m": int(g.m), "K": K},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
