@@ -96,6 +96,11 @@ struct Plan {
   int32_t *pred = nullptr;
   std::vector<int32_t> parts;
   std::vector<int64_t> row_offs;
+  // Boundary rows in their own device buffer (null: in dist/pred with the
+  // part's other rows): part i's boundary rows start at element brow_offs[i].
+  void *bdist = nullptr;
+  int32_t *bpred = nullptr;
+  std::vector<int64_t> brow_offs;
   std::vector<const void *> sig;  // engine work buffers the tables point into
   // device tables (one allocation)
   DevBuf tables;
@@ -186,6 +191,7 @@ struct fap_engine {
   DevBuf sssp_scratch, sssp_bits;
   int sssp_slots_alloc = 0;
   DevBuf res_d, res_p;         // device results when the caller passes host memory
+  DevBuf bnd_d, bnd_p;         // boundary rows when the inner rows go straight to mapped host memory
   DevBuf small;                // tables of standalone calls
   std::vector<std::unique_ptr<Plan>> plans;
   double times[5] = {0, 0, 0, 0, 0};
@@ -351,6 +357,9 @@ int build_plan(fap_engine *e, Plan &pl) {
   int32_t *fwp = static_cast<int32_t *>(e->fw_p.p);
   const bool pred = pl.pred != nullptr;
   char *dist = static_cast<char *>(pl.dist);
+  // where the boundary rows live: their own buffer, or the part's rows
+  char *bdist = pl.bdist ? static_cast<char *>(pl.bdist) : dist;
+  int32_t *bpred = pl.bdist ? pl.bpred : pl.pred;
 
   TableBuilder tb;
   struct GroupOffs {
@@ -374,13 +383,14 @@ int build_plan(fap_engine *e, Plan &pl) {
       int p = pl.parts[idx];
       int sub = e->ver_num[p], bdy = e->bdy_num[p], start = e->ver_offset[p];
       int64_t roff = pl.row_offs[idx];
+      int64_t boff = pl.bdist ? pl.brow_offs[idx] : roff;  // first boundary row
       const int L = pl.sssp_lanes;
       for (int b0 = 0; b0 < bdy; b0 += L) {
         SsspBatch sb{};
         sb.count = std::min(L, bdy - b0);
         for (int l = 0; l < sb.count; l++) {
           sb.src[l] = e->st2ed[start + b0 + l];
-          sb.row_off[l] = roff + (int64_t)(b0 + l) * n;
+          sb.row_off[l] = boff + (int64_t)(b0 + l) * n;
         }
         batches.push_back(sb);
       }
@@ -392,7 +402,7 @@ int build_plan(fap_engine *e, Plan &pl) {
       d.start = start;
       d.ld = ldv[idx];
       d.mat_off = mat_off[idx];
-      d.row_off = roff;
+      d.row_off = boff;
       pdesc.push_back(d);
       row_begin.push_back(row_begin.back() + d.ld);
       dec_begin.push_back(dec_begin.back() + bdy);
@@ -404,7 +414,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         int tiles = 0;
         const size_t es = 4;
         MpSegment s = mp_segment(fwd + (size_t)(mat_off[idx] + (int64_t)bdy * d.ld) * es, d.ld,
-                                 dist + (size_t)roff * es, n, pred ? pl.pred + roff : nullptr, n,
+                                 bdist + (size_t)boff * es, n, pred ? bpred + boff : nullptr, n,
                                  dist + (size_t)(roff + (int64_t)bdy * n) * es, n,
                                  pred ? pl.pred + roff + (int64_t)bdy * n : nullptr, n, inner,
                                  (int)n, bdy, tiles);
@@ -542,8 +552,8 @@ fapk::BuildArgs build_args(fap_engine *e, const Plan &pl, const Plan::Group &G) 
   a.dec_rows = G.dec_rows;
   a.mat = e->fw_d.p;
   a.matp = pl.pred ? static_cast<int32_t *>(e->fw_p.p) : nullptr;
-  a.rows = pl.dist;
-  a.rowsp = pl.pred;
+  a.rows = pl.bdist ? pl.bdist : pl.dist;  // the boundary rows
+  a.rowsp = pl.bdist ? pl.bpred : pl.pred;
   a.ldr = e->n;
   return a;
 }
@@ -573,8 +583,8 @@ struct Issuer {
     sa.iw = e->d_iw;
     sa.batches = G.batches;
     sa.nbatches = G.nbatches;
-    sa.dist = pl.dist;
-    sa.pred = pl.pred;
+    sa.dist = pl.bdist ? pl.bdist : pl.dist;  // SSSP rows are the boundary rows
+    sa.pred = pl.bdist ? pl.bpred : pl.pred;
     sa.scratch = e->sssp_scratch.p;
     sa.slots = std::min(G.nbatches, e->sssp_slots_alloc);
     sa.bits = e->sssp_bits.p;
@@ -614,7 +624,8 @@ struct Issuer {
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, packed, st));
     }
     if (last) FAP_CUDA(rec(4));
-    FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, st));
+    FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.bdist ? pl.bdist : pl.dist,
+                                 pl.bdist ? pl.bpred : pl.pred, st));
     if (last) FAP_CUDA(rec(5));
     return FAP_OK;
   }
@@ -731,18 +742,22 @@ std::vector<const void *> buffer_signature(const fap_engine *e) {
 }
 
 Plan *find_plan(fap_engine *e, int mode, void *dist, int32_t *pred,
-                const std::vector<int32_t> &parts, const std::vector<int64_t> &offs) {
+                const std::vector<int32_t> &parts, const std::vector<int64_t> &offs, void *bdist,
+                int32_t *bpred) {
   const std::vector<const void *> sig = buffer_signature(e);
   for (auto &p : e->plans)
     if (p->mode == mode && p->dist == dist && p->pred == pred && p->parts == parts &&
-        p->row_offs == offs && p->sig == sig)
+        p->row_offs == offs && p->bdist == bdist && p->bpred == bpred && p->sig == sig)
       return p.get();
   return nullptr;
 }
 
-// Runs `parts` (row offsets `offs` into the device buffers dist/pred).
+// Runs `parts` (row offsets `offs` into dist/pred, device-accessible).  With
+// bdist, the parts' boundary rows go to that device buffer instead (part i's
+// at element boffs[i]) and dist/pred receive only the inner rows.
 int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vector<int32_t> &parts,
-              const std::vector<int64_t> &offs, cudaStream_t st) {
+              const std::vector<int64_t> &offs, cudaStream_t st, void *bdist = nullptr,
+              int32_t *bpred = nullptr, const std::vector<int64_t> &boffs = {}) {
   int rc;
   // work buffers
   size_t fw_elems = 0;
@@ -761,7 +776,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e));
   if ((rc = ensure_sssp_scratch(e, slots)) != FAP_OK) return rc;
 
-  Plan *pl = find_plan(e, mode, dist, pred, parts, offs);
+  Plan *pl = find_plan(e, mode, dist, pred, parts, offs, bdist, bpred);
   if (!pl) {
     if (e->plans.size() >= 8) e->plans.erase(e->plans.begin());
     auto np = std::make_unique<Plan>();
@@ -770,6 +785,9 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     np->pred = pred;
     np->parts = parts;
     np->row_offs = offs;
+    np->bdist = bdist;
+    np->bpred = bpred;
+    np->brow_offs = boffs;
     np->sig = buffer_signature(e);
     np->sssp_lanes = lanes;
     if ((rc = build_plan(e, *np)) != FAP_OK) return rc;
@@ -1079,6 +1097,8 @@ int fap_destroy(fap_engine *e) {
     e->sssp_bits.release();
     e->res_d.release();
     e->res_p.release();
+    e->bnd_d.release();
+    e->bnd_p.release();
     e->small.release();
     void *ptrs[] = {e->d_ro, e->d_col, e->d_iro, e->d_icol, e->d_gid, e->d_st2ed, e->d_ed2st,
                     e->d_w, e->d_iw, e->d_status, e->d_stats};
@@ -1126,6 +1146,17 @@ int fap_part_info(const fap_engine *e, int32_t part, int32_t *sub, int32_t *bdy,
   return FAP_OK;
 }
 
+// Device address of page-locked, mapped host memory (null otherwise).
+static void *mapped_host_ptr(void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
 static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_t rows, void *dist,
                         int32_t *pred, int mode, void *stream) {
   std::lock_guard<std::mutex> lk(e->mu);
@@ -1135,26 +1166,59 @@ static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_
   const size_t bytes = (size_t)rows * e->n * 4;
   const bool dev_d = is_device_ptr(dist);
   const bool dev_p = pred == nullptr || is_device_ptr(pred);
-  void *dd = dist;
-  int32_t *dp = pred;
-  int rc;
-  if (!dev_d) {
-    if ((rc = e->res_d.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
-    dd = e->res_d.p;
-  }
-  if (pred && !dev_p) {
-    if ((rc = e->res_p.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
-    dp = static_cast<int32_t *>(e->res_p.p);
-  }
   std::vector<int64_t> offs;
   int64_t acc = 0;
   for (int32_t p : parts) {
     offs.push_back(acc * e->n);
     acc += e->ver_num[p];
   }
-  if ((rc = run_parts(e, mode, dd, dp, parts, offs, st)) != FAP_OK) return rc;
-  if (!dev_d) FAP_CUDA(cudaMemcpyAsync(dist, dd, bytes, cudaMemcpyDeviceToHost, st));
-  if (pred && !dev_p) FAP_CUDA(cudaMemcpyAsync(pred, dp, bytes, cudaMemcpyDeviceToHost, st));
+  int rc;
+  // Page-locked host results: the kernels write the inner rows straight into
+  // them (no device copy of the n x n result, and the copy-out overlaps the
+  // min-plus); the boundary rows, which the FW build and the min-plus read
+  // back, stay in a device buffer and are copied out at the end.
+  void *hd = dev_d ? nullptr : mapped_host_ptr(dist);
+  void *hp = (pred && !dev_p) ? mapped_host_ptr(pred) : nullptr;
+  if (!dev_d && hd && (pred == nullptr || hp)) {
+    std::vector<int64_t> boffs;
+    int64_t bacc = 0;
+    for (int32_t p : parts) {
+      boffs.push_back(bacc * e->n);
+      bacc += e->bdy_num[p];
+    }
+    const size_t bbytes = std::max<size_t>((size_t)bacc * e->n * 4, 4);
+    if ((rc = e->bnd_d.ensure(bbytes)) != FAP_OK) return rc;
+    if (pred && (rc = e->bnd_p.ensure(bbytes)) != FAP_OK) return rc;
+    int32_t *bp = pred ? static_cast<int32_t *>(e->bnd_p.p) : nullptr;
+    if ((rc = run_parts(e, mode, hd, static_cast<int32_t *>(hp), parts, offs, st, e->bnd_d.p, bp,
+                        boffs)) != FAP_OK)
+      return rc;
+    for (size_t i = 0; i < parts.size(); i++) {
+      const size_t rb = (size_t)e->bdy_num[parts[i]] * e->n * 4;
+      if (rb == 0) continue;
+      FAP_CUDA(cudaMemcpyAsync(static_cast<char *>(dist) + offs[i] * 4,
+                               static_cast<char *>(e->bnd_d.p) + boffs[i] * 4, rb,
+                               cudaMemcpyDeviceToHost, st));
+      if (pred)
+        FAP_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(pred) + offs[i] * 4,
+                                 static_cast<char *>(e->bnd_p.p) + boffs[i] * 4, rb,
+                                 cudaMemcpyDeviceToHost, st));
+    }
+  } else {
+    void *dd = dist;
+    int32_t *dp = pred;
+    if (!dev_d) {
+      if ((rc = e->res_d.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
+      dd = e->res_d.p;
+    }
+    if (pred && !dev_p) {
+      if ((rc = e->res_p.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
+      dp = static_cast<int32_t *>(e->res_p.p);
+    }
+    if ((rc = run_parts(e, mode, dd, dp, parts, offs, st)) != FAP_OK) return rc;
+    if (!dev_d) FAP_CUDA(cudaMemcpyAsync(dist, dd, bytes, cudaMemcpyDeviceToHost, st));
+    if (pred && !dev_p) FAP_CUDA(cudaMemcpyAsync(pred, dp, bytes, cudaMemcpyDeviceToHost, st));
+  }
   FAP_CUDA(cudaStreamSynchronize(st));
   if (mode == FAP_MODE_BATCHED && st != e->stream) FAP_CUDA(cudaStreamSynchronize(e->stream));
   read_times(e);

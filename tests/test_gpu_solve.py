@@ -110,3 +110,29 @@ def test_fapgraph_mirror_solve_and_split(gpu):
     assert np.array_equal(G.getSubGraphDistance(2), z["dist"][off:off + sub])
     assert np.array_equal(G.getSubGraphIndex(2), z["mapping"][off:off + sub])
     G.close()
+
+
+@pytest.mark.parametrize("name", INT_CASES[:4] + F32_CASES[:1])
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("with_pred", [True, False])
+def test_solve_into_page_locked_host_rows(gpu, name, mode, with_pred):
+    """Page-locked host results take the direct path (inner rows written by
+    the kernels into host memory, boundary rows copied out): same rows as a
+    device-resident solve, on two calls in a row."""
+    z, g = load_golden(name)
+    n = g.n
+    dtype = gpu.DTYPE_F32 if name.endswith("f32") else gpu.DTYPE_I32
+    tdt = torch.float32 if dtype == gpu.DTYPE_F32 else torch.int32
+    with gpu.Engine(n, g.row_offset, g.col_val, g.weight, int(z["K"]), graph_id=z["graph_id"],
+                    dtype=dtype) as eng:
+        dd = torch.empty((n, n), dtype=tdt, device="cuda")
+        pd = torch.empty((n, n), dtype=torch.int32, device="cuda") if with_pred else None
+        eng.solve(dd, pd, mode)
+        torch.cuda.synchronize()
+        for _ in range(2):
+            dh = torch.full((n, n), 7, dtype=tdt).pin_memory()
+            ph = torch.full((n, n), 7, dtype=torch.int32).pin_memory() if with_pred else None
+            eng.solve(dh, ph, mode)
+            assert torch.equal(dh, dd.cpu())
+            if with_pred:
+                assert torch.equal(ph, pd.cpu())
