@@ -608,8 +608,12 @@ struct Issuer {
     FAP_CUDA(fapk::launch_build(f32, pred, ba, st));
     if (last) FAP_CUDA(rec(2));
     for (size_t r = 0; r < G.diag.size(); r++) {
-      FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
-      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
+      if (packed) {  // pivot block and both panels in one launch
+        FAP_CUDA(fapk::launch_fw_pivot(pred, G.diag[r], G.diag_cnt[r], st));
+      } else {
+        FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
+        FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
+      }
       if (packed)  // remaining tiles: strip form (rows x columns of the pivot-free lists)
         FAP_CUDA(fapk::launch_fw_strips(pred, G.rest[r], G.rest_nseg[r], G.rest_strips[r], st));
       else
@@ -1383,8 +1387,13 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
     packed = (unsigned long long)mx * (unsigned long long)std::max(max_size - 1, 1) < fapk::pack_limit();
   }
   for (int r = 0; r < maxnb; r++) {
-    FAP_CUDA(fapk::launch_fw_diag(f32, pred, reinterpret_cast<const FwDiagJob *>(base + od[r]), nd[r], st));
-    FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], packed, st));
+    const FwDiagJob *djobs = reinterpret_cast<const FwDiagJob *>(base + od[r]);
+    if (packed) {  // pivot block and both panels in one launch
+      FAP_CUDA(fapk::launch_fw_pivot(pred, djobs, nd[r], st));
+    } else {
+      FAP_CUDA(fapk::launch_fw_diag(f32, pred, djobs, nd[r], st));
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], packed, st));
+    }
     const MpSegment *rseg = reinterpret_cast<const MpSegment *>(base + orr[r]);
     if (packed) FAP_CUDA(fapk::launch_fw_strips(pred, rseg, nr[r], sr[r], st));
     else FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, rseg, nr[r], tr[r], packed, st));

@@ -22,6 +22,7 @@
 // min(D_ij, D_ir (x) D_rj).  Ties keep the current value, so predecessors
 // follow P[i][j] = P[k][j] on strict improvement as in the reference.
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -1082,6 +1083,178 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Pivot step of one FW round in the packed int32 form, for every matrix of
+// the batch: a cluster of two CTAs per matrix.  CTA 0 closes the pivot block
+// (as fw_diag_kernel) and writes it back; after a cluster barrier CTA 1 copies
+// the closed block out of CTA 0's shared memory (no second closure, and no
+// read of the block while it is being written).  Then CTA 0 updates the row
+// panel D_rb = min(D_rb, D_rr (x) D_rb) and CTA 1 the column panel
+// D_br = min(D_br, D_br (x) D_rr), block by block, with the next block's copy
+// in flight (cp.async) while the current one is multiplied: 64x64 outputs,
+// 4x4 per thread, packed keys, the block's own values joining with index 0.
+// One launch replaces the diagonal launch and the panel launch of the tile
+// kernel (whose 128x128 tiles were half empty for 64-wide panels).
+struct PivotSmem {
+  unsigned D[kBlk][kBlk + 1];  // pivot block values (closure)
+  int32_t P[kBlk][kBlk + 1];   // and predecessors
+  unsigned Kp[kBlk][kBlk];     // pivot keys: A^T (row panel) or B (column panel)
+  unsigned Xv[2][kBlk][kBlk];  // panel block values, double-buffered
+  int32_t Xp[2][kBlk][kBlk];   // and predecessors
+  unsigned Kx[kBlk][kBlk];     // keys of the current panel block: B (row panel) or A^T (column)
+};
+
+template <bool PRED>
+__device__ __forceinline__ void pivot_load_block(PivotSmem &sm, int buf, const FwDiagJob &job,
+                                                 int rb, int cb) {
+  const unsigned *Dg = static_cast<const unsigned *>(job.D);
+  for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
+    const int i = idx >> 6, j = idx & 63;
+    const int gi = rb * kBlk + i, gj = cb * kBlk + j;
+    if (gi < job.size && gj < job.size) {
+      cp_async4(&sm.Xv[buf][i][j], Dg + (int64_t)gi * job.ld + gj);
+      if (PRED) cp_async4(&sm.Xp[buf][i][j], job.P + (int64_t)gi * job.ld + gj);
+    } else {
+      sm.Xv[buf][i][j] = Dist<uint32_t>::inf();
+      if (PRED) sm.Xp[buf][i][j] = -1;
+    }
+  }
+}
+
+template <bool PRED>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+    fw_pivot_kernel(const FwDiagJob *__restrict__ jobs) {
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PivotSmem &sm = *reinterpret_cast<PivotSmem *>(smem_raw);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int role = (int)cluster.block_rank();  // 0: pivot block + row panel, 1: column panel
+  const FwDiagJob job = jobs[blockIdx.x >> 1];
+  const int r = job.block;
+  const int nb = (job.size + kBlk - 1) / kBlk;
+  const int npanel = nb - 1;
+  const unsigned INF = Dist<uint32_t>::inf();
+  auto panel_block = [&](int i) { return i < r ? i : i + 1; };  // i-th block other than r
+
+  if (npanel > 0) {
+    if (role == 0) pivot_load_block<PRED>(sm, 0, job, r, panel_block(0));
+    else pivot_load_block<PRED>(sm, 0, job, panel_block(0), r);
+  }
+  cp_async_commit();
+
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  if (role == 0) {
+    unsigned *Dg = static_cast<unsigned *>(job.D);
+    const int base = r * kBlk;
+    for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
+      const int i = idx >> 6, j = idx & 63;
+      const int gi = base + i, gj = base + j;
+      const bool ok = gi < job.size && gj < job.size;
+      sm.D[i][j] = ok ? Dg[(int64_t)gi * job.ld + gj] : (i == j ? 0u : INF);
+      if (PRED) sm.P[i][j] = ok ? job.P[(int64_t)gi * job.ld + gj] : -1;
+    }
+    __syncthreads();
+    for (int k = 0; k < kBlk; k++) {
+      unsigned a[4], b[4];
+      int32_t bp[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        a[q] = sm.D[ty * 4 + q][k];
+        b[q] = sm.D[k][tx * 4 + q];
+        if (PRED) bp[q] = sm.P[k][tx * 4 + q];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const unsigned v = Dist<uint32_t>::add(a[i], b[c]);
+          if (v < sm.D[ty * 4 + i][tx * 4 + c]) {
+            sm.D[ty * 4 + i][tx * 4 + c] = v;
+            if (PRED) sm.P[ty * 4 + i][tx * 4 + c] = bp[c];
+          }
+        }
+      __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
+      const int i = idx >> 6, j = idx & 63;
+      const int gi = base + i, gj = base + j;
+      if (gi < job.size && gj < job.size) {
+        Dg[(int64_t)gi * job.ld + gj] = sm.D[i][j];
+        if (PRED) job.P[(int64_t)gi * job.ld + gj] = sm.P[i][j];
+      }
+    }
+  }
+  cluster.sync();  // the closed pivot block is in CTA 0's shared memory
+  if (role == 1) {
+    const unsigned *rD = cluster.map_shared_rank(&sm.D[0][0], 0);
+    const int32_t *rP = cluster.map_shared_rank(&sm.P[0][0], 0);
+    for (int idx = threadIdx.x; idx < kBlk * (kBlk + 1); idx += kThreads) {
+      (&sm.D[0][0])[idx] = rD[idx];
+      if (PRED) (&sm.P[0][0])[idx] = rP[idx];
+    }
+  }
+  cluster.sync();  // CTA 0's shared memory is no longer read; CTA 1's copy is complete
+  for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
+    const int i = idx >> 6, j = idx & 63;
+    if (role == 0) sm.Kp[j][i] = min(sm.D[i][j], kPackH) << kIdxBits;  // A^T, idx 0
+    else sm.Kp[i][j] = (min(sm.D[i][j], kPackH) << kIdxBits) | (unsigned)(i + 1);  // B, idx k + 1
+  }
+
+  for (int pi = 0; pi < npanel; pi++) {
+    const int buf = pi & 1;
+    const int b = panel_block(pi);
+    if (pi + 1 < npanel) {
+      if (role == 0) pivot_load_block<PRED>(sm, buf ^ 1, job, r, panel_block(pi + 1));
+      else pivot_load_block<PRED>(sm, buf ^ 1, job, panel_block(pi + 1), r);
+    }
+    cp_async_commit();
+    cp_async_wait_1();
+    __syncthreads();  // this block landed for every thread; Kp built
+    for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
+      const int i = idx >> 6, j = idx & 63;
+      const unsigned v = min(sm.Xv[buf][i][j], kPackH) << kIdxBits;
+      if (role == 0) sm.Kx[i][j] = v | (unsigned)(i + 1);  // B = the panel block, row k = i
+      else sm.Kx[j][i] = v;                                // A^T of the panel block
+    }
+    __syncthreads();
+    const unsigned *Aop = role == 0 ? &sm.Kp[0][0] : &sm.Kx[0][0];
+    const unsigned *Bop = role == 0 ? &sm.Kx[0][0] : &sm.Kp[0][0];
+    unsigned acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc[i][c] = kPackH << kIdxBits;
+#pragma unroll 4
+    for (int kk = 0; kk < kBlk; kk++) {
+      const uint4 av = *reinterpret_cast<const uint4 *>(Aop + kk * kBlk + ty * 4);
+      const uint4 bv = *reinterpret_cast<const uint4 *>(Bop + kk * kBlk + tx * 4);
+      const unsigned a[4] = {av.x, av.y, av.z, av.w};
+      const unsigned bb[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[i][c] = __viaddmin_u32(a[i], bb[c], acc[i][c]);
+    }
+    unsigned *Dg = static_cast<unsigned *>(job.D);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int li = ty * 4 + i;
+      const int gi = (role == 0 ? r : b) * kBlk + li;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int lj = tx * 4 + c;
+        const int gj = (role == 0 ? b : r) * kBlk + lj;
+        const unsigned key = min(min(sm.Xv[buf][li][lj], kPackH) << kIdxBits, acc[i][c]);
+        const unsigned idx = key & kIdxMask;
+        if (idx == 0 || gi >= job.size || gj >= job.size) continue;
+        Dg[(int64_t)gi * job.ld + gj] = key >> kIdxBits;
+        if (PRED) job.P[(int64_t)gi * job.ld + gj] = role == 0 ? sm.Xp[buf][idx - 1][lj] : sm.P[idx - 1][lj];
+      }
+    }
+    __syncthreads();  // Kx and this buffer are free again
+  }
+  cp_async_wait_0();
+}
+
 template <typename T, bool PRED>
 cudaError_t launch_mp_t(const MpSegment *d_segs, int nseg, int tiles, int tile0, cudaStream_t st) {
   if (tiles <= 0 || nseg <= 0) return cudaSuccess;
@@ -1161,6 +1334,13 @@ cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cu
 unsigned pack_limit() { return kPackH; }
 int max_packed_k() { return kMaxPackedK; }
 
+cudaError_t launch_fw_pivot(bool pred, const FwDiagJob *d_jobs, int njobs, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  if (pred) fw_pivot_kernel<true><<<2 * njobs, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
+  else fw_pivot_kernel<false><<<2 * njobs, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njobs,
                            cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
@@ -1188,6 +1368,12 @@ cudaError_t init_minplus_kernels() {
     return e;
   if ((e = cudaFuncSetAttribute(mp_strip_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smax)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(fw_pivot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(PivotSmem))) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(fw_pivot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(PivotSmem))) != cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(mp_fwstrip_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(FwStripSmem))) != cudaSuccess)
