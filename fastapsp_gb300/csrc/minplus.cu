@@ -489,9 +489,9 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
       unsigned *crow = static_cast<unsigned *>(s.C) + (int64_t)row * s.ldc;
       int32_t *prow = PRED ? s.Cp + (int64_t)row * s.ldcp : nullptr;
-      if (vec && col0 + 3 < s.N) {
-        *reinterpret_cast<uint4 *>(crow + col0) = make_uint4(d[0], d[1], d[2], d[3]);
-        if (PRED) *reinterpret_cast<int4 *>(prow + col0) = make_int4(p[0], p[1], p[2], p[3]);
+      if (vec && col0 + 3 < s.N) {  // streaming stores: the rows are not read again here
+        __stcs(reinterpret_cast<uint4 *>(crow + col0), make_uint4(d[0], d[1], d[2], d[3]));
+        if (PRED) __stcs(reinterpret_cast<int4 *>(prow + col0), make_int4(p[0], p[1], p[2], p[3]));
       } else {
 #pragma unroll
         for (int q = 0; q < 4; q++)
@@ -769,9 +769,9 @@ __global__ void __launch_bounds__(kThreads, 2)
             }
           }
         }
-        if (vec_c && col0 + 3 < s.N) {
-          *reinterpret_cast<uint4 *>(crow + col0) = make_uint4(d[0], d[1], d[2], d[3]);
-          if (PRED) *reinterpret_cast<int4 *>(prow + col0) = make_int4(p[0], p[1], p[2], p[3]);
+        if (vec_c && col0 + 3 < s.N) {  // streaming stores: the rows are not read again here
+          __stcs(reinterpret_cast<uint4 *>(crow + col0), make_uint4(d[0], d[1], d[2], d[3]));
+          if (PRED) __stcs(reinterpret_cast<int4 *>(prow + col0), make_int4(p[0], p[1], p[2], p[3]));
         } else {
 #pragma unroll
           for (int q = 0; q < 4; q++)
