@@ -37,8 +37,8 @@ int max_packed_k();
 cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njobs,
                            cudaStream_t st);
 // Packed int32 form: closes each job's pivot block and updates its row and
-// column panels (a cluster of two CTAs per job); replaces launch_fw_diag and
-// the panel launch.
+// column panels (a cluster of CTAs per job); replaces launch_fw_diag and the
+// panel launch.
 cudaError_t launch_fw_pivot(bool pred, const FwDiagJob *d_jobs, int njobs, cudaStream_t st);
 int minplus_tile_rows();  // CTA output tile edge (128)
 int fw_block();           // FW pivot block edge (64)

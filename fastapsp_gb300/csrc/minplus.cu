@@ -1030,10 +1030,90 @@ __global__ void max_finite_kernel(const MatRef *__restrict__ mats, unsigned *out
 }
 
 
-// Closes the 64x64 pivot block of one matrix per CTA: sequential k inside the
-// block, 16 elements per thread, one barrier per k.  Row k and column k do not
-// change at step k (zero diagonal), so only strictly improved entries are
-// written and no second barrier is needed.
+// Closes a 64x64 block held in shared memory (D values, P predecessors, row
+// pitch 65): sequential k as the reference's floyd_CPU_path
+// (fap/kernel/floyd.h:37-48), strict improvements only, P[i][j] = P[k][j].
+// Each thread keeps its 4x4 entries in registers; row k and column k do not
+// change at step k (zero diagonal), so their owners publish them for the
+// next step into a double-buffered row/column copy and one barrier per step
+// suffices.  Ends with the closed block back in D/P and a barrier.
+template <typename T, bool PRED>
+__device__ __forceinline__ void close_block(T (*D)[kBlk + 1], int32_t (*P)[kBlk + 1]) {
+  __shared__ T rowk[2][kBlk], colk[2][kBlk];
+  __shared__ int32_t prowk[2][kBlk];
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  T d[4][4];
+  int32_t p[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      d[i][c] = D[ty * 4 + i][tx * 4 + c];
+      p[i][c] = PRED ? P[ty * 4 + i][tx * 4 + c] : -1;
+    }
+  // publish row 0 / column 0
+  if (ty == 0)
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      rowk[0][tx * 4 + c] = d[0][c];
+      if (PRED) prowk[0][tx * 4 + c] = p[0][c];
+    }
+  if (tx == 0)
+#pragma unroll
+    for (int i = 0; i < 4; i++) colk[0][ty * 4 + i] = d[i][0];
+  __syncthreads();
+  for (int k = 0; k < kBlk; k++) {
+    const int buf = k & 1;
+    T a[4], b[4];
+    int32_t bp[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      a[q] = colk[buf][ty * 4 + q];
+      b[q] = rowk[buf][tx * 4 + q];
+      if (PRED) bp[q] = prowk[buf][tx * 4 + q];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const T v = Dist<T>::add(a[i], b[c]);
+        if (v < d[i][c]) {
+          d[i][c] = v;
+          if (PRED) p[i][c] = bp[c];
+        }
+      }
+    const int kn = k + 1;
+    if (kn < kBlk) {
+      const int kq = kn & 3;
+      if (ty == (kn >> 2))
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          if (i == kq)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              rowk[buf ^ 1][tx * 4 + c] = d[i][c];
+              if (PRED) prowk[buf ^ 1][tx * 4 + c] = p[i][c];
+            }
+      if (tx == (kn >> 2))
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+          if (c == kq)
+#pragma unroll
+            for (int i = 0; i < 4; i++) colk[buf ^ 1][ty * 4 + i] = d[i][c];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      D[ty * 4 + i][tx * 4 + c] = d[i][c];
+      if (PRED) P[ty * 4 + i][tx * 4 + c] = p[i][c];
+    }
+  __syncthreads();
+}
+
+// Closes the 64x64 pivot block of one matrix per CTA (close_block).
 template <typename T, bool PRED>
 __global__ void __launch_bounds__(256)
     fw_diag_kernel(const FwDiagJob *__restrict__ jobs) {
@@ -1051,28 +1131,7 @@ __global__ void __launch_bounds__(256)
     if (PRED) P[i][j] = ok ? job.P[(int64_t)gi * job.ld + gj] : -1;
   }
   __syncthreads();
-  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-  for (int k = 0; k < kBlk; k++) {
-    T a[4], b[4];
-    int32_t bp[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      a[q] = D[ty * 4 + q][k];
-      b[q] = D[k][tx * 4 + q];
-      if (PRED) bp[q] = P[k][tx * 4 + q];
-    }
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const T v = Dist<T>::add(a[r], b[c]);
-        if (v < D[ty * 4 + r][tx * 4 + c]) {
-          D[ty * 4 + r][tx * 4 + c] = v;
-          if (PRED) P[ty * 4 + r][tx * 4 + c] = bp[c];
-        }
-      }
-    __syncthreads();
-  }
+  close_block<T, PRED>(D, P);
   for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += blockDim.x) {
     const int i = idx >> 6, j = idx & 63;
     const int gi = base + i, gj = base + j;
@@ -1084,65 +1143,64 @@ __global__ void __launch_bounds__(256)
 }
 
 // Pivot step of one FW round in the packed int32 form, for every matrix of
-// the batch: a cluster of two CTAs per matrix.  CTA 0 closes the pivot block
-// (as fw_diag_kernel) and writes it back; after a cluster barrier CTA 1 copies
-// the closed block out of CTA 0's shared memory (no second closure, and no
-// read of the block while it is being written).  Then CTA 0 updates the row
-// panel D_rb = min(D_rb, D_rr (x) D_rb) and CTA 1 the column panel
-// D_br = min(D_br, D_br (x) D_rr), block by block, with the next block's copy
-// in flight (cp.async) while the current one is multiplied: 64x64 outputs,
-// 4x4 per thread, packed keys, the block's own values joining with index 0.
-// One launch replaces the diagonal launch and the panel launch of the tile
-// kernel (whose 128x128 tiles were half empty for 64-wide panels).
+// the batch: a cluster of kPivotCtas CTAs per matrix (two CTAs per SM).  CTA
+// 0 closes the pivot block (as fw_diag_kernel) and writes it back; after a
+// cluster barrier the others copy the closed block out of CTA 0's shared
+// memory (no second closure, and no read of the block while it is being
+// written).  Then CTAs of the first half update the row panel
+// D_rb = min(D_rb, D_rr (x) D_rb) and those of the second half the column
+// panel D_br = min(D_br, D_br (x) D_rr), each taking every (kPivotCtas/2)-th
+// block: 64x64 outputs, 4x4 per thread, packed keys, the block's own values
+// joining with index 0.  One launch replaces the diagonal launch and the
+// panel launch of the tile kernel (whose 128x128 tiles were half empty for
+// 64-wide panels).
+constexpr int kPivotCtas = 4;
+
 struct PivotSmem {
   unsigned D[kBlk][kBlk + 1];  // pivot block values (closure)
   int32_t P[kBlk][kBlk + 1];   // and predecessors
   unsigned Kp[kBlk][kBlk];     // pivot keys: A^T (row panel) or B (column panel)
-  unsigned Xv[2][kBlk][kBlk];  // panel block values, double-buffered
-  int32_t Xp[2][kBlk][kBlk];   // and predecessors
-  unsigned Kx[kBlk][kBlk];     // keys of the current panel block: B (row panel) or A^T (column)
+  unsigned Xv[kBlk][kBlk];     // the current panel block's values
+  int32_t Xp[kBlk][kBlk];      // and predecessors
+  unsigned Kx[kBlk][kBlk];     // its keys: B (row panel) or A^T (column panel)
 };
 
 template <bool PRED>
-__device__ __forceinline__ void pivot_load_block(PivotSmem &sm, int buf, const FwDiagJob &job,
-                                                 int rb, int cb) {
+__device__ __forceinline__ void pivot_load_block(PivotSmem &sm, const FwDiagJob &job, int rb,
+                                                 int cb) {
   const unsigned *Dg = static_cast<const unsigned *>(job.D);
   for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
     const int i = idx >> 6, j = idx & 63;
     const int gi = rb * kBlk + i, gj = cb * kBlk + j;
     if (gi < job.size && gj < job.size) {
-      cp_async4(&sm.Xv[buf][i][j], Dg + (int64_t)gi * job.ld + gj);
-      if (PRED) cp_async4(&sm.Xp[buf][i][j], job.P + (int64_t)gi * job.ld + gj);
+      cp_async4(&sm.Xv[i][j], Dg + (int64_t)gi * job.ld + gj);
+      if (PRED) cp_async4(&sm.Xp[i][j], job.P + (int64_t)gi * job.ld + gj);
     } else {
-      sm.Xv[buf][i][j] = Dist<uint32_t>::inf();
-      if (PRED) sm.Xp[buf][i][j] = -1;
+      sm.Xv[i][j] = Dist<uint32_t>::inf();
+      if (PRED) sm.Xp[i][j] = -1;
     }
   }
 }
 
 template <bool PRED>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+__global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2)
     fw_pivot_kernel(const FwDiagJob *__restrict__ jobs) {
   namespace cg = cooperative_groups;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   PivotSmem &sm = *reinterpret_cast<PivotSmem *>(smem_raw);
   cg::cluster_group cluster = cg::this_cluster();
-  const int role = (int)cluster.block_rank();  // 0: pivot block + row panel, 1: column panel
-  const FwDiagJob job = jobs[blockIdx.x >> 1];
+  const int rank = (int)cluster.block_rank();
+  const int role = rank / (kPivotCtas / 2);  // 0: row panel, 1: column panel
+  const int sub = rank % (kPivotCtas / 2);   // which of the panel's blocks
+  const FwDiagJob job = jobs[blockIdx.x / kPivotCtas];
   const int r = job.block;
   const int nb = (job.size + kBlk - 1) / kBlk;
   const int npanel = nb - 1;
   const unsigned INF = Dist<uint32_t>::inf();
   auto panel_block = [&](int i) { return i < r ? i : i + 1; };  // i-th block other than r
 
-  if (npanel > 0) {
-    if (role == 0) pivot_load_block<PRED>(sm, 0, job, r, panel_block(0));
-    else pivot_load_block<PRED>(sm, 0, job, panel_block(0), r);
-  }
-  cp_async_commit();
-
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-  if (role == 0) {
+  if (rank == 0) {
     unsigned *Dg = static_cast<unsigned *>(job.D);
     const int base = r * kBlk;
     for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
@@ -1153,27 +1211,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
       if (PRED) sm.P[i][j] = ok ? job.P[(int64_t)gi * job.ld + gj] : -1;
     }
     __syncthreads();
-    for (int k = 0; k < kBlk; k++) {
-      unsigned a[4], b[4];
-      int32_t bp[4];
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        a[q] = sm.D[ty * 4 + q][k];
-        b[q] = sm.D[k][tx * 4 + q];
-        if (PRED) bp[q] = sm.P[k][tx * 4 + q];
-      }
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const unsigned v = Dist<uint32_t>::add(a[i], b[c]);
-          if (v < sm.D[ty * 4 + i][tx * 4 + c]) {
-            sm.D[ty * 4 + i][tx * 4 + c] = v;
-            if (PRED) sm.P[ty * 4 + i][tx * 4 + c] = bp[c];
-          }
-        }
-      __syncthreads();
-    }
+    close_block<uint32_t, PRED>(sm.D, sm.P);
     for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
       const int i = idx >> 6, j = idx & 63;
       const int gi = base + i, gj = base + j;
@@ -1184,7 +1222,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
     }
   }
   cluster.sync();  // the closed pivot block is in CTA 0's shared memory
-  if (role == 1) {
+  if (rank != 0) {
     const unsigned *rD = cluster.map_shared_rank(&sm.D[0][0], 0);
     const int32_t *rP = cluster.map_shared_rank(&sm.P[0][0], 0);
     for (int idx = threadIdx.x; idx < kBlk * (kBlk + 1); idx += kThreads) {
@@ -1192,26 +1230,23 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
       if (PRED) (&sm.P[0][0])[idx] = rP[idx];
     }
   }
-  cluster.sync();  // CTA 0's shared memory is no longer read; CTA 1's copy is complete
+  cluster.sync();  // CTA 0's shared memory is no longer read; every copy is complete
   for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
     const int i = idx >> 6, j = idx & 63;
     if (role == 0) sm.Kp[j][i] = min(sm.D[i][j], kPackH) << kIdxBits;  // A^T, idx 0
     else sm.Kp[i][j] = (min(sm.D[i][j], kPackH) << kIdxBits) | (unsigned)(i + 1);  // B, idx k + 1
   }
 
-  for (int pi = 0; pi < npanel; pi++) {
-    const int buf = pi & 1;
+  for (int pi = sub; pi < npanel; pi += kPivotCtas / 2) {
     const int b = panel_block(pi);
-    if (pi + 1 < npanel) {
-      if (role == 0) pivot_load_block<PRED>(sm, buf ^ 1, job, r, panel_block(pi + 1));
-      else pivot_load_block<PRED>(sm, buf ^ 1, job, panel_block(pi + 1), r);
-    }
+    if (role == 0) pivot_load_block<PRED>(sm, job, r, b);
+    else pivot_load_block<PRED>(sm, job, b, r);
     cp_async_commit();
-    cp_async_wait_1();
-    __syncthreads();  // this block landed for every thread; Kp built
+    cp_async_wait_0();
+    __syncthreads();  // this block landed for every thread (and Kp is built)
     for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
       const int i = idx >> 6, j = idx & 63;
-      const unsigned v = min(sm.Xv[buf][i][j], kPackH) << kIdxBits;
+      const unsigned v = min(sm.Xv[i][j], kPackH) << kIdxBits;
       if (role == 0) sm.Kx[i][j] = v | (unsigned)(i + 1);  // B = the panel block, row k = i
       else sm.Kx[j][i] = v;                                // A^T of the panel block
     }
@@ -1243,16 +1278,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
       for (int c = 0; c < 4; c++) {
         const int lj = tx * 4 + c;
         const int gj = (role == 0 ? b : r) * kBlk + lj;
-        const unsigned key = min(min(sm.Xv[buf][li][lj], kPackH) << kIdxBits, acc[i][c]);
+        const unsigned key = min(min(sm.Xv[li][lj], kPackH) << kIdxBits, acc[i][c]);
         const unsigned idx = key & kIdxMask;
         if (idx == 0 || gi >= job.size || gj >= job.size) continue;
         Dg[(int64_t)gi * job.ld + gj] = key >> kIdxBits;
-        if (PRED) job.P[(int64_t)gi * job.ld + gj] = role == 0 ? sm.Xp[buf][idx - 1][lj] : sm.P[idx - 1][lj];
+        if (PRED) job.P[(int64_t)gi * job.ld + gj] = role == 0 ? sm.Xp[idx - 1][lj] : sm.P[idx - 1][lj];
       }
     }
-    __syncthreads();  // Kx and this buffer are free again
+    __syncthreads();  // Kx and the block buffer are free again
   }
-  cp_async_wait_0();
 }
 
 template <typename T, bool PRED>
@@ -1336,8 +1370,9 @@ int max_packed_k() { return kMaxPackedK; }
 
 cudaError_t launch_fw_pivot(bool pred, const FwDiagJob *d_jobs, int njobs, cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
-  if (pred) fw_pivot_kernel<true><<<2 * njobs, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
-  else fw_pivot_kernel<false><<<2 * njobs, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
+  const unsigned grid = (unsigned)(kPivotCtas * njobs);
+  if (pred) fw_pivot_kernel<true><<<grid, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
+  else fw_pivot_kernel<false><<<grid, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
   return cudaGetLastError();
 }
 
