@@ -29,7 +29,8 @@ int minplus_strip_tiles();
 cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
                              cudaStream_t st);
 int fw_strip_tiles();
-int minplus_strip_max_k();
+int minplus_strip_max_k();   // largest K of the strip form
+int minplus_strip_pair_k();  // largest K at which it runs two CTAs per SM
 // Largest finite int32 entry of the matrices, atomicMax-ed into *out.
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st);
 unsigned pack_limit();

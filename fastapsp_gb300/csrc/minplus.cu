@@ -507,7 +507,8 @@ __global__ void __launch_bounds__(kThreads, 2)
 // Strip form of the packed min-plus for products that do not accumulate into
 // C (the inner rows of every part) with K <= kStripMaxK.  One CTA owns a
 // strip: one 128-row tile of a segment and up to kStripTiles consecutive
-// 128-column tiles, two CTAs per SM.  A's 128 x K block is staged once per
+// 128-column tiles, two CTAs per SM (one when K > kStripPairK, whose shared
+// memory is larger).  A's 128 x K block is staged once per
 // strip (transposed, so that a thread's 8 row operands of one k are two
 // 16-byte loads); B's K x 128 tiles are double-buffered, so the next tile's
 // copy is in flight while the current one is multiplied; B's predecessor
@@ -524,7 +525,8 @@ __global__ void __launch_bounds__(kThreads, 2)
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
 constexpr int kStripTiles = 16;
-constexpr int kStripMaxK = 48;
+constexpr int kStripPairK = 48;   // largest K with two CTAs per SM
+constexpr int kStripMaxK = 100;   // largest K of the strip form (one CTA per SM above kStripPairK)
 constexpr int kOwnCap = 12;
 
 __host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
@@ -1358,6 +1360,7 @@ cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int s
 }
 int fw_strip_tiles() { return kFwStripTiles; }
 int minplus_strip_max_k() { return kStripMaxK; }
+int minplus_strip_pair_k() { return kStripPairK; }
 
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st) {
   if (nmats <= 0) return cudaSuccess;
