@@ -57,6 +57,7 @@ SIGNATURES = {
     "fap_solve_part": (C.c_int, [_p, _i32, _p, _p, _p]),
     "fap_solve": (C.c_int, [_p, _p, _p, _i32, _p]),
     "fap_last_times": (C.c_int, [_p, C.POINTER(C.c_double)]),
+    "fap_last_launches": (C.c_int, [_p, C.POINTER(C.c_int64)]),
     "fap_minplus": (C.c_int, [_p, _i32, _i32, _i32, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i64,
                               _p, _i64, _p]),
     "fap_floyd_batched": (C.c_int, [_p, _i32, _i32, _p, _p, _p, _p, _p]),

@@ -138,6 +138,7 @@ struct Plan {
   int max_mp_k = 0;     // largest min-plus K (boundary count) of the plan
   int pack = -1;        // packed int32 form: -1 undecided, 0 no, 1 yes
   int sssp_lanes = 32;  // sources per SSSP batch
+  int launches = 0;     // kernels one run of the plan launches
   // graph (batched mode)
   cudaGraphExec_t exec = nullptr;
   ~Plan() {
@@ -197,6 +198,7 @@ struct fap_engine {
   DevBuf small;                // tables of standalone calls
   std::vector<std::unique_ptr<Plan>> plans;
   double times[5] = {0, 0, 0, 0, 0};
+  int64_t last_launches = 0;  // kernels the last solve launched
   std::mutex mu;
 
   bool f32() const { return dtype == FAP_DTYPE_F32; }
@@ -652,12 +654,14 @@ struct Issuer {
   // Plain plans interleave per part (SSSP, rest); batched plans have one group.
   int all() {
     int rc;
+    const int c0 = fapk::launch_count();
     FAP_CUDA(rec(0));
     for (size_t g = 0; g < pl.groups.size(); g++) {
       if ((rc = sssp(g)) != FAP_OK) return rc;
       if (g + 1 == pl.groups.size()) FAP_CUDA(rec(1));
       if ((rc = rest(g, g + 1 == pl.groups.size())) != FAP_OK) return rc;
     }
+    pl.launches = fapk::launch_count() - c0;
     return FAP_OK;
   }
 };
@@ -851,6 +855,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     Issuer is{e, *pl, st, false};
     if ((rc = is.all()) != FAP_OK) return rc;
   }
+  e->last_launches = pl->launches;
   return FAP_OK;
 }
 
@@ -1264,6 +1269,12 @@ int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode, void *stre
 int fap_last_times(const fap_engine *e, double *times5) {
   if (!e || !times5) return set_error(FAP_ERR_INVALID, "null argument");
   for (int i = 0; i < 5; i++) times5[i] = e->times[i];
+  return FAP_OK;
+}
+
+int fap_last_launches(const fap_engine *e, int64_t *count) {
+  if (!e || !count) return set_error(FAP_ERR_INVALID, "null argument");
+  *count = e->last_launches;
   return FAP_OK;
 }
 

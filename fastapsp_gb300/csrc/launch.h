@@ -8,6 +8,10 @@
 
 namespace fapk {
 
+// Kernel launches issued by this host thread (each launcher below adds the
+// kernels it actually launches); plans record how many one solve issues.
+int &launch_count();
+
 // minplus.cu
 // packed = true selects the packed int32 form (uint32 distances only); the
 // caller must have checked that every finite result stays below
@@ -68,6 +72,7 @@ struct SsspArgs {
   double delta;               // near-far threshold step (> 0; huge = plain Bellman-Ford)
   unsigned long long *stats;  // may be null: [near steps, far splits, frontier
                               // vertices relaxed, far entries scanned, batches]
+  int32_t defer_output;       // set by launch_sssp: output pass in its own launch
 };
 // delta value that puts every vertex in the near frontier (plain frontier BF)
 constexpr double kSsspNoDelta = 2147483647.0;

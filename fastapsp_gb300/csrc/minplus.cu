@@ -1294,6 +1294,7 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
 template <typename T, bool PRED>
 cudaError_t launch_mp_t(const MpSegment *d_segs, int nseg, int tiles, int tile0, cudaStream_t st) {
   if (tiles <= 0 || nseg <= 0) return cudaSuccess;
+  ++launch_count();
   mp_tile_kernel<T, PRED><<<tiles, kThreads, sizeof(MpSmem<T>), st>>>(d_segs, nseg, tile0);
   return cudaGetLastError();
 }
@@ -1301,6 +1302,7 @@ cudaError_t launch_mp_t(const MpSegment *d_segs, int nseg, int tiles, int tile0,
 template <bool PRED>
 cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int tiles, int tile0, cudaStream_t st) {
   if (tiles <= 0 || nseg <= 0) return cudaSuccess;
+  ++launch_count();
   mp_tile_packed_kernel<PRED><<<tiles, kThreads, sizeof(KeySmem), st>>>(d_segs, nseg, tile0);
   return cudaGetLastError();
 }
@@ -1308,6 +1310,7 @@ cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int tiles, int ti
 template <bool PRED>
 cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks, cudaStream_t st) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
+  ++launch_count();
   mp_strip_kernel<PRED><<<strips, kThreads, strip_smem_bytes(ks), st>>>(d_segs, nseg, ks);
   return cudaGetLastError();
 }
@@ -1315,6 +1318,7 @@ cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks
 template <bool PRED>
 cudaError_t launch_fwstrip_t(const MpSegment *d_segs, int nseg, int strips, cudaStream_t st) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
+  ++launch_count();
   mp_fwstrip_kernel<PRED><<<strips, kThreads, sizeof(FwStripSmem), st>>>(d_segs, nseg);
   return cudaGetLastError();
 }
@@ -1364,6 +1368,7 @@ int minplus_strip_pair_k() { return kStripPairK; }
 
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st) {
   if (nmats <= 0) return cudaSuccess;
+  ++launch_count();
   max_finite_kernel<<<dim3(32, nmats), 256, 0, st>>>(d_mats, out);
   return cudaGetLastError();
 }
@@ -1374,8 +1379,8 @@ int max_packed_k() { return kMaxPackedK; }
 cudaError_t launch_fw_pivot(bool pred, const FwDiagJob *d_jobs, int njobs, cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
   const unsigned grid = (unsigned)(kPivotCtas * njobs);
-  if (pred) fw_pivot_kernel<true><<<grid, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
-  else fw_pivot_kernel<false><<<grid, kThreads, sizeof(PivotSmem), st>>>(d_jobs);
+  if (pred) { ++launch_count(); fw_pivot_kernel<true><<<grid, kThreads, sizeof(PivotSmem), st>>>(d_jobs); }
+  else { ++launch_count(); fw_pivot_kernel<false><<<grid, kThreads, sizeof(PivotSmem), st>>>(d_jobs); }
   return cudaGetLastError();
 }
 
@@ -1383,11 +1388,11 @@ cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njo
                            cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
   if (f32) {
-    if (pred) fw_diag_kernel<float, true><<<njobs, 256, 0, st>>>(d_jobs);
-    else fw_diag_kernel<float, false><<<njobs, 256, 0, st>>>(d_jobs);
+    if (pred) { ++launch_count(); fw_diag_kernel<float, true><<<njobs, 256, 0, st>>>(d_jobs); }
+    else { ++launch_count(); fw_diag_kernel<float, false><<<njobs, 256, 0, st>>>(d_jobs); }
   } else {
-    if (pred) fw_diag_kernel<uint32_t, true><<<njobs, 256, 0, st>>>(d_jobs);
-    else fw_diag_kernel<uint32_t, false><<<njobs, 256, 0, st>>>(d_jobs);
+    if (pred) { ++launch_count(); fw_diag_kernel<uint32_t, true><<<njobs, 256, 0, st>>>(d_jobs); }
+    else { ++launch_count(); fw_diag_kernel<uint32_t, false><<<njobs, 256, 0, st>>>(d_jobs); }
   }
   return cudaGetLastError();
 }

@@ -50,6 +50,7 @@ namespace {
 
 constexpr int kSsspThreads = 512;
 constexpr int kSsspWarps = kSsspThreads / 32;
+constexpr int kOutThreads = 256;  // the separate output kernel
 
 // dvm (n x 32 four-byte or n x 16 eight-byte entries) + near/far frontiers
 // (2 + 2), n ints each.
@@ -94,6 +95,115 @@ struct Acc<float, true> {  // FP32 weights, FP64 search
   static __device__ __forceinline__ V from_double(double x) { return x; }
 };
 
+// Predecessors and transposed output of one 32-vertex block of batch b (the
+// calling warp's; the warp synchronizes only with itself).  A lane group
+// takes two vertices at a time and scans their in-edge lists side by side
+// (edge j of both per iteration), so their loads overlap; the block then
+// goes through the warp's shared-memory tile so that every source row is
+// written with coalesced stores.
+template <typename T, bool PRED, int LANES, bool ACC64>
+__device__ __forceinline__ void sssp_out_block(const SsspArgs &a,
+                                               const typename Acc<T, ACC64>::K *dvm, int b,
+                                               int cnt, int my_src, int v0, OutTile<LANES> &tile,
+                                               unsigned &local_max) {
+  using A = Acc<T, ACC64>;
+  using V = typename A::V;
+  using K = typename A::K;
+  constexpr int VPW = 32 / LANES;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / LANES, sl = lane % LANES;
+  const int32_t n = a.n;
+  const unsigned *iwb = static_cast<const unsigned *>(a.iw);
+  const K INF = A::inf();
+  for (int vb = 0; vb < 32; vb += 2 * VPW) {
+    int vv[2], e0[2], deg[2], bu[2];
+    K dk[2], bdu[2];
+    V dvv[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      vv[i] = v0 + vb + i * VPW + sub;
+      const bool in = vv[i] < n;
+      dk[i] = (in && sl < cnt) ? __ldcg(&dvm[(size_t)vv[i] * LANES + sl]) : INF;
+      dvv[i] = A::val(dk[i]);
+      e0[i] = (PRED && in) ? a.iro[vv[i]] : 0;
+      deg[i] = (PRED && in) ? a.iro[vv[i] + 1] - e0[i] : 0;
+      bdu[i] = ~(K)0;
+      bu[i] = -1;
+    }
+    if (PRED) {
+      int dmax = max(deg[0], deg[1]);
+      if (VPW == 2) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, 16));
+      for (int j = 0; j < dmax; j++) {
+        int u[2];
+        unsigned wq[2];
+        K duk[2];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+          const bool has = j < deg[i];
+          u[i] = has ? a.icol[e0[i] + j] : 0;
+          wq[i] = has ? iwb[e0[i] + j] : 0u;
+          duk[i] = (has && dk[i] < INF) ? __ldcg(&dvm[(size_t)u[i] * LANES + sl]) : INF;
+        }
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+          const bool better = duk[i] < INF && A::val(duk[i]) + A::weight(wq[i]) == dvv[i] &&
+                              (duk[i] < bdu[i] || (duk[i] == bdu[i] && u[i] < bu[i]));
+          bdu[i] = better ? duk[i] : bdu[i];
+          bu[i] = better ? u[i] : bu[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      unsigned dv_out = Dist<T>::bits(Dist<T>::inf());
+      int32_t p = -1;
+      if (dk[i] < INF) {
+        dv_out = A::out(dk[i]);
+        if (!std::is_same<T, float>::value) local_max = max(local_max, dv_out);
+        if (PRED) p = vv[i] == my_src ? vv[i] : bu[i];
+      }
+      tile.d[vb + i * VPW + sub][sl] = dv_out;
+      tile.p[vb + i * VPW + sub][sl] = p;
+    }
+  }
+  __syncwarp();
+  const int col = v0 + lane;
+  if (col < n) {
+    for (int s = 0; s < cnt; s++) {
+      const int64_t off = a.batches[b].row_off[s] + col;
+      static_cast<unsigned *>(a.dist)[off] = tile.d[lane][s];
+      if (PRED) a.pred[off] = tile.p[lane][s];
+    }
+  }
+  __syncwarp();
+}
+
+// Output pass of every batch at once, after a search launch that deferred it
+// (one batch per search CTA, so batch b's distance table is slot b): block
+// (x, b) has its warps take 32-vertex blocks x * warps + w of batch b.
+template <typename T, bool PRED, int LANES, bool ACC64>
+__global__ void __launch_bounds__(kOutThreads)
+    sssp_output_kernel(SsspArgs a) {
+  using A = Acc<T, ACC64>;
+  using K = typename A::K;
+  extern __shared__ __align__(16) unsigned char out_smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  OutTile<LANES> &tile = reinterpret_cast<OutTile<LANES> *>(out_smem_raw)[warp];
+  const int b = blockIdx.y;
+  const K *dvm = reinterpret_cast<const K *>(static_cast<const unsigned char *>(a.scratch) +
+                                             (size_t)b * slot_bytes(a.n));
+  const int cnt = a.batches[b].count;
+  const int sl = lane % LANES;
+  const int my_src = sl < cnt ? a.batches[b].src[sl] : -1;
+  unsigned local_max = 0;
+  const int v0 = (blockIdx.x * (kOutThreads / 32) + warp) * 32;
+  if (v0 < a.n) sssp_out_block<T, PRED, LANES, ACC64>(a, dvm, b, cnt, my_src, v0, tile, local_max);
+  if (a.maxd != nullptr) {
+    local_max = __reduce_max_sync(0xffffffffu, local_max);
+    if (lane == 0 && local_max) atomicMax(a.maxd, local_max);
+  }
+}
+
 // Frontier membership bitmaps: near[2] (entry of the next near frontier,
 // alternating per step) and far (entry of the far list), ceil(n / 32) words
 // each.  They live in the dynamic shared memory (overlaid on the output
@@ -129,7 +239,6 @@ __global__ void __launch_bounds__(kSsspThreads)
   int32_t *const nearq0 = reinterpret_cast<int32_t *>(base + (size_t)n * 32 * 4);
   int32_t *const farq0 = nearq0 + 2 * (size_t)n;
   const unsigned *wb = static_cast<const unsigned *>(a.w);
-  const unsigned *iwb = static_cast<const unsigned *>(a.iw);
   const K INF = A::inf();
   const V delta = A::from_double(a.delta);
 
@@ -338,69 +447,9 @@ __global__ void __launch_bounds__(kSsspThreads)
     // 32-vertex blocks and synchronize only within the warp.  A lane group
     // takes two vertices at a time and scans their in-edge lists side by
     // side (edge j of both per iteration), so their loads overlap. ----
-    for (int v0 = warp * 32; v0 < n; v0 += kSsspWarps * 32) {
-      for (int vb = 0; vb < 32; vb += 2 * VPW) {
-        int vv[2], e0[2], deg[2], bu[2];
-        K dk[2], bdu[2];
-        V dvv[2];
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-          vv[i] = v0 + vb + i * VPW + sub;
-          const bool in = vv[i] < n;
-          dk[i] = (in && sl < cnt) ? __ldcg(&dvm[(size_t)vv[i] * LANES + sl]) : INF;
-          dvv[i] = A::val(dk[i]);
-          e0[i] = (PRED && in) ? a.iro[vv[i]] : 0;
-          deg[i] = (PRED && in) ? a.iro[vv[i] + 1] - e0[i] : 0;
-          bdu[i] = ~(K)0;
-          bu[i] = -1;
-        }
-        if (PRED) {
-          int dmax = max(deg[0], deg[1]);
-          if (VPW == 2) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, 16));
-          for (int j = 0; j < dmax; j++) {
-            int u[2];
-            unsigned wq[2];
-            K duk[2];
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-              const bool has = j < deg[i];
-              u[i] = has ? a.icol[e0[i] + j] : 0;
-              wq[i] = has ? iwb[e0[i] + j] : 0u;
-              duk[i] = (has && dk[i] < INF) ? __ldcg(&dvm[(size_t)u[i] * LANES + sl]) : INF;
-            }
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-              const bool better = duk[i] < INF && A::val(duk[i]) + A::weight(wq[i]) == dvv[i] &&
-                                  (duk[i] < bdu[i] || (duk[i] == bdu[i] && u[i] < bu[i]));
-              bdu[i] = better ? duk[i] : bdu[i];
-              bu[i] = better ? u[i] : bu[i];
-            }
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-          unsigned dv_out = Dist<T>::bits(Dist<T>::inf());
-          int32_t p = -1;
-          if (dk[i] < INF) {
-            dv_out = A::out(dk[i]);
-            if (!std::is_same<T, float>::value) local_max = max(local_max, dv_out);
-            if (PRED) p = vv[i] == my_src ? vv[i] : bu[i];
-          }
-          tile.d[vb + i * VPW + sub][sl] = dv_out;
-          tile.p[vb + i * VPW + sub][sl] = p;
-        }
-      }
-      __syncwarp();
-      const int col = v0 + lane;
-      if (col < n) {
-        for (int s = 0; s < cnt; s++) {
-          const int64_t off = a.batches[b].row_off[s] + col;
-          static_cast<unsigned *>(a.dist)[off] = tile.d[lane][s];
-          if (PRED) a.pred[off] = tile.p[lane][s];
-        }
-      }
-      __syncwarp();
-    }
+    if (!a.defer_output)
+      for (int v0 = warp * 32; v0 < n; v0 += kSsspWarps * 32)
+        sssp_out_block<T, PRED, LANES, ACC64>(a, dvm, b, cnt, my_src, v0, tile, local_max);
     __syncthreads();  // dvm, the frontiers and the bitmaps are reset by the next batch
     st_batches++;
   }
@@ -417,11 +466,26 @@ __global__ void __launch_bounds__(kSsspThreads)
   }
 }
 
+template <int LANES>
+constexpr size_t out_kernel_smem() { return sizeof(OutTile<LANES>) * (kOutThreads / 32); }
+
+// When every batch has its own CTA (and so its own distance table), the
+// output pass -- predecessors, transposes and row writes, bound by memory
+// latency per vertex -- runs as a second launch over all batches and vertex
+// blocks at once instead of inside each batch's CTA.
 template <typename T, bool PRED, int LANES, bool ACC64>
-cudaError_t launch_one(const SsspArgs &a, cudaStream_t st) {
+cudaError_t launch_one(const SsspArgs &a0, cudaStream_t st) {
+  SsspArgs a = a0;
+  a.defer_output = a.nbatches <= a.slots ? 1 : 0;
   size_t smem = out_smem<LANES>();
   if (bitmap_bytes(a.n) <= kBitmapSmemMax) smem = std::max(smem, bitmap_bytes(a.n));
+  ++launch_count();
   sssp_kernel<T, PRED, LANES, ACC64><<<a.slots, kSsspThreads, smem, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !a.defer_output) return e;
+  const dim3 grid((unsigned)((a.n + kOutThreads - 1) / kOutThreads), (unsigned)a.nbatches);
+  ++launch_count();
+  sssp_output_kernel<T, PRED, LANES, ACC64><<<grid, kOutThreads, out_kernel_smem<LANES>(), st>>>(a);
   return cudaGetLastError();
 }
 
@@ -437,9 +501,12 @@ cudaError_t launch_t(const SsspArgs &a, cudaStream_t st) {
 
 template <typename T, bool PRED, int LANES, bool ACC64>
 cudaError_t set_attr() {
-  return cudaFuncSetAttribute(sssp_kernel<T, PRED, LANES, ACC64>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)std::max(out_smem<LANES>(), kBitmapSmemMax));
+  cudaError_t e = cudaFuncSetAttribute(sssp_kernel<T, PRED, LANES, ACC64>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)std::max(out_smem<LANES>(), kBitmapSmemMax));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(sssp_output_kernel<T, PRED, LANES, ACC64>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)out_kernel_smem<LANES>());
 }
 
 }  // namespace

@@ -112,15 +112,20 @@ __global__ void __launch_bounds__(128) decode_kernel(BuildArgs a, T *rows, int32
 
 }  // namespace
 
+int &launch_count() {
+  static thread_local int count = 0;
+  return count;
+}
+
 cudaError_t launch_build(bool f32, bool pred, const BuildArgs &a, cudaStream_t st) {
   if (a.total_rows <= 0) return cudaSuccess;
   const unsigned grid = (unsigned)a.total_rows;
   if (f32) {
-    if (pred) build_kernel<float, true><<<grid, 128, 0, st>>>(a);
-    else build_kernel<float, false><<<grid, 128, 0, st>>>(a);
+    if (pred) { ++launch_count(); build_kernel<float, true><<<grid, 128, 0, st>>>(a); }
+    else { ++launch_count(); build_kernel<float, false><<<grid, 128, 0, st>>>(a); }
   } else {
-    if (pred) build_kernel<uint32_t, true><<<grid, 128, 0, st>>>(a);
-    else build_kernel<uint32_t, false><<<grid, 128, 0, st>>>(a);
+    if (pred) { ++launch_count(); build_kernel<uint32_t, true><<<grid, 128, 0, st>>>(a); }
+    else { ++launch_count(); build_kernel<uint32_t, false><<<grid, 128, 0, st>>>(a); }
   }
   return cudaGetLastError();
 }
@@ -130,11 +135,11 @@ cudaError_t launch_decode(bool f32, bool pred, const BuildArgs &a, void *rows, i
   if (a.dec_rows <= 0) return cudaSuccess;
   const unsigned grid = (unsigned)a.dec_rows;
   if (f32) {
-    if (pred) decode_kernel<float, true><<<grid, 128, 0, st>>>(a, (float *)rows, rowsp);
-    else decode_kernel<float, false><<<grid, 128, 0, st>>>(a, (float *)rows, rowsp);
+    if (pred) { ++launch_count(); decode_kernel<float, true><<<grid, 128, 0, st>>>(a, (float *)rows, rowsp); }
+    else { ++launch_count(); decode_kernel<float, false><<<grid, 128, 0, st>>>(a, (float *)rows, rowsp); }
   } else {
-    if (pred) decode_kernel<uint32_t, true><<<grid, 128, 0, st>>>(a, (uint32_t *)rows, rowsp);
-    else decode_kernel<uint32_t, false><<<grid, 128, 0, st>>>(a, (uint32_t *)rows, rowsp);
+    if (pred) { ++launch_count(); decode_kernel<uint32_t, true><<<grid, 128, 0, st>>>(a, (uint32_t *)rows, rowsp); }
+    else { ++launch_count(); decode_kernel<uint32_t, false><<<grid, 128, 0, st>>>(a, (uint32_t *)rows, rowsp); }
   }
   return cudaGetLastError();
 }

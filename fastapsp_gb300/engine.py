@@ -146,6 +146,12 @@ class Engine:
         check(lib().fap_last_times(self._h, t), "fap_last_times")
         return dict(zip(["sssp", "floyd", "min_plus", "data", "total"], list(t)))
 
+    def last_launches(self) -> int:
+        """Kernels the last solve launched."""
+        v = C.c_int64(0)
+        check(lib().fap_last_launches(self._h, C.byref(v)), "fap_last_launches")
+        return int(v.value)
+
     def sssp_stats(self):
         """Counters of the last solve's SSSP phase."""
         v = (C.c_uint64 * 5)()

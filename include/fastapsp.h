@@ -171,6 +171,9 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value);
  * [sssp, floyd, min_plus, data, total] (the getTime* counters of
  * fap/fap.cpp:622-639, measured with CUDA events). */
 int fap_last_times(const fap_engine *e, double *times5);
+/* Number of kernels the last solve launched (no reference counterpart; the
+ * bench reports it as the GPU launch count of a step). */
+int fap_last_launches(const fap_engine *e, int64_t *count);
 
 /* ---- standalone kernels on caller device memory ------------------------- */
 
