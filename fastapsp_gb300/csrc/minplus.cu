@@ -524,13 +524,16 @@ __global__ void __launch_bounds__(kThreads, 2)
 //   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
-constexpr int kStripTiles = 16;
+constexpr int kStripTiles = 16;  // 128-column tiles per strip
 constexpr int kStripPairK = 48;   // largest K with two CTAs per SM
 constexpr int kStripMaxK = 100;   // largest K of the strip form (one CTA per SM above kStripPairK)
 constexpr int kOwnCap = 12;
 
+// Shared memory of the strip kernel with TN-column tiles, in bytes.
+template <int TN>
 __host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
-  return (size_t)4 * ks * kTile * 4 + (size_t)4 * kTile * 4 + (size_t)2 * kOwnCap * kTile * 4;
+  return ((size_t)2 * ks * TN + (size_t)(ks + 1) * TN + 3 * TN + (size_t)2 * kOwnCap * kTile +
+          (size_t)ks * kTile) * 4;
 }
 
 __device__ __forceinline__ const MpSegment &find_strip_segment(const MpSegment *__restrict__ segs,
@@ -543,18 +546,20 @@ __device__ __forceinline__ const MpSegment &find_strip_segment(const MpSegment *
   return segs[lo];
 }
 
-// Copies a ks x 128 tile of a row-major 4-byte matrix (rows < K, columns
-// [col0, col0 + 128) < N) into dst[ks][128]; each thread moves 4 consecutive
+// Copies a ks x TN tile of a row-major 4-byte matrix (rows < K, columns
+// [col0, col0 + TN) < N) into dst[ks][TN]; each thread moves 4 consecutive
 // columns of a row per pass (one 16-byte copy when `vec`), and writes `fill`
 // where the source is outside the matrix.
+template <int TN>
 __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *src, int64_t ld,
                                                 int K, int N, int ks, int col0, bool vec,
                                                 unsigned fill) {
+  constexpr int TPR = TN / 4;  // threads per row
   const int t = threadIdx.x;
-  const int j = (t & 31) * 4;
+  const int j = (t % TPR) * 4;
   const int col = col0 + j;
-  for (int kk = t >> 5; kk < ks; kk += kThreads / 32) {
-    unsigned *d = dst + kk * kTile + j;
+  for (int kk = t / TPR; kk < ks; kk += kThreads / TPR) {
+    unsigned *d = dst + kk * TN + j;
     const unsigned *g = src + (int64_t)kk * ld + col;
     if (kk < K && vec && col + 3 < N) {
       cp_async16(d, g);
@@ -570,11 +575,13 @@ __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *s
 
 // Turns the B values this thread copied (same mapping as strip_load_rows)
 // into keys (d << 7) | (k + 1).
+template <int TN>
 __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks) {
+  constexpr int TPR = TN / 4;
   const int t = threadIdx.x;
-  const int j = (t & 31) * 4;
-  for (int kk = t >> 5; kk < ks; kk += kThreads / 32) {
-    uint4 *p = reinterpret_cast<uint4 *>(Bs + kk * kTile + j);
+  const int j = (t % TPR) * 4;
+  for (int kk = t / TPR; kk < ks; kk += kThreads / TPR) {
+    uint4 *p = reinterpret_cast<uint4 *>(Bs + kk * TN + j);
     const unsigned idx = (unsigned)(kk & kMaxPackedK) + 1u;
     uint4 v = *p;
     v.x = (min(v.x, kPackH) << kIdxBits) | idx;
@@ -585,17 +592,22 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks) {
   }
 }
 
-template <bool PRED>
-__global__ void __launch_bounds__(kThreads, 2)
+// TN = 128: 128x128 tiles, 8x8 outputs per thread, two CTAs per SM (the form
+// used).  TN = 64 (128x64 tiles, 8x4 outputs per thread, three CTAs per SM)
+// measured within 1-4 % of it on this GPU, so occupancy is not what bounds
+// the kernel.  A strip always spans kStripTiles x 128 columns.
+template <bool PRED, int TN>
+__global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     mp_strip_kernel(const MpSegment *__restrict__ segs, int nseg, int ks) {
+  constexpr int CH = TN / 64;  // 64-column halves of a thread's outputs
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  unsigned *Bs = reinterpret_cast<unsigned *>(smem_raw);  // [2][ks][128]
-  int32_t *Bps = reinterpret_cast<int32_t *>(Bs + 2 * ks * kTile);  // [1 + ks][128]
-  int32_t *colp = Bps + (ks + 1) * kTile;  // col_part of the tile's columns
-  int32_t *coll = colp + kTile;            // col_local of the tile's columns
-  int32_t *ownidx = coll + kTile;          // own column: staging slot, or -2 (not staged); else -1
-  unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + kTile);  // [kOwnCap][128]
-  int32_t *Fpst = reinterpret_cast<int32_t *>(Fst + kOwnCap * kTile);  // [kOwnCap][128]
+  unsigned *Bs = reinterpret_cast<unsigned *>(smem_raw);  // [2][ks][TN]
+  int32_t *Bps = reinterpret_cast<int32_t *>(Bs + 2 * ks * TN);  // [1 + ks][TN]
+  int32_t *colp = Bps + (ks + 1) * TN;  // col_part of the tile's columns
+  int32_t *coll = colp + TN;            // col_local of the tile's columns
+  int32_t *ownidx = coll + TN;          // own column: staging slot, or -2 (not staged); else -1
+  unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + TN);  // [kOwnCap][128 rows]
+  int32_t *Fpst = reinterpret_cast<int32_t *>(Fst + kOwnCap * kTile);  // [kOwnCap][128 rows]
   unsigned *As = reinterpret_cast<unsigned *>(Fpst + kOwnCap * kTile);  // A^T [ks][128]
   __shared__ MpSegment seg;
   __shared__ int s_own[2];                   // own columns of the tile (per tile parity)
@@ -604,14 +616,15 @@ __global__ void __launch_bounds__(kThreads, 2)
     seg = find_strip_segment(segs, nseg, blockIdx.x);
     s_own[0] = s_own[1] = 0;
   }
-  if (threadIdx.x < kTile) Bps[threadIdx.x] = -1;  // predecessor of idx 0
+  if (threadIdx.x < TN) Bps[threadIdx.x] = -1;  // predecessor of idx 0
   __syncthreads();
   const MpSegment &s = seg;
   const int strips_x = (s.tiles_x + kStripTiles - 1) / kStripTiles;
   const int local = blockIdx.x - s.strip_begin;
   const int rt = local / strips_x;
-  const int jt0 = (local - rt * strips_x) * kStripTiles;
-  const int jt1 = min(jt0 + kStripTiles, s.tiles_x);
+  // column tiles of TN: this strip's 128-column tiles, split
+  const int jt0 = (local - rt * strips_x) * kStripTiles * (128 / TN);
+  const int jt1 = min(jt0 + kStripTiles * (128 / TN), (s.N + TN - 1) / TN);
   const int row0 = rt * kTile;
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
   const unsigned INF = Dist<uint32_t>::inf();
@@ -622,9 +635,9 @@ __global__ void __launch_bounds__(kThreads, 2)
 
   auto load_side = [&](int col0) {  // B's predecessor rows and column flags of a tile
     if (PRED)
-      strip_load_rows(reinterpret_cast<unsigned *>(Bps + kTile), reinterpret_cast<const unsigned *>(s.Bp),
-                      s.ldbp, s.K, s.N, kseg, col0, vec_bp, 0xffffffffu);
-    if (threadIdx.x < kTile) {
+      strip_load_rows<TN>(reinterpret_cast<unsigned *>(Bps + TN), reinterpret_cast<const unsigned *>(s.Bp),
+                          s.ldbp, s.K, s.N, kseg, col0, vec_bp, 0xffffffffu);
+    if (threadIdx.x < TN) {
       const int j = threadIdx.x, col = col0 + j;
       if (s.col_part != nullptr && col < s.N) {
         cp_async4(&colp[j], s.col_part + col);
@@ -644,27 +657,27 @@ __global__ void __launch_bounds__(kThreads, 2)
     else
       *d = INF;
   }
-  strip_load_rows(Bs, static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, kseg, jt0 * kTile, vec_b, INF);
+  strip_load_rows<TN>(Bs, static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, kseg, jt0 * TN, vec_b, INF);
   cp_async_commit();
-  load_side(jt0 * kTile);
+  load_side(jt0 * TN);
   cp_async_commit();
 
   for (int jt = jt0; jt < jt1; jt++) {
     const int buf = (jt - jt0) & 1;
-    unsigned *Bcur = Bs + buf * ks * kTile;
+    unsigned *Bcur = Bs + buf * ks * TN;
     if (jt + 1 < jt1)
-      strip_load_rows(Bs + (buf ^ 1) * ks * kTile, static_cast<const unsigned *>(s.B), s.ldb, s.K,
-                      s.N, kseg, (jt + 1) * kTile, vec_b, INF);
+      strip_load_rows<TN>(Bs + (buf ^ 1) * ks * TN, static_cast<const unsigned *>(s.B), s.ldb, s.K,
+                          s.N, kseg, (jt + 1) * TN, vec_b, INF);
     cp_async_commit();
     cp_async_wait_1();  // all but the next tile's B have landed
     if (jt == jt0)
       for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads)
         As[idx] = min(As[idx], kPackH) << kIdxBits;
-    strip_keys_b(Bcur, kseg);
-    // List the tile's own columns (threads 0..127 copied their column's flags;
-    // slots are taken in any order through a counter).
+    strip_keys_b<TN>(Bcur, kseg);
+    // List the tile's own columns (threads 0..TN-1 copied their column's
+    // flags; slots are taken in any order through a counter).
     if (threadIdx.x == 0) s_own[buf ^ 1] = 0;  // used by the next tile
-    if (threadIdx.x < kTile) {
+    if (threadIdx.x < TN) {
       const int j = threadIdx.x;
       const bool own = colp[j] == s.part;
       const unsigned bal = __ballot_sync(0xffffffffu, own);
@@ -693,32 +706,32 @@ __global__ void __launch_bounds__(kThreads, 2)
       cp_async_commit();
     }
 
-    unsigned acc[8][8];
+    unsigned acc[8][4 * CH];
 #pragma unroll
     for (int r = 0; r < 8; r++)
 #pragma unroll
-      for (int c = 0; c < 8; c++) acc[r][c] = kPackH << kIdxBits;
-    // Operands of step k + 1 are loaded while step k's 64 add-mins issue.
+      for (int c = 0; c < 4 * CH; c++) acc[r][c] = kPackH << kIdxBits;
+    // Operands of step k + 1 are loaded while step k's add-mins issue.
     if (kseg > 0) {
       const unsigned *acol = As + ty * 4;
       const unsigned *bcol = Bcur + tx * 4;
       uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
       uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
       uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
-      uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kBlk);
+      uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kBlk) : nb0;
 #pragma unroll 2
       for (int kk = 0; kk < kseg; kk++) {
         const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
         const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
-        const int kn = (kk + 1 < kseg ? kk + 1 : kk) * kTile;
-        na0 = *reinterpret_cast<const uint4 *>(acol + kn);
-        na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
-        nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
-        nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
+        const int kn = kk + 1 < kseg ? kk + 1 : kk;
+        na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
+        na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
+        nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
+        if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
 #pragma unroll
         for (int r = 0; r < 8; r++)
 #pragma unroll
-          for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+          for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
       }
     }
 
@@ -729,11 +742,11 @@ __global__ void __launch_bounds__(kThreads, 2)
     // Epilogue: distances, predecessors from the staged rows, own-part
     // columns from the part's Floyd-Warshall matrix (only when the tile has
     // any; the test is uniform over the CTA).
-    const int colbase = jt * kTile;
+    const int colbase = jt * TN;
     unsigned ownmask = 0;  // bit h * 4 + q: this thread's column sc0 + q of half h is the part's own
     if (nown > 0) {
 #pragma unroll
-      for (int c = 0; c < 8; c++)
+      for (int c = 0; c < 4 * CH; c++)
         if (ownidx[(c >> 2) * kBlk + tx * 4 + (c & 3)] != -1) ownmask |= 1u << c;
     }
 #pragma unroll
@@ -743,7 +756,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       unsigned *crow = static_cast<unsigned *>(s.C) + (int64_t)row * s.ldc;
       int32_t *prow = PRED ? s.Cp + (int64_t)row * s.ldcp : nullptr;
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
+      for (int h = 0; h < CH; h++) {
         const int sc0 = h * kBlk + tx * 4;
         const int col0 = colbase + sc0;
         if (col0 >= s.N) continue;
@@ -754,7 +767,7 @@ __global__ void __launch_bounds__(kThreads, 2)
           const unsigned key = acc[r][h * 4 + q];
           const unsigned dist = key >> kIdxBits;
           d[q] = dist >= kPackH ? INF : dist;
-          if (PRED) p[q] = Bps[(key & kIdxMask) * kTile + sc0 + q];
+          if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
         }
         if ((ownmask >> (h * 4)) & 0xfu) {
 #pragma unroll
@@ -785,7 +798,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
     }
     __syncthreads();  // B[buf], Bp and the column flags are free again
-    if (jt + 1 < jt1) load_side((jt + 1) * kTile);
+    if (jt + 1 < jt1) load_side((jt + 1) * TN);
     cp_async_commit();
   }
   cp_async_wait_0();
@@ -1307,11 +1320,11 @@ cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int tiles, int ti
   return cudaGetLastError();
 }
 
-template <bool PRED>
+template <bool PRED, int TN>
 cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks, cudaStream_t st) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
   ++launch_count();
-  mp_strip_kernel<PRED><<<strips, kThreads, strip_smem_bytes(ks), st>>>(d_segs, nseg, ks);
+  mp_strip_kernel<PRED, TN><<<strips, kThreads, strip_smem_bytes<TN>(ks), st>>>(d_segs, nseg, ks);
   return cudaGetLastError();
 }
 
@@ -1351,8 +1364,8 @@ cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, 
                                   int max_k, cudaStream_t st) {
   if (max_k < 0 || max_k > kStripMaxK) return cudaErrorInvalidValue;
   const int ks = (max_k + 3) & ~3;
-  return pred ? launch_strip_t<true>(d_segs, nseg, strips, ks, st)
-              : launch_strip_t<false>(d_segs, nseg, strips, ks, st);
+  return pred ? launch_strip_t<true, 128>(d_segs, nseg, strips, ks, st)
+              : launch_strip_t<false, 128>(d_segs, nseg, strips, ks, st);
 }
 
 int minplus_strip_tiles() { return kStripTiles; }
@@ -1405,13 +1418,14 @@ cudaError_t init_minplus_kernels() {
   if ((e = set_mp_attr<uint32_t, false>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<true>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<false>()) != cudaSuccess) return e;
-  const int smax = (int)strip_smem_bytes((kStripMaxK + 3) & ~3);
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const int smax = (int)strip_smem_bytes<128>((kStripMaxK + 3) & ~3);
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smax)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smax)) != cudaSuccess)
     return e;
+
   if ((e = cudaFuncSetAttribute(fw_pivot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(PivotSmem))) != cudaSuccess)
     return e;
