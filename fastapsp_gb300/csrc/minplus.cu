@@ -574,9 +574,10 @@ __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *s
 }
 
 // Turns the B values this thread copied (same mapping as strip_load_rows)
-// into keys (d << 7) | (k + 1).
+// into keys (d << 7) | (k + 1), and sets bit k of kmask (a 128-bit mask in
+// shared memory) for every row k that has a finite entry in the tile.
 template <int TN>
-__device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks) {
+__device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kmask) {
   constexpr int TPR = TN / 4;
   const int t = threadIdx.x;
   const int j = (t % TPR) * 4;
@@ -584,11 +585,13 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks) {
     uint4 *p = reinterpret_cast<uint4 *>(Bs + kk * TN + j);
     const unsigned idx = (unsigned)(kk & kMaxPackedK) + 1u;
     uint4 v = *p;
+    const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < kPackH;
     v.x = (min(v.x, kPackH) << kIdxBits) | idx;
     v.y = (min(v.y, kPackH) << kIdxBits) | idx;
     v.z = (min(v.z, kPackH) << kIdxBits) | idx;
     v.w = (min(v.w, kPackH) << kIdxBits) | idx;
     *p = v;
+    if (fin) atomicOr(&kmask[kk >> 5], 1u << (kk & 31));
   }
 }
 
@@ -612,10 +615,12 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
   __shared__ MpSegment seg;
   __shared__ int s_own[2];                   // own columns of the tile (per tile parity)
   __shared__ int16_t s_ownlist[2][kOwnCap];  // their tile columns, by slot
+  __shared__ unsigned s_kmask[2][4];         // rows k of B with a finite entry (per tile parity)
   if (threadIdx.x == 0) {
     seg = find_strip_segment(segs, nseg, blockIdx.x);
     s_own[0] = s_own[1] = 0;
   }
+  if (threadIdx.x < 8) (&s_kmask[0][0])[threadIdx.x] = 0u;
   if (threadIdx.x < TN) Bps[threadIdx.x] = -1;  // predecessor of idx 0
   __syncthreads();
   const MpSegment &s = seg;
@@ -673,10 +678,11 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     if (jt == jt0)
       for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads)
         As[idx] = min(As[idx], kPackH) << kIdxBits;
-    strip_keys_b<TN>(Bcur, kseg);
+    strip_keys_b<TN>(Bcur, kseg, s_kmask[buf]);
     // List the tile's own columns (threads 0..TN-1 copied their column's
     // flags; slots are taken in any order through a counter).
     if (threadIdx.x == 0) s_own[buf ^ 1] = 0;  // used by the next tile
+    if (threadIdx.x < 4) s_kmask[buf ^ 1][threadIdx.x] = 0u;
     if (threadIdx.x < TN) {
       const int j = threadIdx.x;
       const bool own = colp[j] == s.part;
@@ -711,27 +717,70 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 4 * CH; c++) acc[r][c] = kPackH << kIdxBits;
-    // Operands of step k + 1 are loaded while step k's add-mins issue.
-    if (kseg > 0) {
+    // Only the steps k whose B row has a finite entry in this tile can change
+    // an output (any other candidate is at least "unreached", which never
+    // wins).  When every row has one the loop runs over all k (unrolled);
+    // otherwise it walks the set bits of the tile's row mask -- on graphs
+    // with limited reachability most rows are skipped.  Either way the next
+    // step's operands load while the current step's add-mins issue.
+    {
       const unsigned *acol = As + ty * 4;
       const unsigned *bcol = Bcur + tx * 4;
-      uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
-      uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
-      uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
-      uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kBlk) : nb0;
+      unsigned long long mlo = (unsigned long long)s_kmask[buf][0] | ((unsigned long long)s_kmask[buf][1] << 32);
+      unsigned long long mhi = (unsigned long long)s_kmask[buf][2] | ((unsigned long long)s_kmask[buf][3] << 32);
+      const int nact = __popcll(mlo) + __popcll(mhi);
+      if (nact == s.K && s.K > 0) {
+        uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
+        uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
+        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
+        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kBlk) : nb0;
 #pragma unroll 2
-      for (int kk = 0; kk < kseg; kk++) {
-        const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
-        const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
-        const int kn = kk + 1 < kseg ? kk + 1 : kk;
-        na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
-        na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
-        nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
-        if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
+        for (int kk = 0; kk < kseg; kk++) {
+          const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
+          const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
+          const int kn = kk + 1 < kseg ? kk + 1 : kk;
+          na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
+          na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
+          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
 #pragma unroll
-        for (int r = 0; r < 8; r++)
+          for (int r = 0; r < 8; r++)
 #pragma unroll
-          for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+            for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+        }
+      } else if (nact > 0) {
+        auto next_k = [&]() {  // lowest remaining step, or -1
+          if (mlo) {
+            const int b = __ffsll(mlo) - 1;
+            mlo &= mlo - 1ull;
+            return b;
+          }
+          if (mhi) {
+            const int b = __ffsll(mhi) - 1;
+            mhi &= mhi - 1ull;
+            return 64 + b;
+          }
+          return -1;
+        };
+        int kk = next_k();
+        uint4 na0 = *reinterpret_cast<const uint4 *>(acol + kk * kTile);
+        uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kk * kTile + kBlk);
+        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * TN);
+        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kk * TN + kBlk) : nb0;
+        while (kk >= 0) {
+          const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
+          const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
+          kk = next_k();
+          const int kn = kk >= 0 ? kk : 0;
+          na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
+          na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
+          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
+#pragma unroll
+          for (int r = 0; r < 8; r++)
+#pragma unroll
+            for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+        }
       }
     }
 
@@ -858,7 +907,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FwStripSmem &sm = *reinterpret_cast<FwStripSmem *>(smem_raw);
   __shared__ MpSegment seg;
+  __shared__ unsigned s_kmask[2][2];  // rows k of B with a finite entry (per tile parity)
   if (threadIdx.x == 0) seg = find_strip_segment(segs, nseg, blockIdx.x);
+  if (threadIdx.x < 4) (&s_kmask[0][0])[threadIdx.x] = 0u;
   __syncthreads();
   const MpSegment &s = seg;
   const int sx = fw_strips_x(s);
@@ -912,18 +963,22 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (jt == jt0)
       for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads)
         (&sm.A[0][0])[idx] = min((&sm.A[0][0])[idx], kPackH) << kIdxBits;
-    {
+    {  // B keys; a warp converts whole rows and marks those with a finite entry
       const int j = (threadIdx.x & 31) * 4;
       for (int kk = threadIdx.x >> 5; kk < kBlk; kk += kThreads / 32) {
         uint4 *p = reinterpret_cast<uint4 *>(&sm.B[buf][kk][j]);
         const unsigned idx = (unsigned)kk + 1u;
         uint4 v = *p;
+        const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < kPackH;
         v.x = (min(v.x, kPackH) << kIdxBits) | idx;
         v.y = (min(v.y, kPackH) << kIdxBits) | idx;
         v.z = (min(v.z, kPackH) << kIdxBits) | idx;
         v.w = (min(v.w, kPackH) << kIdxBits) | idx;
         *p = v;
+        if (__any_sync(0xffffffffu, fin) && (threadIdx.x & 31) == 0)
+          atomicOr(&s_kmask[buf][kk >> 5], 1u << (kk & 31));
       }
+      if (threadIdx.x < 2) s_kmask[buf ^ 1][threadIdx.x] = 0u;  // for the next tile
     }
     __syncthreads();
     // Stage this tile's C behind the DPX loop.
@@ -954,26 +1009,56 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 8; c++) acc[r][c] = kPackH << kIdxBits;
-    if (kseg > 0) {  // operands of step k + 1 load while step k issues
+    // Only steps k whose B row (pivot row k over this tile's columns) has a
+    // finite entry can improve an output: all k (unrolled) when every row
+    // has one, else the set bits of the row mask.  The next step's operands
+    // load while the current step's add-mins issue.
+    {
       const unsigned *acol = &sm.A[0][ty * 4];
       const unsigned *bcol = &sm.B[buf][0][tx * 4];
-      uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
-      uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
-      uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
-      uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kBlk);
+      unsigned long long msk = (unsigned long long)s_kmask[buf][0] | ((unsigned long long)s_kmask[buf][1] << 32);
+      if (kseg < 64) msk &= (1ull << kseg) - 1ull;
+      if (__popcll(msk) == s.K && s.K > 0) {
+        uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
+        uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
+        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
+        uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kBlk);
 #pragma unroll 2
-      for (int kk = 0; kk < kseg; kk++) {
-        const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
-        const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
-        const int kn = (kk + 1 < kseg ? kk + 1 : kk) * kTile;
-        na0 = *reinterpret_cast<const uint4 *>(acol + kn);
-        na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
-        nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
-        nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
+        for (int kk = 0; kk < kseg; kk++) {
+          const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
+          const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
+          const int kn = (kk + 1 < kseg ? kk + 1 : kk) * kTile;
+          na0 = *reinterpret_cast<const uint4 *>(acol + kn);
+          na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
+          nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
 #pragma unroll
-        for (int r = 0; r < 8; r++)
+          for (int r = 0; r < 8; r++)
 #pragma unroll
-          for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+            for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+        }
+      } else if (msk) {
+        int kk = __ffsll(msk) - 1;
+        msk &= msk - 1ull;
+        uint4 na0 = *reinterpret_cast<const uint4 *>(acol + kk * kTile);
+        uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kk * kTile + kBlk);
+        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile);
+        uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile + kBlk);
+        while (kk >= 0) {
+          const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
+          const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
+          kk = msk ? __ffsll(msk) - 1 : -1;
+          if (msk) msk &= msk - 1ull;
+          const int kn = (kk >= 0 ? kk : 0) * kTile;
+          na0 = *reinterpret_cast<const uint4 *>(acol + kn);
+          na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
+          nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
+#pragma unroll
+          for (int r = 0; r < 8; r++)
+#pragma unroll
+            for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+        }
       }
     }
     cp_async_wait_0();
