@@ -616,11 +616,13 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
   __shared__ int s_own[2];                   // own columns of the tile (per tile parity)
   __shared__ int16_t s_ownlist[2][kOwnCap];  // their tile columns, by slot
   __shared__ unsigned s_kmask[2][4];         // rows k of B with a finite entry (per tile parity)
+  __shared__ unsigned s_amask[4];            // columns k of A with a finite entry (per strip)
   if (threadIdx.x == 0) {
     seg = find_strip_segment(segs, nseg, blockIdx.x);
     s_own[0] = s_own[1] = 0;
   }
   if (threadIdx.x < 8) (&s_kmask[0][0])[threadIdx.x] = 0u;
+  if (threadIdx.x < 4) s_amask[threadIdx.x] = 0u;
   if (threadIdx.x < TN) Bps[threadIdx.x] = -1;  // predecessor of idx 0
   __syncthreads();
   const MpSegment &s = seg;
@@ -675,9 +677,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
                           s.N, kseg, (jt + 1) * TN, vec_b, INF);
     cp_async_commit();
     cp_async_wait_1();  // all but the next tile's B have landed
-    if (jt == jt0)
-      for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads)
-        As[idx] = min(As[idx], kPackH) << kIdxBits;
+    if (jt == jt0)  // A keys; a warp converts 32 entries of one step k and marks finite ones
+      for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
+        const unsigned v = As[idx];
+        As[idx] = min(v, kPackH) << kIdxBits;
+        const int kk = idx >> 7;
+        if (__any_sync(0xffffffffu, v < kPackH) && (threadIdx.x & 31) == 0)
+          atomicOr(&s_amask[kk >> 5], 1u << (kk & 31));
+      }
     strip_keys_b<TN>(Bcur, kseg, s_kmask[buf]);
     // List the tile's own columns (threads 0..TN-1 copied their column's
     // flags; slots are taken in any order through a counter).
@@ -717,17 +724,19 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 4 * CH; c++) acc[r][c] = kPackH << kIdxBits;
-    // Only the steps k whose B row has a finite entry in this tile can change
-    // an output (any other candidate is at least "unreached", which never
-    // wins).  When every row has one the loop runs over all k (unrolled);
+    // Only the steps k whose B row has a finite entry in this tile and whose
+    // A column has one in this strip can change an output (any other
+    // candidate is at least "unreached", which never wins).  When every row has one the loop runs over all k (unrolled);
     // otherwise it walks the set bits of the tile's row mask -- on graphs
     // with limited reachability most rows are skipped.  Either way the next
     // step's operands load while the current step's add-mins issue.
     {
       const unsigned *acol = As + ty * 4;
       const unsigned *bcol = Bcur + tx * 4;
-      unsigned long long mlo = (unsigned long long)s_kmask[buf][0] | ((unsigned long long)s_kmask[buf][1] << 32);
-      unsigned long long mhi = (unsigned long long)s_kmask[buf][2] | ((unsigned long long)s_kmask[buf][3] << 32);
+      unsigned long long mlo = (unsigned long long)(s_kmask[buf][0] & s_amask[0]) |
+                               ((unsigned long long)(s_kmask[buf][1] & s_amask[1]) << 32);
+      unsigned long long mhi = (unsigned long long)(s_kmask[buf][2] & s_amask[2]) |
+                               ((unsigned long long)(s_kmask[buf][3] & s_amask[3]) << 32);
       const int nact = __popcll(mlo) + __popcll(mhi);
       if (nact == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
@@ -908,8 +917,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   FwStripSmem &sm = *reinterpret_cast<FwStripSmem *>(smem_raw);
   __shared__ MpSegment seg;
   __shared__ unsigned s_kmask[2][2];  // rows k of B with a finite entry (per tile parity)
+  __shared__ unsigned s_amask[2];     // columns k of A with a finite entry (per strip)
   if (threadIdx.x == 0) seg = find_strip_segment(segs, nseg, blockIdx.x);
   if (threadIdx.x < 4) (&s_kmask[0][0])[threadIdx.x] = 0u;
+  if (threadIdx.x < 2) s_amask[threadIdx.x] = 0u;
   __syncthreads();
   const MpSegment &s = seg;
   const int sx = fw_strips_x(s);
@@ -960,9 +971,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 col_bases(jt + 1), vec_b, INF);
     cp_async_commit();
     cp_async_wait_1();  // A, this tile's B and its predecessors have landed
-    if (jt == jt0)
-      for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads)
-        (&sm.A[0][0])[idx] = min((&sm.A[0][0])[idx], kPackH) << kIdxBits;
+    if (jt == jt0)  // A keys; a warp converts 32 entries of one step k and marks finite ones
+      for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads) {
+        const unsigned v = (&sm.A[0][0])[idx];
+        (&sm.A[0][0])[idx] = min(v, kPackH) << kIdxBits;
+        const int kk = idx >> 7;
+        if (__any_sync(0xffffffffu, v < kPackH) && (threadIdx.x & 31) == 0)
+          atomicOr(&s_amask[kk >> 5], 1u << (kk & 31));
+      }
     {  // B keys; a warp converts whole rows and marks those with a finite entry
       const int j = (threadIdx.x & 31) * 4;
       for (int kk = threadIdx.x >> 5; kk < kBlk; kk += kThreads / 32) {
@@ -1009,14 +1025,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 8; c++) acc[r][c] = kPackH << kIdxBits;
-    // Only steps k whose B row (pivot row k over this tile's columns) has a
-    // finite entry can improve an output: all k (unrolled) when every row
+    // Only steps k whose B row (pivot row k over this tile's columns) and A
+    // column (over this strip's rows) have a finite entry can improve an
+    // output: all k (unrolled) when every row
     // has one, else the set bits of the row mask.  The next step's operands
     // load while the current step's add-mins issue.
     {
       const unsigned *acol = &sm.A[0][ty * 4];
       const unsigned *bcol = &sm.B[buf][0][tx * 4];
-      unsigned long long msk = (unsigned long long)s_kmask[buf][0] | ((unsigned long long)s_kmask[buf][1] << 32);
+      unsigned long long msk = (unsigned long long)(s_kmask[buf][0] & s_amask[0]) |
+                               ((unsigned long long)(s_kmask[buf][1] & s_amask[1]) << 32);
       if (kseg < 64) msk &= (1ull << kseg) - 1ull;
       if (__popcll(msk) == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
