@@ -58,6 +58,7 @@ SIGNATURES = {
     "fap_solve": (C.c_int, [_p, _p, _p, _i32, _p]),
     "fap_last_times": (C.c_int, [_p, C.POINTER(C.c_double)]),
     "fap_last_launches": (C.c_int, [_p, C.POINTER(C.c_int64)]),
+    "fap_minplus_counters": (C.c_int, [_p, C.POINTER(C.c_uint64), _i32]),
     "fap_minplus": (C.c_int, [_p, _i32, _i32, _i32, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i64,
                               _p, _i64, _p]),
     "fap_floyd_batched": (C.c_int, [_p, _i32, _i32, _p, _p, _p, _p, _p]),

@@ -1272,6 +1272,16 @@ int fap_last_times(const fap_engine *e, double *times5) {
   return FAP_OK;
 }
 
+int fap_minplus_counters(fap_engine *e, uint64_t *out3, int32_t reset) {
+  if (!e || !out3) return set_error(FAP_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard g(e->device);
+  unsigned long long v[3] = {0, 0, 0};
+  FAP_CUDA(fapk::strip_counters(v, reset != 0));
+  for (int i = 0; i < 3; i++) out3[i] = v[i];
+  return FAP_OK;
+}
+
 int fap_last_launches(const fap_engine *e, int64_t *count) {
   if (!e || !count) return set_error(FAP_ERR_INVALID, "null argument");
   *count = e->last_launches;

@@ -38,6 +38,9 @@ int minplus_strip_pair_k();  // largest K at which it runs two CTAs per SM
 // Largest finite int32 entry of the matrices, atomicMax-ed into *out.
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st);
 unsigned pack_limit();
+// Work counters of the strip min-plus on the current device: [tiles, tiles
+// with no active step, active steps over all tiles]; optionally reset.
+cudaError_t strip_counters(unsigned long long out[3], bool reset);
 int max_packed_k();
 cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njobs,
                            cudaStream_t st);

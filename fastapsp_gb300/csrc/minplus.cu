@@ -524,6 +524,10 @@ __global__ void __launch_bounds__(kThreads, 2)
 //   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
+// Work counters of the strip min-plus (diagnostics): [tiles, tiles with no
+// active step, active steps summed over tiles].  One atomic per tile.
+__device__ unsigned long long g_strip_counters[3];
+
 constexpr int kStripTiles = 16;  // 128-column tiles per strip
 constexpr int kStripPairK = 48;   // largest K with two CTAs per SM
 constexpr int kStripMaxK = 100;   // largest K of the strip form (one CTA per SM above kStripPairK)
@@ -738,6 +742,11 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
       unsigned long long mhi = (unsigned long long)(s_kmask[buf][2] & s_amask[2]) |
                                ((unsigned long long)(s_kmask[buf][3] & s_amask[3]) << 32);
       const int nact = __popcll(mlo) + __popcll(mhi);
+      if (threadIdx.x == 0) {
+        atomicAdd(&g_strip_counters[0], 1ull);
+        if (nact == 0) atomicAdd(&g_strip_counters[1], 1ull);
+        atomicAdd(&g_strip_counters[2], (unsigned long long)nact);
+      }
       if (nact == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
         uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
@@ -818,14 +827,20 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
         const int sc0 = h * kBlk + tx * 4;
         const int col0 = colbase + sc0;
         if (col0 >= s.N) continue;
-        unsigned d[4];
-        int32_t p[4];
+        unsigned d[4] = {INF, INF, INF, INF};
+        int32_t p[4] = {-1, -1, -1, -1};
+        // a quad of unreached outputs (the common case on sparse graphs) needs
+        // no decode and no predecessor gathers
+        const unsigned qmin = min(min(acc[r][h * 4], acc[r][h * 4 + 1]),
+                                  min(acc[r][h * 4 + 2], acc[r][h * 4 + 3]));
+        if (qmin < (kPackH << kIdxBits)) {
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const unsigned key = acc[r][h * 4 + q];
-          const unsigned dist = key >> kIdxBits;
-          d[q] = dist >= kPackH ? INF : dist;
-          if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
+          for (int q = 0; q < 4; q++) {
+            const unsigned key = acc[r][h * 4 + q];
+            const unsigned dist = key >> kIdxBits;
+            d[q] = dist >= kPackH ? INF : dist;
+            if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
+          }
         }
         if ((ownmask >> (h * 4)) & 0xfu) {
 #pragma unroll
@@ -1490,6 +1505,13 @@ cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cu
 }
 
 unsigned pack_limit() { return kPackH; }
+
+cudaError_t strip_counters(unsigned long long out[3], bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_strip_counters, sizeof(unsigned long long) * 3);
+  if (e != cudaSuccess || !reset) return e;
+  const unsigned long long zero[3] = {0, 0, 0};
+  return cudaMemcpyToSymbol(g_strip_counters, zero, sizeof(zero));
+}
 int max_packed_k() { return kMaxPackedK; }
 
 cudaError_t launch_fw_pivot(bool pred, const FwDiagJob *d_jobs, int njobs, cudaStream_t st) {

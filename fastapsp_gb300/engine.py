@@ -152,6 +152,13 @@ class Engine:
         check(lib().fap_last_launches(self._h, C.byref(v)), "fap_last_launches")
         return int(v.value)
 
+    def minplus_counters(self, reset: bool = True):
+        """Strip min-plus work counters since the last reset: tiles, tiles with
+        no active k-step, active k-steps over all tiles."""
+        v = (C.c_uint64 * 3)()
+        check(lib().fap_minplus_counters(self._h, v, int(bool(reset))), "fap_minplus_counters")
+        return dict(zip(["tiles", "empty_tiles", "active_steps"], list(v)))
+
     def sssp_stats(self):
         """Counters of the last solve's SSSP phase."""
         v = (C.c_uint64 * 5)()

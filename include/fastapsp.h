@@ -174,6 +174,11 @@ int fap_last_times(const fap_engine *e, double *times5);
 /* Number of kernels the last solve launched (no reference counterpart; the
  * bench reports it as the GPU launch count of a step). */
 int fap_last_launches(const fap_engine *e, int64_t *count);
+/* Work counters of the min-plus strip kernel on the engine's GPU since the
+ * last reset (no reference counterpart; diagnostics of the sparsity skip):
+ * [128x128 tiles, tiles with no active k-step, active k-steps summed over
+ * tiles].  reset != 0 clears them after reading. */
+int fap_minplus_counters(fap_engine *e, uint64_t *out3, int32_t reset);
 
 /* ---- standalone kernels on caller device memory ------------------------- */
 
