@@ -536,7 +536,7 @@ constexpr int kOwnCap = 12;
 // Shared memory of the strip kernel with TN-column tiles, in bytes.
 template <int TN>
 __host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
-  return ((size_t)2 * ks * TN + (size_t)(ks + 1) * TN + 3 * TN + (size_t)2 * kOwnCap * kTile +
+  return ((size_t)2 * ks * TN + (size_t)(ks + 1) * TN + 6 * TN + (size_t)2 * kOwnCap * kTile +
           (size_t)ks * kTile) * 4;
 }
 
@@ -610,10 +610,10 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned *Bs = reinterpret_cast<unsigned *>(smem_raw);  // [2][ks][TN]
   int32_t *Bps = reinterpret_cast<int32_t *>(Bs + 2 * ks * TN);  // [1 + ks][TN]
-  int32_t *colp = Bps + (ks + 1) * TN;  // col_part of the tile's columns
-  int32_t *coll = colp + TN;            // col_local of the tile's columns
-  int32_t *ownidx = coll + TN;          // own column: staging slot, or -2 (not staged); else -1
-  unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + TN);  // [kOwnCap][128 rows]
+  int32_t *colp = Bps + (ks + 1) * TN;  // [2][TN] col_part of the tile's columns (per tile parity)
+  int32_t *coll = colp + 2 * TN;        // [2][TN] col_local of the tile's columns
+  int32_t *ownidx = coll + 2 * TN;      // [2][TN] own column: staging slot, or -2 (not staged); else -1
+  unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + 2 * TN);  // [kOwnCap][128 rows]
   int32_t *Fpst = reinterpret_cast<int32_t *>(Fst + kOwnCap * kTile);  // [kOwnCap][128 rows]
   unsigned *As = reinterpret_cast<unsigned *>(Fpst + kOwnCap * kTile);  // A^T [ks][128]
   __shared__ MpSegment seg;
@@ -644,22 +644,49 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
   const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
   const bool vec_c = vec_stores_ok<PRED>(s);
 
-  auto load_side = [&](int col0) {  // B's predecessor rows and column flags of a tile
-    if (PRED)
-      strip_load_rows<TN>(reinterpret_cast<unsigned *>(Bps + TN), reinterpret_cast<const unsigned *>(s.Bp),
-                          s.ldbp, s.K, s.N, kseg, col0, vec_bp, 0xffffffffu);
+  auto load_flags = [&](int col0, int fb) {  // column flags of a tile, into parity fb
     if (threadIdx.x < TN) {
       const int j = threadIdx.x, col = col0 + j;
       if (s.col_part != nullptr && col < s.N) {
-        cp_async4(&colp[j], s.col_part + col);
-        cp_async4(&coll[j], s.col_local + col);
+        cp_async4(&colp[fb * TN + j], s.col_part + col);
+        cp_async4(&coll[fb * TN + j], s.col_local + col);
       } else {
-        colp[j] = -1;
+        colp[fb * TN + j] = -1;
+      }
+    }
+  };
+  // B's predecessor rows of the steps k in (lo, hi) only (row k goes to Bps
+  // row k + 1); warp w copies every eighth of them, 4 columns a lane.
+  auto load_bp_rows = [&](int col0, unsigned long long lo, unsigned long long hi) {
+    const int warp = threadIdx.x >> 5;
+    const int j = (threadIdx.x & 31) * 4, col = col0 + j;
+    int i = 0;
+    while (lo | hi) {
+      int k;
+      if (lo) {
+        k = __ffsll(lo) - 1;
+        lo &= lo - 1ull;
+      } else {
+        k = 64 + __ffsll(hi) - 1;
+        hi &= hi - 1ull;
+      }
+      if ((i++ & 7) == warp && j < TN) {
+        int32_t *d = Bps + (k + 1) * TN + j;
+        const int32_t *g = s.Bp + (int64_t)k * s.ldbp + col;
+        if (vec_bp && col + 3 < s.N) {
+          cp_async16(d, g);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            if (col + q < s.N) cp_async4(d + q, g + q);
+            else d[q] = -1;
+          }
+        }
       }
     }
   };
 
-  // Prologue: A and B of the first tile | side data of the first tile.
+  // Prologue: A, B and the column flags of the first tile.
   for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
     const int kk = idx >> 7, m = idx & (kTile - 1);
     unsigned *d = &As[idx];
@@ -669,18 +696,23 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
       *d = INF;
   }
   strip_load_rows<TN>(Bs, static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, kseg, jt0 * TN, vec_b, INF);
-  cp_async_commit();
-  load_side(jt0 * TN);
+  load_flags(jt0 * TN, 0);
   cp_async_commit();
 
+  // Per tile: two barriers.  (A) after the B keys, masks and own-column list;
+  // then the tile's predecessor rows (active steps only), its staged FW
+  // values and the next tile's flags are copied (one group), then the next
+  // tile's B (a second group), while the add-mins issue; (B) once the first
+  // group has landed, before the epilogue.  The next B is waited for at the
+  // top of the next tile, so it also has the epilogue to land.  Every buffer
+  // written between (A) and (B) was last read before (A); the flags and
+  // own-column slots are double-buffered by tile parity because the epilogue
+  // of one tile runs into the next tile's list without a barrier.
+  unsigned long long n_tiles = 0, n_empty = 0, n_steps = 0;  // work counters (thread 0)
   for (int jt = jt0; jt < jt1; jt++) {
     const int buf = (jt - jt0) & 1;
     unsigned *Bcur = Bs + buf * ks * TN;
-    if (jt + 1 < jt1)
-      strip_load_rows<TN>(Bs + (buf ^ 1) * ks * TN, static_cast<const unsigned *>(s.B), s.ldb, s.K,
-                          s.N, kseg, (jt + 1) * TN, vec_b, INF);
-    cp_async_commit();
-    cp_async_wait_1();  // all but the next tile's B have landed
+    cp_async_wait_0();  // this tile's B (and, first tile, A and the flags)
     if (jt == jt0)  // A keys; a warp converts 32 entries of one step k and marks finite ones
       for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
         const unsigned v = As[idx];
@@ -696,7 +728,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     if (threadIdx.x < 4) s_kmask[buf ^ 1][threadIdx.x] = 0u;
     if (threadIdx.x < TN) {
       const int j = threadIdx.x;
-      const bool own = colp[j] == s.part;
+      const bool own = colp[buf * TN + j] == s.part;
       const unsigned bal = __ballot_sync(0xffffffffu, own);
       int base = 0;
       if ((threadIdx.x & 31) == 0 && bal) base = atomicAdd(&s_own[buf], __popc(bal));
@@ -707,46 +739,52 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
         if (slot < kOwnCap) s_ownlist[buf][slot] = (int16_t)j;
         else slot = -2;
       }
-      ownidx[j] = slot;
+      ownidx[buf * TN + j] = slot;
     }
-    __syncthreads();
+    __syncthreads();  // (A)
+    if (jt + 1 < jt1) load_flags((jt + 1) * TN, buf ^ 1);
     const int nown = min(s_own[buf], kOwnCap);
     if (nown > 0) {  // stage the FW values of the own columns (rows of this tile)
       for (int it = threadIdx.x; it < nown * kTile; it += kThreads) {
         const int sl = it / kTile, m = it - sl * kTile;
         if (row0 + m < s.M) {
-          const int64_t off = (int64_t)(row0 + m) * s.ldf + (coll[s_ownlist[buf][sl]] - s.local0);
+          const int64_t off =
+              (int64_t)(row0 + m) * s.ldf + (coll[buf * TN + s_ownlist[buf][sl]] - s.local0);
           cp_async4(&Fst[sl * kTile + m], static_cast<const unsigned *>(s.F) + off);
           if (PRED) cp_async4(&Fpst[sl * kTile + m], s.Fp + off);
         }
       }
-      cp_async_commit();
     }
+    // Only the steps k whose B row has a finite entry in this tile and whose
+    // A column has one in this strip can change an output (any other
+    // candidate is at least "unreached", which never wins).
+    unsigned long long mlo = (unsigned long long)(s_kmask[buf][0] & s_amask[0]) |
+                             ((unsigned long long)(s_kmask[buf][1] & s_amask[1]) << 32);
+    unsigned long long mhi = (unsigned long long)(s_kmask[buf][2] & s_amask[2]) |
+                             ((unsigned long long)(s_kmask[buf][3] & s_amask[3]) << 32);
+    const int nact = __popcll(mlo) + __popcll(mhi);
+    n_tiles++;
+    n_empty += nact == 0;
+    n_steps += nact;
+    if (PRED && nact > 0) load_bp_rows(jt * TN, mlo, mhi);
+    cp_async_commit();
+    if (jt + 1 < jt1)  // B[buf ^ 1] was last read by the previous tile's add-mins, before (B)
+      strip_load_rows<TN>(Bs + (buf ^ 1) * ks * TN, static_cast<const unsigned *>(s.B), s.ldb, s.K,
+                          s.N, kseg, (jt + 1) * TN, vec_b, INF);
+    cp_async_commit();
 
     unsigned acc[8][4 * CH];
 #pragma unroll
     for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 4 * CH; c++) acc[r][c] = kPackH << kIdxBits;
-    // Only the steps k whose B row has a finite entry in this tile and whose
-    // A column has one in this strip can change an output (any other
-    // candidate is at least "unreached", which never wins).  When every row has one the loop runs over all k (unrolled);
-    // otherwise it walks the set bits of the tile's row mask -- on graphs
-    // with limited reachability most rows are skipped.  Either way the next
-    // step's operands load while the current step's add-mins issue.
+    // When every step is active the loop runs over all k (unrolled);
+    // otherwise it walks the set bits of the mask -- on graphs with limited
+    // reachability most steps are skipped.  Either way the next step's
+    // operands load while the current step's add-mins issue.
     {
       const unsigned *acol = As + ty * 4;
       const unsigned *bcol = Bcur + tx * 4;
-      unsigned long long mlo = (unsigned long long)(s_kmask[buf][0] & s_amask[0]) |
-                               ((unsigned long long)(s_kmask[buf][1] & s_amask[1]) << 32);
-      unsigned long long mhi = (unsigned long long)(s_kmask[buf][2] & s_amask[2]) |
-                               ((unsigned long long)(s_kmask[buf][3] & s_amask[3]) << 32);
-      const int nact = __popcll(mlo) + __popcll(mhi);
-      if (threadIdx.x == 0) {
-        atomicAdd(&g_strip_counters[0], 1ull);
-        if (nact == 0) atomicAdd(&g_strip_counters[1], 1ull);
-        atomicAdd(&g_strip_counters[2], (unsigned long long)nact);
-      }
       if (nact == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
         uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
@@ -802,10 +840,8 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
       }
     }
 
-    if (nown > 0) {  // staged FW values visible to every thread
-      cp_async_wait_0();
-      __syncthreads();
-    }
+    cp_async_wait_1();
+    __syncthreads();  // (B)
     // Epilogue: distances, predecessors from the staged rows, own-part
     // columns from the part's Floyd-Warshall matrix (only when the tile has
     // any; the test is uniform over the CTA).
@@ -814,7 +850,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     if (nown > 0) {
 #pragma unroll
       for (int c = 0; c < 4 * CH; c++)
-        if (ownidx[(c >> 2) * kBlk + tx * 4 + (c & 3)] != -1) ownmask |= 1u << c;
+        if (ownidx[buf * TN + (c >> 2) * kBlk + tx * 4 + (c & 3)] != -1) ownmask |= 1u << c;
     }
 #pragma unroll
     for (int r = 0; r < 8; r++) {
@@ -846,12 +882,12 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
 #pragma unroll
           for (int q = 0; q < 4; q++) {
             if (!((ownmask >> (h * 4 + q)) & 1u)) continue;
-            const int oi = ownidx[sc0 + q];
+            const int oi = ownidx[buf * TN + sc0 + q];
             if (oi >= 0) {  // own-part column: the FW value, staged
               d[q] = Fst[oi * kTile + row - row0];
               if (PRED) p[q] = Fpst[oi * kTile + row - row0];
             } else if (oi == -2) {  // own-part column beyond the staging slots
-              const int64_t fj = coll[sc0 + q] - s.local0;
+              const int64_t fj = coll[buf * TN + sc0 + q] - s.local0;
               d[q] = static_cast<const unsigned *>(s.F)[(int64_t)row * s.ldf + fj];
               if (PRED) p[q] = s.Fp[(int64_t)row * s.ldf + fj];
             }
@@ -870,11 +906,13 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
         }
       }
     }
-    __syncthreads();  // B[buf], Bp and the column flags are free again
-    if (jt + 1 < jt1) load_side((jt + 1) * TN);
-    cp_async_commit();
   }
   cp_async_wait_0();
+  if (threadIdx.x == 0 && n_tiles > 0) {
+    atomicAdd(&g_strip_counters[0], n_tiles);
+    atomicAdd(&g_strip_counters[1], n_empty);
+    atomicAdd(&g_strip_counters[2], n_steps);
+  }
 }
 
 // Strip form of the accumulating packed product of the Floyd-Warshall
