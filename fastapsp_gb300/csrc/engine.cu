@@ -125,11 +125,14 @@ struct Plan {
     // min-plus
     const MpSegment *mp = nullptr;
     int mp_nseg = 0, mp_tiles = 0;
-    // strip form: the first mp_strip_nseg segments (two CTAs per SM), then
-    // mp_large_nseg with a larger K (one CTA per SM); mp_strip_tiles = tiles of
-    // both in the tile numbering, which the tile form's launch skips
-    int mp_strip_nseg = 0, mp_strip_tiles = 0, mp_strips = 0, mp_max_k = 0;
-    int mp_large_nseg = 0, mp_large_strips = 0, mp_large_max_k = 0;
+    // strip form: class c (K up to fapk::minplus_strip_class_k(c)) holds
+    // mp_cls_nseg[c] segments from mp_cls_first[c], one launch each with CTAs
+    // numbered from 0; mp_strip_tiles = tiles of all of them in the tile
+    // numbering, which the tile form's launch skips
+    static constexpr int kMaxCls = 4;
+    int mp_ncls = 0, mp_strip_tiles = 0;
+    int mp_cls_first[kMaxCls] = {}, mp_cls_nseg[kMaxCls] = {};
+    int mp_cls_strips[kMaxCls] = {}, mp_cls_max_k[kMaxCls] = {};
     int max_sub = 0;  // largest part of the group (bound of the packed form)
   };
   std::vector<Group> groups;
@@ -379,9 +382,10 @@ int build_plan(fap_engine *e, Plan &pl) {
     std::vector<SsspBatch> batches;
     std::vector<PartDesc> pdesc;
     std::vector<int64_t> row_begin(1, 0), dec_begin(1, 0);
-    // min-plus segments: those the strip form can take (K <= its limit)
-    // first, then the rest; tiles are numbered over all of them
-    std::vector<MpSegment> mps, mps_large, mps_wide;
+    // min-plus segments: the strip form's classes of K in order, then those
+    // above its limit; tiles are numbered over all of them
+    std::vector<MpSegment> mps_cls[Plan::Group::kMaxCls], mps_wide;
+    const int ncls = std::min(fapk::minplus_strip_classes(), (int)Plan::Group::kMaxCls);
     int maxnb = 0;
     for (int idx : groups[g]) {
       int p = pl.parts[idx];
@@ -431,8 +435,9 @@ int build_plan(fap_engine *e, Plan &pl) {
         s.Fp = pred ? fwp + mat_off[idx] + (int64_t)bdy * d.ld : nullptr;
         s.ldf = d.ld;
         pl.max_mp_k = std::max(pl.max_mp_k, bdy);
-        if (bdy <= fapk::minplus_strip_pair_k()) mps.push_back(s);
-        else if (bdy <= fapk::minplus_strip_max_k()) mps_large.push_back(s);
+        int c = 0;
+        while (c < ncls && bdy > fapk::minplus_strip_class_k(c)) c++;
+        if (c < ncls) mps_cls[c].push_back(s);
         else mps_wide.push_back(s);
       }
     }
@@ -444,22 +449,21 @@ int build_plan(fap_engine *e, Plan &pl) {
     O.pdesc = tb.add(pdesc.data(), pdesc.size());
     O.row_begin = tb.add(row_begin.data(), row_begin.size());
     O.dec_begin = tb.add(dec_begin.data(), dec_begin.size());
-    int mp_tiles = 0, mp_strips = 0, mp_max_k = 0, lg_strips = 0, lg_max_k = 0;
-    for (MpSegment &s : mps) {
-      s.strip_begin = mp_strips;
-      mp_strips += mp_strips_of(s);
-      mp_max_k = std::max(mp_max_k, s.K);
+    std::vector<MpSegment> mps;
+    G.mp_ncls = ncls;
+    for (int c = 0; c < ncls; c++) {
+      G.mp_cls_first[c] = (int)mps.size();
+      G.mp_cls_nseg[c] = (int)mps_cls[c].size();
+      for (MpSegment &s : mps_cls[c]) {
+        s.strip_begin = G.mp_cls_strips[c];
+        G.mp_cls_strips[c] += mp_strips_of(s);
+        G.mp_cls_max_k[c] = std::max(G.mp_cls_max_k[c], s.K);
+      }
+      mps.insert(mps.end(), mps_cls[c].begin(), mps_cls[c].end());
     }
-    for (MpSegment &s : mps_large) {
-      s.strip_begin = lg_strips;
-      lg_strips += mp_strips_of(s);
-      lg_max_k = std::max(lg_max_k, s.K);
-    }
-    G.mp_strip_nseg = (int)mps.size();
-    G.mp_large_nseg = (int)mps_large.size();
-    mps.insert(mps.end(), mps_large.begin(), mps_large.end());
+    const int nstrip = (int)mps.size();
     mps.insert(mps.end(), mps_wide.begin(), mps_wide.end());
-    const int nstrip = G.mp_strip_nseg + G.mp_large_nseg;
+    int mp_tiles = 0;
     for (MpSegment &s : mps) {
       s.tile_begin = mp_tiles;
       mp_tiles += mp_tiles_of(s);
@@ -467,10 +471,6 @@ int build_plan(fap_engine *e, Plan &pl) {
     }
     G.mp_nseg = (int)mps.size();
     G.mp_tiles = mp_tiles;
-    G.mp_strips = mp_strips;
-    G.mp_max_k = mp_max_k;
-    G.mp_large_strips = lg_strips;
-    G.mp_large_max_k = lg_max_k;
     O.mp = tb.add(mps.data(), mps.size());
     // FW rounds
     G.diag_cnt.assign(maxnb, 0);
@@ -637,9 +637,9 @@ struct Issuer {
     }
     if (last) FAP_CUDA(rec(3));
     if (packed) {  // strip form for the small-K segments, tiles for the rest
-      FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp, G.mp_strip_nseg, G.mp_strips, G.mp_max_k, st));
-      FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp + G.mp_strip_nseg, G.mp_large_nseg,
-                                           G.mp_large_strips, G.mp_large_max_k, st));
+      for (int c = 0; c < G.mp_ncls; c++)
+        FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
+                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles - G.mp_strip_tiles,
                                           packed, st, G.mp_strip_tiles));
     } else {

@@ -34,7 +34,11 @@ cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int s
                              cudaStream_t st);
 int fw_strip_tiles();
 int minplus_strip_max_k();   // largest K of the strip form
-int minplus_strip_pair_k();  // largest K at which it runs two CTAs per SM
+// Segments go to the strip form in classes of K (one launch per class, each
+// with its own CTAs per SM): class c takes K <= minplus_strip_class_k(c)
+// above the previous bound; -1 past the last class.
+int minplus_strip_classes();
+int minplus_strip_class_k(int c);
 // Largest finite int32 entry of the matrices, atomicMax-ed into *out.
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st);
 unsigned pack_limit();

@@ -506,32 +506,41 @@ __global__ void __launch_bounds__(kThreads, 2)
 
 // Strip form of the packed min-plus for products that do not accumulate into
 // C (the inner rows of every part) with K <= kStripMaxK.  One CTA owns a
-// strip: one 128-row tile of a segment and up to kStripTiles consecutive
-// 128-column tiles, two CTAs per SM (one when K > kStripPairK, whose shared
-// memory is larger).  A's 128 x K block is staged once per
-// strip (transposed, so that a thread's 8 row operands of one k are two
-// 16-byte loads); B's K x 128 tiles are double-buffered, so the next tile's
+// strip: one 128-row tile of a segment and the TN-column tiles of
+// kStripTiles x 128 consecutive columns.  A's 128 x K block is staged once
+// per strip (transposed, so that a thread's 8 row operands of one k are two
+// 16-byte loads); B's K x TN tiles are double-buffered, so the next tile's
 // copy is in flight while the current one is multiplied; B's predecessor
-// rows and the own-part column flags of the next tile are staged right after
-// each epilogue, behind the next tile's DPX loop.  The part's own columns of
-// a tile (the Floyd-Warshall values replace the product there) are listed
-// when the tile's column flags land, and the FW values of up to kOwnCap of
-// them are staged with cp.async behind the DPX loop; further own columns are
-// read from global memory in the epilogue.  The descriptor search, the
-// staging of A and the pipeline fill of the tile kernel are paid once per
-// strip instead of once per tile.  Shared memory (ks = K rounded up to 4):
-//   B[2][ks][128] | Bp[1 + ks][128] | colp[128] | coll[128] | ownidx[128] |
+// rows of the tile's active steps, its own-part FW values and the next
+// tile's column flags are copied behind the DPX loop.  The part's own
+// columns of a tile (the Floyd-Warshall values replace the product there)
+// are listed when the tile's column flags land, and the FW values of up to
+// kOwnCap of them are staged; further own columns are read from global
+// memory in the epilogue.  The descriptor search, the staging of A and the
+// pipeline fill of the tile kernel are paid once per strip instead of once
+// per tile.  Shared memory (ks = K rounded up to 4):
+//   B[2][ks][TN] | Bp[1 + ks][TN] | colp[2][TN] | coll[2][TN] | ownidx[2][TN] |
 //   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
 // Work counters of the strip min-plus (diagnostics): [tiles, tiles with no
-// active step, active steps summed over tiles].  One atomic per tile.
+// active step, active steps summed over tiles], summed per CTA.
 __device__ unsigned long long g_strip_counters[3];
 
-constexpr int kStripTiles = 16;  // 128-column tiles per strip
-constexpr int kStripPairK = 48;   // largest K with two CTAs per SM
-constexpr int kStripMaxK = 100;   // largest K of the strip form (one CTA per SM above kStripPairK)
+constexpr int kStripTiles = 16;  // a strip spans kStripTiles x 128 columns
+constexpr int kStripMaxK = 100;  // largest K of the strip form
 constexpr int kOwnCap = 12;
+// Column tile of the form used: 128 x 64 tiles with 8 x 4 outputs a thread.
+// On sparse products most of a tile's time is its fixed work (B keys, masks,
+// epilogue), whose latencies only more resident warps hide; against 128 x
+// 128 tiles at two CTAs per SM it measured 16 % faster on a 65,536-vertex
+// geometric graph and within a few percent on dense products.
+constexpr int kStripTN = 64;
+// Segments are launched in classes of K, each with the CTAs per SM that its
+// shared memory allows: K <= 48 three, up to kStripMaxK one or two.  (Four
+// CTAs per SM for K <= 32, at 64 registers a thread, measured no faster.)
+constexpr int kStripClassK[] = {48, kStripMaxK};
+constexpr int kStripClasses = 2;
 
 // Shared memory of the strip kernel with TN-column tiles, in bytes.
 template <int TN>
@@ -599,10 +608,9 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
   }
 }
 
-// TN = 128: 128x128 tiles, 8x8 outputs per thread, two CTAs per SM (the form
-// used).  TN = 64 (128x64 tiles, 8x4 outputs per thread, three CTAs per SM)
-// measured within 1-4 % of it on this GPU, so occupancy is not what bounds
-// the kernel.  A strip always spans kStripTiles x 128 columns.
+// TN = 64 (kStripTN, the form used): 128x64 tiles, 8x4 outputs per thread,
+// three CTAs per SM.  TN = 128: 128x128 tiles, 8x8 outputs per thread, two
+// CTAs per SM.
 template <bool PRED, int TN>
 __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     mp_strip_kernel(const MpSegment *__restrict__ segs, int nseg, int ks) {
@@ -1520,8 +1528,8 @@ cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, 
                                   int max_k, cudaStream_t st) {
   if (max_k < 0 || max_k > kStripMaxK) return cudaErrorInvalidValue;
   const int ks = (max_k + 3) & ~3;
-  return pred ? launch_strip_t<true, 128>(d_segs, nseg, strips, ks, st)
-              : launch_strip_t<false, 128>(d_segs, nseg, strips, ks, st);
+  return pred ? launch_strip_t<true, kStripTN>(d_segs, nseg, strips, ks, st)
+              : launch_strip_t<false, kStripTN>(d_segs, nseg, strips, ks, st);
 }
 
 int minplus_strip_tiles() { return kStripTiles; }
@@ -1533,7 +1541,8 @@ cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int s
 }
 int fw_strip_tiles() { return kFwStripTiles; }
 int minplus_strip_max_k() { return kStripMaxK; }
-int minplus_strip_pair_k() { return kStripPairK; }
+int minplus_strip_classes() { return kStripClasses; }
+int minplus_strip_class_k(int c) { return c >= 0 && c < kStripClasses ? kStripClassK[c] : -1; }
 
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st) {
   if (nmats <= 0) return cudaSuccess;
@@ -1581,12 +1590,12 @@ cudaError_t init_minplus_kernels() {
   if ((e = set_mp_attr<uint32_t, false>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<true>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<false>()) != cudaSuccess) return e;
-  const int smax = (int)strip_smem_bytes<128>((kStripMaxK + 3) & ~3);
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                smax)) != cudaSuccess)
+  const int smax = (int)strip_smem_bytes<kStripTN>((kStripMaxK + 3) & ~3);
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, kStripTN>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                smax)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, kStripTN>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax)) != cudaSuccess)
     return e;
 
   if ((e = cudaFuncSetAttribute(fw_pivot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -38,7 +38,8 @@ def as_oracle(a):
 @pytest.mark.parametrize("f32", [False, True])
 @pytest.mark.parametrize("M,N,K", [(1, 1, 1), (31, 33, 7), (64, 64, 64), (65, 129, 33), (200, 300, 130),
                                    (130, 70, 0), (5, 1000, 257), (300, 2100, 29), (129, 2053, 48),
-                                   (257, 4100, 49), (150, 700, 100), (70, 300, 101)])
+                                   (257, 4100, 49), (150, 700, 100), (70, 300, 101), (200, 2200, 32),
+                                   (131, 1100, 33)])
 def test_minplus_matches_oracle(ctx, oracle_lib, f32, M, N, K):
     rng = np.random.default_rng(M * 1000 + N * 10 + K)
     A = rand_dist(rng, (M, K), 0.2, f32)
