@@ -925,21 +925,27 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
 
 // Strip form of the accumulating packed product of the Floyd-Warshall
 // remaining-tile phase: D_ij = min(D_ij, D_ir (x) D_rj) with K <= 64 (one
-// pivot block), ties keeping D_ij.  One CTA per SM (197 KB of shared memory)
-// owns a strip: one row tile of the segment's row list (A = D_ir resident)
-// and up to kFwStripTiles column tiles of its column list.  Everything a tile
-// needs is in flight before it is needed: B (= D_rj) double-buffered, the
-// current tile's C staged behind its DPX loop, B's predecessors staged behind
-// the next tile's loop.  The product starts from "unreached" and C joins in
-// the epilogue with index 0, which gives the same minimum and tie rule as
+// pivot block), ties keeping D_ij.  A CTA owns a strip: one 128-row tile of
+// the segment's row list (A = D_ir resident) and the column tiles of up to
+// kFwStripTiles block pairs of its column list.  Everything a tile needs is
+// in flight before it is needed: B (= D_rj) double-buffered, the current
+// tile's C staged behind its DPX loop, B's predecessors staged behind the
+// next tile's loop.  The product starts from "unreached" and C joins in the
+// epilogue with index 0, which gives the same minimum and tie rule as
 // starting from C.
-constexpr int kFwStripTiles = 4;
+constexpr int kFwStripTiles = 4;  // block pairs (128 columns) per strip
+// Column tile of the form used: one 64-column block (128 x 64 tiles, 8 x 4
+// outputs a thread, 112 KB of shared memory, two CTAs per SM, so that one
+// CTA's epilogue overlaps the other's add-mins).  TN = 128 (block pairs,
+// 197 KB, one CTA per SM) is the other form.
+constexpr int kFwStripTN = 64;
 
+template <int TN>
 struct FwStripSmem {
-  unsigned A[kBlk][kTile];       // A keys, transposed: pivot block x strip rows
-  unsigned B[2][kBlk][kTile];    // B keys of the current / next tile
-  int32_t Bp[kBlk][kTile];       // B's predecessors of the current tile
-  unsigned C[kTile][kTile];      // C of the current tile
+  unsigned A[kBlk][kTile];     // A keys, transposed: pivot block x strip rows
+  unsigned B[2][kBlk][TN];     // B keys of the current / next tile
+  int32_t Bp[kBlk][TN];        // B's predecessors of the current tile
+  unsigned C[kTile][TN];       // C of the current tile
 };
 
 __device__ __forceinline__ int fw_strips_x(const MpSegment &s) {
@@ -947,17 +953,19 @@ __device__ __forceinline__ int fw_strips_x(const MpSegment &s) {
 }
 
 // Copies rows [0, 64) of B-like data (row k at src + k * ld, columns of the
-// two 64-column blocks starting at cbase.x / cbase.y, -1 for none) into
-// dst[64][128]; 16-byte copies of 4 columns where aligned, `fill` outside the
+// tile's 64-column blocks starting at cbase.x / cbase.y, -1 for none) into
+// dst[64][TN]; 16-byte copies of 4 columns where aligned, `fill` outside the
 // matrix.
+template <int TN>
 __device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, int64_t ld, int K,
                                           int N, int2 cbase, bool vec, unsigned fill) {
+  constexpr int TPR = TN / 4;  // threads per row
   const int t = threadIdx.x;
-  const int j = (t & 31) * 4;
+  const int j = (t % TPR) * 4;
   const int cb = (j >> 6) ? cbase.y : cbase.x;
   const int col = cb + (j & 63);
-  for (int kk = t >> 5; kk < kBlk; kk += kThreads / 32) {
-    unsigned *d = dst + kk * kTile + j;
+  for (int kk = t / TPR; kk < kBlk; kk += kThreads / TPR) {
+    unsigned *d = dst + kk * TN + j;
     const unsigned *g = src + (int64_t)kk * ld + col;
     if (cb >= 0 && kk < K && vec && col + 3 < N) {
       cp_async16(d, g);
@@ -971,11 +979,13 @@ __device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, in
   }
 }
 
-template <bool PRED>
-__global__ void __launch_bounds__(kThreads, 1)
+template <bool PRED, int TN>
+__global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     mp_fwstrip_kernel(const MpSegment *__restrict__ segs, int nseg) {
+  constexpr int CH = TN / 64;   // 64-column blocks of a tile
+  constexpr int TPR = TN / 4;   // threads per row in the row-wise copies
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  FwStripSmem &sm = *reinterpret_cast<FwStripSmem *>(smem_raw);
+  FwStripSmem<TN> &sm = *reinterpret_cast<FwStripSmem<TN> *>(smem_raw);
   __shared__ MpSegment seg;
   __shared__ unsigned s_kmask[2][2];  // rows k of B with a finite entry (per tile parity)
   __shared__ unsigned s_amask[2];     // columns k of A with a finite entry (per strip)
@@ -987,15 +997,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int sx = fw_strips_x(s);
   const int local = blockIdx.x - s.strip_begin;
   const int tyt = local / sx;
-  const int jt0 = (local - tyt * sx) * kFwStripTiles;
-  const int jt1 = min(jt0 + kFwStripTiles, s.tiles_x);
   const int nbr = (s.M + kBlk - 1) / kBlk, nbc = (s.N + kBlk - 1) / kBlk;
+  // column list length, in blocks, and this strip's column tiles of CH blocks
+  const int ncb = s.col_fix >= 0 ? 1 : nbc - ((s.col_skip >= 0 && s.col_skip < nbc) ? 1 : 0);
+  const int jt0 = (local - tyt * sx) * kFwStripTiles * (2 / CH);
+  const int jt1 = min(jt0 + kFwStripTiles * (2 / CH), (ncb + CH - 1) / CH);
   const int rl0 = list_block(2 * tyt, s.row_skip, s.row_fix, nbr);
   const int rl1 = list_block(2 * tyt + 1, s.row_skip, s.row_fix, nbr);
   const int rbase0 = rl0 >= 0 ? rl0 * kBlk : -1, rbase1 = rl1 >= 0 ? rl1 * kBlk : -1;
-  auto col_bases = [&](int jt) {  // first columns of the tile's two blocks (-1: none)
-    const int b0 = list_block(2 * jt, s.col_skip, s.col_fix, nbc);
-    const int b1 = list_block(2 * jt + 1, s.col_skip, s.col_fix, nbc);
+  auto col_bases = [&](int jt) {  // first columns of the tile's blocks (-1: none)
+    const int b0 = list_block(CH * jt, s.col_skip, s.col_fix, nbc);
+    const int b1 = CH == 2 ? list_block(CH * jt + 1, s.col_skip, s.col_fix, nbc) : -1;
     return make_int2(b0 >= 0 ? b0 * kBlk : -1, b1 >= 0 ? b1 * kBlk : -1);
   };
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
@@ -1017,18 +1029,18 @@ __global__ void __launch_bounds__(kThreads, 1)
       *d = INF;
   }
   int2 cb = col_bases(jt0);
-  fw_load_b(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
+  fw_load_b<TN>(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
   cp_async_commit();
   if (PRED)
-    fw_load_b(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
-              s.ldbp, s.K, s.N, cb, vec_bp, 0xffffffffu);
+    fw_load_b<TN>(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
+                  s.ldbp, s.K, s.N, cb, vec_bp, 0xffffffffu);
   cp_async_commit();
 
   for (int jt = jt0; jt < jt1; jt++) {
     const int buf = (jt - jt0) & 1;
     cb = col_bases(jt);
     if (jt + 1 < jt1)
-      fw_load_b(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
+      fw_load_b<TN>(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
                 col_bases(jt + 1), vec_b, INF);
     cp_async_commit();
     cp_async_wait_1();  // A, this tile's B and its predecessors have landed
@@ -1040,9 +1052,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (__any_sync(0xffffffffu, v < kPackH) && (threadIdx.x & 31) == 0)
           atomicOr(&s_amask[kk >> 5], 1u << (kk & 31));
       }
-    {  // B keys; a warp converts whole rows and marks those with a finite entry
-      const int j = (threadIdx.x & 31) * 4;
-      for (int kk = threadIdx.x >> 5; kk < kBlk; kk += kThreads / 32) {
+    {  // B keys; TPR lanes convert a whole row and its first lane marks it when finite
+      const int j = (threadIdx.x % TPR) * 4;
+      const int lane = threadIdx.x & 31;
+      for (int kk = threadIdx.x / TPR; kk < kBlk; kk += kThreads / TPR) {
         uint4 *p = reinterpret_cast<uint4 *>(&sm.B[buf][kk][j]);
         const unsigned idx = (unsigned)kk + 1u;
         uint4 v = *p;
@@ -1052,7 +1065,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         v.z = (min(v.z, kPackH) << kIdxBits) | idx;
         v.w = (min(v.w, kPackH) << kIdxBits) | idx;
         *p = v;
-        if (__any_sync(0xffffffffu, fin) && (threadIdx.x & 31) == 0)
+        const unsigned bal = __ballot_sync(0xffffffffu, fin);  // every lane runs the same trips
+        const unsigned grp = TPR == 32 ? 0xffffffffu : ((1u << (TPR & 31)) - 1u);
+        if (lane % TPR == 0 && ((bal >> lane) & grp) != 0u)
           atomicOr(&s_kmask[buf][kk >> 5], 1u << (kk & 31));
       }
       if (threadIdx.x < 2) s_kmask[buf ^ 1][threadIdx.x] = 0u;  // for the next tile
@@ -1060,10 +1075,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     // Stage this tile's C behind the DPX loop.
     {
-      const int j = (threadIdx.x & 31) * 4;
+      const int j = (threadIdx.x % TPR) * 4;
       const int cbj = (j >> 6) ? cb.y : cb.x;
       const int col = cbj + (j & 63);
-      for (int m = threadIdx.x >> 5; m < kTile; m += kThreads / 32) {
+      for (int m = threadIdx.x / TPR; m < kTile; m += kThreads / TPR) {
         const int rb = (m >> 6) ? rbase1 : rbase0;
         const int row = rb + (m & 63);
         unsigned *d = &sm.C[m][j];
@@ -1081,11 +1096,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       cp_async_commit();
     }
 
-    unsigned acc[8][8];
+    unsigned acc[8][4 * CH];
 #pragma unroll
     for (int r = 0; r < 8; r++)
 #pragma unroll
-      for (int c = 0; c < 8; c++) acc[r][c] = kPackH << kIdxBits;
+      for (int c = 0; c < 4 * CH; c++) acc[r][c] = kPackH << kIdxBits;
     // Only steps k whose B row (pivot row k over this tile's columns) and A
     // column (over this strip's rows) have a finite entry can improve an
     // output: all k (unrolled) when every row
@@ -1101,42 +1116,42 @@ __global__ void __launch_bounds__(kThreads, 1)
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
         uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
         uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
-        uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kBlk);
+        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kBlk) : nb0;
 #pragma unroll 2
         for (int kk = 0; kk < kseg; kk++) {
           const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
           const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
-          const int kn = (kk + 1 < kseg ? kk + 1 : kk) * kTile;
-          na0 = *reinterpret_cast<const uint4 *>(acol + kn);
-          na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
-          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
-          nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
+          const int kn = kk + 1 < kseg ? kk + 1 : kk;
+          na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
+          na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
+          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
 #pragma unroll
           for (int r = 0; r < 8; r++)
 #pragma unroll
-            for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+            for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
         }
       } else if (msk) {
         int kk = __ffsll(msk) - 1;
         msk &= msk - 1ull;
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol + kk * kTile);
         uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kk * kTile + kBlk);
-        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile);
-        uint4 nb1 = *reinterpret_cast<const uint4 *>(bcol + kk * kTile + kBlk);
+        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * TN);
+        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kk * TN + kBlk) : nb0;
         while (kk >= 0) {
           const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
           const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
           kk = msk ? __ffsll(msk) - 1 : -1;
           if (msk) msk &= msk - 1ull;
-          const int kn = (kk >= 0 ? kk : 0) * kTile;
-          na0 = *reinterpret_cast<const uint4 *>(acol + kn);
-          na1 = *reinterpret_cast<const uint4 *>(acol + kn + kBlk);
-          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn);
-          nb1 = *reinterpret_cast<const uint4 *>(bcol + kn + kBlk);
+          const int kn = kk >= 0 ? kk : 0;
+          na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
+          na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
+          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
 #pragma unroll
           for (int r = 0; r < 8; r++)
 #pragma unroll
-            for (int c = 0; c < 8; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+            for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
         }
       }
     }
@@ -1151,7 +1166,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int row = rb + ty * 4 + (r & 3);
       if (rb < 0 || row >= s.M) continue;
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
+      for (int h = 0; h < CH; h++) {
         const int cbh = h ? cb.y : cb.x;
         if (cbh < 0) continue;
         const int sc0 = h * kBlk + tx * 4;
@@ -1170,7 +1185,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();  // C, B[buf] and the predecessors are free again
     if (PRED && jt + 1 < jt1)
-      fw_load_b(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
+      fw_load_b<TN>(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
                 s.ldbp, s.K, s.N, col_bases(jt + 1), vec_bp, 0xffffffffu);
     cp_async_commit();
   }
@@ -1496,7 +1511,8 @@ template <bool PRED>
 cudaError_t launch_fwstrip_t(const MpSegment *d_segs, int nseg, int strips, cudaStream_t st) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
   ++launch_count();
-  mp_fwstrip_kernel<PRED><<<strips, kThreads, sizeof(FwStripSmem), st>>>(d_segs, nseg);
+  mp_fwstrip_kernel<PRED, kFwStripTN>
+      <<<strips, kThreads, sizeof(FwStripSmem<kFwStripTN>), st>>>(d_segs, nseg);
   return cudaGetLastError();
 }
 
@@ -1604,11 +1620,13 @@ cudaError_t init_minplus_kernels() {
   if ((e = cudaFuncSetAttribute(fw_pivot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(PivotSmem))) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_fwstrip_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sizeof(FwStripSmem))) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(mp_fwstrip_kernel<true, kFwStripTN>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(FwStripSmem<kFwStripTN>))) != cudaSuccess)
     return e;
-  return cudaFuncSetAttribute(mp_fwstrip_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sizeof(FwStripSmem));
+  return cudaFuncSetAttribute(mp_fwstrip_kernel<false, kFwStripTN>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(FwStripSmem<kFwStripTN>));
 }
 
 int minplus_tile_rows() { return kTile; }
