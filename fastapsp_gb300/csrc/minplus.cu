@@ -1345,34 +1345,34 @@ __global__ void __launch_bounds__(256)
 // D_rb = min(D_rb, D_rr (x) D_rb) and those of the second half the column
 // panel D_br = min(D_br, D_br (x) D_rr), each taking every (kPivotCtas/2)-th
 // block: 64x64 outputs, 4x4 per thread, packed keys, the block's own values
-// joining with index 0.  One launch replaces the diagonal launch and the
-// panel launch of the tile kernel (whose 128x128 tiles were half empty for
-// 64-wide panels).
+// joining with index 0.  The panel blocks are a pipeline: the first one's
+// copy is issued before the closure (it lands while CTA 0 closes and the
+// others wait), each next block's values are copied behind the current
+// block's add-mins, and (row panel) its predecessors behind the current
+// block's epilogue.  One launch replaces the diagonal launch and the panel
+// launch of the tile kernel (whose 128x128 tiles were half empty for 64-wide
+// panels).
 constexpr int kPivotCtas = 4;
 
 struct PivotSmem {
   unsigned D[kBlk][kBlk + 1];  // pivot block values (closure)
   int32_t P[kBlk][kBlk + 1];   // and predecessors
   unsigned Kp[kBlk][kBlk];     // pivot keys: A^T (row panel) or B (column panel)
-  unsigned Xv[kBlk][kBlk];     // the current panel block's values
-  int32_t Xp[kBlk][kBlk];      // and predecessors
-  unsigned Kx[kBlk][kBlk];     // its keys: B (row panel) or A^T (column panel)
+  unsigned Xv[kBlk][kBlk];     // the next panel block's values (copy in flight)
+  int32_t Xp[kBlk][kBlk];      // the current block's predecessors (row panel)
+  unsigned Kx[kBlk][kBlk];     // the current block's keys: B (row panel) or A^T (column panel)
 };
 
-template <bool PRED>
-__device__ __forceinline__ void pivot_load_block(PivotSmem &sm, const FwDiagJob &job, int rb,
-                                                 int cb) {
-  const unsigned *Dg = static_cast<const unsigned *>(job.D);
+// Copies the 64x64 block (rb, cb) of a job's matrix (values, or predecessors
+// when P) into dst[64][64], "unreached" / -1 outside the matrix.
+template <bool P>
+__device__ __forceinline__ void pivot_load_block(unsigned *dst, const FwDiagJob &job, int rb, int cb) {
+  const unsigned *src = P ? reinterpret_cast<const unsigned *>(job.P) : static_cast<const unsigned *>(job.D);
   for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
     const int i = idx >> 6, j = idx & 63;
     const int gi = rb * kBlk + i, gj = cb * kBlk + j;
-    if (gi < job.size && gj < job.size) {
-      cp_async4(&sm.Xv[i][j], Dg + (int64_t)gi * job.ld + gj);
-      if (PRED) cp_async4(&sm.Xp[i][j], job.P + (int64_t)gi * job.ld + gj);
-    } else {
-      sm.Xv[i][j] = Dist<uint32_t>::inf();
-      if (PRED) sm.Xp[i][j] = -1;
-    }
+    if (gi < job.size && gj < job.size) cp_async4(&dst[idx], src + (int64_t)gi * job.ld + gj);
+    else dst[idx] = P ? 0xffffffffu : Dist<uint32_t>::inf();
   }
 }
 
@@ -1386,12 +1386,27 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
   const int rank = (int)cluster.block_rank();
   const int role = rank / (kPivotCtas / 2);  // 0: row panel, 1: column panel
   const int sub = rank % (kPivotCtas / 2);   // which of the panel's blocks
+  constexpr int kStride = kPivotCtas / 2;
   const FwDiagJob job = jobs[blockIdx.x / kPivotCtas];
   const int r = job.block;
   const int nb = (job.size + kBlk - 1) / kBlk;
   const int npanel = nb - 1;
   const unsigned INF = Dist<uint32_t>::inf();
   auto panel_block = [&](int i) { return i < r ? i : i + 1; };  // i-th block other than r
+  auto load_values = [&](int pi) {  // panel block pi's values -> Xv
+    const int b = panel_block(pi);
+    if (role == 0) pivot_load_block<false>(&sm.Xv[0][0], job, r, b);
+    else pivot_load_block<false>(&sm.Xv[0][0], job, b, r);
+  };
+  auto load_preds = [&](int pi) {  // row panel: block pi's predecessors -> Xp
+    if (PRED && role == 0)
+      pivot_load_block<true>(reinterpret_cast<unsigned *>(&sm.Xp[0][0]), job, r, panel_block(pi));
+  };
+  // The first panel block's copy lands during the closure.
+  if (sub < npanel) load_values(sub);
+  cp_async_commit();
+  if (sub < npanel) load_preds(sub);
+  cp_async_commit();
 
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
   if (rank == 0) {
@@ -1431,20 +1446,39 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
     else sm.Kp[i][j] = (min(sm.D[i][j], kPackH) << kIdxBits) | (unsigned)(i + 1);  // B, idx k + 1
   }
 
-  for (int pi = sub; pi < npanel; pi += kPivotCtas / 2) {
+  for (int pi = sub; pi < npanel; pi += kStride) {
     const int b = panel_block(pi);
-    if (role == 0) pivot_load_block<PRED>(sm, job, r, b);
-    else pivot_load_block<PRED>(sm, job, b, r);
-    cp_async_commit();
-    cp_async_wait_0();
-    __syncthreads();  // this block landed for every thread (and Kp is built)
-    for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
-      const int i = idx >> 6, j = idx & 63;
-      const unsigned v = min(sm.Xv[i][j], kPackH) << kIdxBits;
-      if (role == 0) sm.Kx[i][j] = v | (unsigned)(i + 1);  // B = the panel block, row k = i
-      else sm.Kx[j][i] = v;                                // A^T of the panel block
+    cp_async_wait_1();  // this block's values (its predecessors may still be in flight)
+    __syncthreads();    // ... for every thread's part (and Kp, on the first trip)
+    // Keys of this block from each thread's own 4x4 outputs, whose values
+    // stay in registers for the epilogue.
+    unsigned cv[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const uint4 v = *reinterpret_cast<const uint4 *>(&sm.Xv[ty * 4 + i][tx * 4]);
+      cv[i][0] = min(v.x, kPackH);
+      cv[i][1] = min(v.y, kPackH);
+      cv[i][2] = min(v.z, kPackH);
+      cv[i][3] = min(v.w, kPackH);
     }
-    __syncthreads();
+    if (role == 0) {  // B = the block, row k carries idx k + 1
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const unsigned id = (unsigned)(ty * 4 + i + 1);
+        *reinterpret_cast<uint4 *>(&sm.Kx[ty * 4 + i][tx * 4]) =
+            make_uint4((cv[i][0] << kIdxBits) | id, (cv[i][1] << kIdxBits) | id,
+                       (cv[i][2] << kIdxBits) | id, (cv[i][3] << kIdxBits) | id);
+      }
+    } else {  // A^T of the block
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        *reinterpret_cast<uint4 *>(&sm.Kx[tx * 4 + c][ty * 4]) =
+            make_uint4(cv[0][c] << kIdxBits, cv[1][c] << kIdxBits, cv[2][c] << kIdxBits,
+                       cv[3][c] << kIdxBits);
+    }
+    __syncthreads();  // Kx complete; Xv free for the next block's copy
+    if (pi + kStride < npanel) load_values(pi + kStride);
+    cp_async_commit();
     const unsigned *Aop = role == 0 ? &sm.Kp[0][0] : &sm.Kx[0][0];
     const unsigned *Bop = role == 0 ? &sm.Kx[0][0] : &sm.Kp[0][0];
     unsigned acc[4][4];
@@ -1463,6 +1497,8 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
 #pragma unroll
         for (int c = 0; c < 4; c++) acc[i][c] = __viaddmin_u32(a[i], bb[c], acc[i][c]);
     }
+    cp_async_wait_1();  // this block's predecessors (the next block's values may be in flight)
+    __syncthreads();
     unsigned *Dg = static_cast<unsigned *>(job.D);
 #pragma unroll
     for (int i = 0; i < 4; i++) {
@@ -1472,15 +1508,18 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
       for (int c = 0; c < 4; c++) {
         const int lj = tx * 4 + c;
         const int gj = (role == 0 ? b : r) * kBlk + lj;
-        const unsigned key = min(min(sm.Xv[li][lj], kPackH) << kIdxBits, acc[i][c]);
+        const unsigned key = min(cv[i][c] << kIdxBits, acc[i][c]);
         const unsigned idx = key & kIdxMask;
         if (idx == 0 || gi >= job.size || gj >= job.size) continue;
         Dg[(int64_t)gi * job.ld + gj] = key >> kIdxBits;
         if (PRED) job.P[(int64_t)gi * job.ld + gj] = role == 0 ? sm.Xp[idx - 1][lj] : sm.P[idx - 1][lj];
       }
     }
-    __syncthreads();  // Kx and the block buffer are free again
+    __syncthreads();  // Kx and Xp are free again
+    if (pi + kStride < npanel) load_preds(pi + kStride);
+    cp_async_commit();
   }
+  cp_async_wait_0();
 }
 
 template <typename T, bool PRED>
