@@ -530,16 +530,16 @@ __device__ unsigned long long g_strip_counters[3];
 constexpr int kStripTiles = 16;  // a strip spans kStripTiles x 128 columns
 constexpr int kStripMaxK = 100;  // largest K of the strip form
 constexpr int kOwnCap = 12;
-// Column tile of the form used: 128 x 64 tiles with 8 x 4 outputs a thread.
-// On sparse products most of a tile's time is its fixed work (B keys, masks,
-// epilogue), whose latencies only more resident warps hide; against 128 x
-// 128 tiles at two CTAs per SM it measured 16 % faster on a 65,536-vertex
-// geometric graph and within a few percent on dense products.
-constexpr int kStripTN = 64;
-// Segments are launched in classes of K, each with the CTAs per SM that its
-// shared memory allows: K <= 48 three, up to kStripMaxK one or two.  (Four
-// CTAs per SM for K <= 32, at 64 registers a thread, measured no faster.)
+// Segments are launched in classes of K.  K <= 48: 128 x 64 tiles with 8 x
+// 4 outputs a thread, three CTAs per SM.  On sparse products most of a
+// tile's time is its fixed work (B keys, masks, epilogue), whose latencies
+// only more resident warps hide; against 128 x 128 tiles at two CTAs per SM
+// it measured 16 % faster on a 65,536-vertex geometric graph.  (Four CTAs per
+// SM for K <= 32, at 64 registers a thread, measured no faster.)  K <= 100:
+// 128 x 128 tiles with 8 x 8 outputs a thread (twice the add-mins per shared
+// load), one CTA per SM either way at that K.
 constexpr int kStripClassK[] = {48, kStripMaxK};
+constexpr int kStripClassTN[] = {64, 128};
 constexpr int kStripClasses = 2;
 
 // Shared memory of the strip kernel with TN-column tiles, in bytes.
@@ -608,9 +608,9 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
   }
 }
 
-// TN = 64 (kStripTN, the form used): 128x64 tiles, 8x4 outputs per thread,
-// three CTAs per SM.  TN = 128: 128x128 tiles, 8x8 outputs per thread, two
-// CTAs per SM.
+// TN = 64 (the class K <= 48): 128x64 tiles, 8x4 outputs per thread, up to
+// three CTAs per SM.  TN = 128 (the class K <= 100): 128x128 tiles, 8x8
+// outputs per thread, up to two CTAs per SM.
 template <bool PRED, int TN>
 __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     mp_strip_kernel(const MpSegment *__restrict__ segs, int nseg, int ks) {
@@ -774,7 +774,11 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     n_tiles++;
     n_empty += nact == 0;
     n_steps += nact;
-    if (PRED && nact > 0) load_bp_rows(jt * TN, mlo, mhi);
+    if (PRED && nact == s.K && s.K > 0)  // every step active: all rows, 16-byte copies spread over the CTA
+      strip_load_rows<TN>(reinterpret_cast<unsigned *>(Bps + TN), reinterpret_cast<const unsigned *>(s.Bp),
+                          s.ldbp, s.K, s.N, kseg, jt * TN, vec_bp, 0xffffffffu);
+    else if (PRED && nact > 0)
+      load_bp_rows(jt * TN, mlo, mhi);
     cp_async_commit();
     if (jt + 1 < jt1)  // B[buf ^ 1] was last read by the previous tile's add-mins, before (B)
       strip_load_rows<TN>(Bs + (buf ^ 1) * ks * TN, static_cast<const unsigned *>(s.B), s.ldb, s.K,
@@ -1583,8 +1587,11 @@ cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, 
                                   int max_k, cudaStream_t st) {
   if (max_k < 0 || max_k > kStripMaxK) return cudaErrorInvalidValue;
   const int ks = (max_k + 3) & ~3;
-  return pred ? launch_strip_t<true, kStripTN>(d_segs, nseg, strips, ks, st)
-              : launch_strip_t<false, kStripTN>(d_segs, nseg, strips, ks, st);
+  if (max_k <= kStripClassK[0])
+    return pred ? launch_strip_t<true, kStripClassTN[0]>(d_segs, nseg, strips, ks, st)
+                : launch_strip_t<false, kStripClassTN[0]>(d_segs, nseg, strips, ks, st);
+  return pred ? launch_strip_t<true, kStripClassTN[1]>(d_segs, nseg, strips, ks, st)
+              : launch_strip_t<false, kStripClassTN[1]>(d_segs, nseg, strips, ks, st);
 }
 
 int minplus_strip_tiles() { return kStripTiles; }
@@ -1645,12 +1652,19 @@ cudaError_t init_minplus_kernels() {
   if ((e = set_mp_attr<uint32_t, false>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<true>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<false>()) != cudaSuccess) return e;
-  const int smax = (int)strip_smem_bytes<kStripTN>((kStripMaxK + 3) & ~3);
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, kStripTN>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax)) != cudaSuccess)
+  const int smax0 = (int)strip_smem_bytes<kStripClassTN[0]>((kStripClassK[0] + 3) & ~3);
+  const int smax1 = (int)strip_smem_bytes<kStripClassTN[1]>((kStripClassK[1] + 3) & ~3);
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, kStripClassTN[0]>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax0)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, kStripTN>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, kStripClassTN[0]>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax0)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, kStripClassTN[1]>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax1)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, kStripClassTN[1]>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax1)) != cudaSuccess)
     return e;
 
   if ((e = cudaFuncSetAttribute(fw_pivot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
