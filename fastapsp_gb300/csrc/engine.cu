@@ -122,6 +122,10 @@ struct Plan {
     std::vector<int> panel_nseg, panel_tiles;
     std::vector<const MpSegment *> rest;
     std::vector<int> rest_nseg, rest_tiles, rest_strips;
+    // packed form with lookahead: the remaining tiles of round r without block
+    // row and column r + 1 (which pivot step r + 1 updates itself), strip form
+    std::vector<const MpSegment *> rest2;
+    std::vector<int> rest2_nseg, rest2_strips;
     // min-plus
     const MpSegment *mp = nullptr;
     int mp_nseg = 0, mp_tiles = 0;
@@ -189,9 +193,11 @@ struct fap_engine {
   void *d_w = nullptr, *d_iw = nullptr;
   unsigned *d_status = nullptr;
   unsigned long long *d_stats = nullptr;  // SSSP counters of the last solve
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // highest priority: the FW lookahead's pivot chain runs here
+  cudaStream_t side = nullptr;    // lowest priority: the FW remaining tiles beside that chain
   cudaEvent_t ev[6] = {};
   cudaEvent_t ev_sync[2] = {};
+  cudaEvent_t ev_fw[3] = {};      // FW lookahead: [0] after pivot step r, [1 + r % 2] after round r's tiles
   // work buffers
   DevBuf fw_d, fw_p;           // FW matrices arena
   DevBuf sssp_scratch, sssp_bits;
@@ -296,6 +302,23 @@ void fw_segments(void *D, int32_t *P, int64_t ld, int size, int r, MpSegment &ro
   t_rest = pairs * pairs;
 }
 
+// CTAs of an FW segment in the strip form (tiles_y row tiles).
+int fw_strips_of(const MpSegment &s, int tiles_y) {
+  const int T = fapk::fw_strip_tiles();
+  return tiles_y * ((s.tiles_x + T - 1) / T);
+}
+
+// Lookahead form of fw_segments' `rest` for pivot block r of nb: the rows and
+// columns other than r and r + 1 (block row and column r + 1 get round r's
+// update inside pivot step r + 1).  Returns its CTAs in the strip form.
+int fw_rest_lookahead(MpSegment &rest, int nb, int r) {
+  const int pairs = (nb - 2 + 1) / 2;
+  rest.row_skip2 = r + 1;
+  rest.col_skip2 = r + 1;
+  rest.tiles_x = pairs;
+  return fw_strips_of(rest, pairs);
+}
+
 // Min-plus segment C = A (x) B (fresh C), tiled in 128x128.
 MpSegment mp_segment(const void *A, int64_t lda, const void *B, int64_t ldb, const int32_t *Bp,
                      int64_t ldbp, void *C, int64_t ldc, int32_t *Cp, int64_t ldcp, int M, int N,
@@ -371,7 +394,7 @@ int build_plan(fap_engine *e, Plan &pl) {
   TableBuilder tb;
   struct GroupOffs {
     size_t batches, pdesc, row_begin, dec_begin, mp;
-    std::vector<size_t> diag, panel, rest;
+    std::vector<size_t> diag, panel, rest, rest2;
   };
   std::vector<GroupOffs> goffs(groups.size());
   pl.groups.assign(groups.size(), Plan::Group{});
@@ -479,13 +502,16 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.rest_nseg.assign(maxnb, 0);
     G.rest_tiles.assign(maxnb, 0);
     G.rest_strips.assign(maxnb, 0);
+    G.rest2_nseg.assign(maxnb, 0);
+    G.rest2_strips.assign(maxnb, 0);
     O.diag.assign(maxnb, 0);
     O.panel.assign(maxnb, 0);
     O.rest.assign(maxnb, 0);
+    O.rest2.assign(maxnb, 0);
     for (int r = 0; r < maxnb; r++) {
       std::vector<FwDiagJob> dj;
-      std::vector<MpSegment> ps, rs;
-      int pt = 0, rt = 0, rstrips = 0;
+      std::vector<MpSegment> ps, rs, r2s;
+      int pt = 0, rt = 0, rstrips = 0, r2strips = 0;
       for (const PartDesc &d : pdesc) {
         int nb = d.ld / B;
         if (r >= nb) continue;
@@ -497,6 +523,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         j.ld = d.ld;
         j.size = d.ld;
         j.block = r;
+        j.prev = r - 1;  // used by the packed form's pivot step (lookahead) only
         dj.push_back(j);
         if (nb > 1) {
           MpSegment rp, cp, rest;
@@ -511,8 +538,15 @@ int build_plan(fap_engine *e, Plan &pl) {
           rest.tile_begin = rt;
           rt += a3;
           rest.strip_begin = rstrips;
-          rstrips += rest.tiles_x * ((rest.tiles_x + fapk::fw_strip_tiles() - 1) / fapk::fw_strip_tiles());
+          rstrips += fw_strips_of(rest, rest.tiles_x);
           rs.push_back(rest);
+          MpSegment rest2 = rest;
+          const int s2 = r + 1 < nb ? fw_rest_lookahead(rest2, nb, r) : fw_strips_of(rest, rest.tiles_x);
+          if (s2 > 0) {
+            rest2.strip_begin = r2strips;
+            r2strips += s2;
+            r2s.push_back(rest2);
+          }
         }
       }
       G.diag_cnt[r] = (int)dj.size();
@@ -524,6 +558,9 @@ int build_plan(fap_engine *e, Plan &pl) {
       G.rest_tiles[r] = rt;
       G.rest_strips[r] = rstrips;
       O.rest[r] = tb.add(rs.data(), rs.size());
+      G.rest2_nseg[r] = (int)r2s.size();
+      G.rest2_strips[r] = r2strips;
+      O.rest2[r] = tb.add(r2s.data(), r2s.size());
     }
   }
   int st = pl.tables.ensure(std::max<size_t>(tb.bytes.size(), 64));
@@ -542,10 +579,12 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.diag.resize(R);
     G.panel.resize(R);
     G.rest.resize(R);
+    G.rest2.resize(R);
     for (size_t r = 0; r < R; r++) {
       G.diag[r] = reinterpret_cast<const FwDiagJob *>(base + O.diag[r]);
       G.panel[r] = reinterpret_cast<const MpSegment *>(base + O.panel[r]);
       G.rest[r] = reinterpret_cast<const MpSegment *>(base + O.rest[r]);
+      G.rest2[r] = reinterpret_cast<const MpSegment *>(base + O.rest2[r]);
     }
   }
   return FAP_OK;
@@ -623,18 +662,32 @@ struct Issuer {
     fapk::BuildArgs ba = build_args(e, pl, G);
     FAP_CUDA(fapk::launch_build(f32, pred, ba, st));
     if (last) FAP_CUDA(rec(2));
-    for (size_t r = 0; r < G.diag.size(); r++) {
-      if (packed) {  // pivot block and both panels in one launch
+    const int rounds = (int)G.diag.size();
+    for (int r = 0; r < rounds; r++) {
+      if (packed) {
+        // Lookahead.  Pivot step r (one launch: round r - 1's update of block
+        // row and column r, the closure, both panels) runs on the issuing
+        // stream; round r's remaining tiles other than block row and column
+        // r + 1 (`rest2`) on the side stream, where they overlap pivot step
+        // r + 1.  Pivot step r waits for `rest2` of round r - 2 (the last
+        // launch that wrote block row and column r); `rest2` of round r waits
+        // for pivot step r.  Pivot step r + 1 and `rest2` of round r touch
+        // disjoint entries: the pivot step reads block rows and columns r and
+        // r + 1 and writes r + 1; `rest2` reads block row and column r outside
+        // blocks r and r + 1 and writes neither.
+        if (r >= 2) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + r % 2], 0));
         FAP_CUDA(fapk::launch_fw_pivot(pred, G.diag[r], G.diag_cnt[r], st));
+        FAP_CUDA(cudaEventRecord(e->ev_fw[0], st));
+        FAP_CUDA(cudaStreamWaitEvent(e->side, e->ev_fw[0], 0));
+        FAP_CUDA(fapk::launch_fw_strips(pred, G.rest2[r], G.rest2_nseg[r], G.rest2_strips[r], e->side));
+        FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
       } else {
         FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
         FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
-      }
-      if (packed)  // remaining tiles: strip form (rows x columns of the pivot-free lists)
-        FAP_CUDA(fapk::launch_fw_strips(pred, G.rest[r], G.rest_nseg[r], G.rest_strips[r], st));
-      else
         FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
+      }
     }
+    if (packed && rounds > 0) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (rounds - 1) % 2], 0));  // join
     if (last) FAP_CUDA(rec(3));
     if (packed) {  // strip form for the small-K segments, tiles for the rest
       for (int c = 0; c < G.mp_ncls; c++)
@@ -835,7 +888,8 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
         return irc;
       }
       if (ce != cudaSuccess) return set_error(FAP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&pl->exec, graph, 0);
+      // kernel nodes keep the priority of the stream they were captured from
+      ce = cudaGraphInstantiate(&pl->exec, graph, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(graph);
       if (ce != cudaSuccess) {
         pl->exec = nullptr;
@@ -895,9 +949,13 @@ int init_device(fap_engine *e, int device) {
   if (prop.major < 10) return set_error(FAP_ERR_NO_DEVICE, "the engine is built for sm_103a (Blackwell Ultra) only");
   e->device = device;
   e->sm_count = prop.multiProcessorCount;
-  FAP_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  int prio_low = 0, prio_high = 0;
+  FAP_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+  FAP_CUDA(cudaStreamCreateWithPriority(&e->stream, cudaStreamNonBlocking, prio_high));
+  FAP_CUDA(cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, prio_low));
   for (auto &ev : e->ev) FAP_CUDA(cudaEventCreate(&ev));
   for (auto &ev : e->ev_sync) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  for (auto &ev : e->ev_fw) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   // status words: [0] error flags, [1]/[2] maxima for the packed-form bound
   FAP_CUDA(cudaMalloc(&e->d_status, 4 * sizeof(unsigned)));
   FAP_CUDA(cudaMemset(e->d_status, 0, 4 * sizeof(unsigned)));
@@ -1133,7 +1191,10 @@ int fap_destroy(fap_engine *e) {
       if (ev) cudaEventDestroy(ev);
     for (auto &ev : e->ev_sync)
       if (ev) cudaEventDestroy(ev);
+    for (auto &ev : e->ev_fw)
+      if (ev) cudaEventDestroy(ev);
     if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->side) cudaStreamDestroy(e->side);
     (void)cudaGetLastError();
   }
   delete e;
@@ -1355,12 +1416,12 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
   TableBuilder tb;
-  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb);
-  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), sr(maxnb);
+  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb);
+  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), sr(maxnb), nr2(maxnb), sr2(maxnb);
   for (int r = 0; r < maxnb; r++) {
     std::vector<FwDiagJob> dj;
-    std::vector<MpSegment> ps, rs;
-    int pt = 0, rt = 0, rstrips = 0;
+    std::vector<MpSegment> ps, rs, r2s;
+    int pt = 0, rt = 0, rstrips = 0, r2strips = 0;
     for (int32_t b = 0; b < count; b++) {
       int nb = (sizes[b] + Bk - 1) / Bk;
       if (r >= nb) continue;
@@ -1370,6 +1431,7 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
       j.ld = ld[b];
       j.size = sizes[b];
       j.block = r;
+      j.prev = r - 1;  // used by the packed form's pivot step (lookahead) only
       dj.push_back(j);
       if (nb > 1) {
         MpSegment a, c, rest;
@@ -1385,11 +1447,21 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
         rest.tile_begin = rt;
         rt += t3;
         rest.strip_begin = rstrips;
-        rstrips += rest.tiles_x * ((rest.tiles_x + fapk::fw_strip_tiles() - 1) / fapk::fw_strip_tiles());
+        rstrips += fw_strips_of(rest, rest.tiles_x);
         rs.push_back(rest);
+        MpSegment rest2 = rest;
+        const int s2 = r + 1 < nb ? fw_rest_lookahead(rest2, nb, r) : fw_strips_of(rest, rest.tiles_x);
+        if (s2 > 0) {
+          rest2.strip_begin = r2strips;
+          r2strips += s2;
+          r2s.push_back(rest2);
+        }
       }
     }
     sr[r] = rstrips;
+    nr2[r] = (int)r2s.size();
+    sr2[r] = r2strips;
+    or2[r] = tb.add(r2s.data(), r2s.size());
     nd[r] = (int)dj.size();
     od[r] = tb.add(dj.data(), dj.size());
     np[r] = (int)ps.size();
@@ -1425,16 +1497,22 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   }
   for (int r = 0; r < maxnb; r++) {
     const FwDiagJob *djobs = reinterpret_cast<const FwDiagJob *>(base + od[r]);
-    if (packed) {  // pivot block and both panels in one launch
+    if (packed) {  // lookahead, as in the solve's issue order
+      if (r >= 2) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + r % 2], 0));
       FAP_CUDA(fapk::launch_fw_pivot(pred, djobs, nd[r], st));
+      FAP_CUDA(cudaEventRecord(e->ev_fw[0], st));
+      FAP_CUDA(cudaStreamWaitEvent(e->side, e->ev_fw[0], 0));
+      FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + or2[r]), nr2[r],
+                                      sr2[r], e->side));
+      FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
     } else {
       FAP_CUDA(fapk::launch_fw_diag(f32, pred, djobs, nd[r], st));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], packed, st));
+      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]),
+                                          nr[r], tr[r], packed, st));
     }
-    const MpSegment *rseg = reinterpret_cast<const MpSegment *>(base + orr[r]);
-    if (packed) FAP_CUDA(fapk::launch_fw_strips(pred, rseg, nr[r], sr[r], st));
-    else FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, rseg, nr[r], tr[r], packed, st));
   }
+  if (packed) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (maxnb - 1) % 2], 0));  // join
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);
 }

@@ -57,6 +57,8 @@ struct MpSegment {
   int32_t col_skip;    // same for columns
   int32_t row_fix;     // >= 0: the row list is this one block
   int32_t col_fix;     // >= 0: the column list is this one block
+  int32_t row_skip2;   // a second block left out of the row list (only when > row_skip >= 0)
+  int32_t col_skip2;   // same for columns
   int32_t init_from_c; // 1: start from C/Cp (keep on ties); 0: start unreached/-1
   int32_t tiles_x;     // CTA tiles along columns
   int32_t tile_begin;  // first global CTA index of this segment
@@ -79,6 +81,9 @@ struct FwDiagJob {
   int64_t ld;
   int32_t size;  // matrix size (rows/cols >= size are outside the matrix)
   int32_t block; // pivot block index
+  int32_t prev;  // >= 0: the update of round `prev` (pivot block prev) to this
+                 // block row and column is applied first (lookahead: the
+                 // remaining-tile launch of round prev left them out); -1: none
 };
 
 // A strided row-major matrix of 4-byte values.

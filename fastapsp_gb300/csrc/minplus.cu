@@ -61,12 +61,28 @@ __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_
 __device__ __forceinline__ void cp_async_wait_2() { asm volatile("cp.async.wait_group 2;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
-// Block index of list entry g when block `skip` is left out of 0..nblocks-1.
-__device__ __forceinline__ int list_block(int g, int skip, int fix, int nblocks) {
+// Block index of list entry g of 0..nblocks-1 without block `skip` (and
+// `skip2`, when it is above `skip`), or of the one-block list `fix`; -1 past
+// the list.
+__device__ __forceinline__ int list_block(int g, int skip, int skip2, int fix, int nblocks) {
   if (fix >= 0) return g == 0 ? fix : -1;
-  int len = nblocks - ((skip >= 0 && skip < nblocks) ? 1 : 0);
-  if (g >= len) return -1;
-  return (skip >= 0 && g >= skip) ? g + 1 : g;
+  int b = g;
+  if (skip >= 0) {
+    if (b >= skip) b++;
+    if (skip2 > skip && b >= skip2) b++;
+  }
+  return b < nblocks ? b : -1;
+}
+
+// Length of such a list.
+__device__ __forceinline__ int list_len(int skip, int skip2, int fix, int nblocks) {
+  if (fix >= 0) return 1;
+  int len = nblocks;
+  if (skip >= 0 && skip < nblocks) {
+    len--;
+    if (skip2 > skip && skip2 < nblocks) len--;
+  }
+  return len;
 }
 
 // Stages k-chunk [k0, k0+32) of A (128 rows) and B (128 columns), and of B's
@@ -139,8 +155,8 @@ __device__ __forceinline__ TileGeom tile_geom(const MpSegment &s, int tile) {
   const int nbr = (s.M + kBlk - 1) / kBlk, nbc = (s.N + kBlk - 1) / kBlk;
 #pragma unroll
   for (int i = 0; i < 2; i++) {
-    int rb = list_block(2 * tyt + i, s.row_skip, s.row_fix, nbr);
-    int cb = list_block(2 * txt + i, s.col_skip, s.col_fix, nbc);
+    int rb = list_block(2 * tyt + i, s.row_skip, s.row_skip2, s.row_fix, nbr);
+    int cb = list_block(2 * txt + i, s.col_skip, s.col_skip2, s.col_fix, nbc);
     g.rbase[i] = rb >= 0 ? rb * kBlk : -1;
     g.cbase[i] = cb >= 0 ? cb * kBlk : -1;
   }
@@ -1003,15 +1019,15 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
   const int tyt = local / sx;
   const int nbr = (s.M + kBlk - 1) / kBlk, nbc = (s.N + kBlk - 1) / kBlk;
   // column list length, in blocks, and this strip's column tiles of CH blocks
-  const int ncb = s.col_fix >= 0 ? 1 : nbc - ((s.col_skip >= 0 && s.col_skip < nbc) ? 1 : 0);
+  const int ncb = list_len(s.col_skip, s.col_skip2, s.col_fix, nbc);
   const int jt0 = (local - tyt * sx) * kFwStripTiles * (2 / CH);
   const int jt1 = min(jt0 + kFwStripTiles * (2 / CH), (ncb + CH - 1) / CH);
-  const int rl0 = list_block(2 * tyt, s.row_skip, s.row_fix, nbr);
-  const int rl1 = list_block(2 * tyt + 1, s.row_skip, s.row_fix, nbr);
+  const int rl0 = list_block(2 * tyt, s.row_skip, s.row_skip2, s.row_fix, nbr);
+  const int rl1 = list_block(2 * tyt + 1, s.row_skip, s.row_skip2, s.row_fix, nbr);
   const int rbase0 = rl0 >= 0 ? rl0 * kBlk : -1, rbase1 = rl1 >= 0 ? rl1 * kBlk : -1;
   auto col_bases = [&](int jt) {  // first columns of the tile's blocks (-1: none)
-    const int b0 = list_block(CH * jt, s.col_skip, s.col_fix, nbc);
-    const int b1 = CH == 2 ? list_block(CH * jt + 1, s.col_skip, s.col_fix, nbc) : -1;
+    const int b0 = list_block(CH * jt, s.col_skip, s.col_skip2, s.col_fix, nbc);
+    const int b1 = CH == 2 ? list_block(CH * jt + 1, s.col_skip, s.col_skip2, s.col_fix, nbc) : -1;
     return make_int2(b0 >= 0 ? b0 * kBlk : -1, b1 >= 0 ? b1 * kBlk : -1);
   };
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
@@ -1380,6 +1396,89 @@ __device__ __forceinline__ void pivot_load_block(unsigned *dst, const FwDiagJob 
   }
 }
 
+// Lookahead part of round `r` of the blocked FW for the 64x64 block (cr, cc)
+// of a job's matrix (a block of the next pivot's row or column, or the next
+// pivot block itself), which the remaining-tile launch of round r left out:
+// C = min(C, A (x) B) with A = block (cr, r), B = block (r, cc), ties keeping
+// C, a strict improvement taking B's predecessor -- the same update that
+// launch applies to every other tile.  C comes from and goes back to the
+// closure buffer sm.D / sm.P (TO_SMEM) or global memory.  Kp, Kx and Xp are
+// scratch; ends with a barrier.
+template <bool PRED, bool TO_SMEM>
+__device__ void pivot_prev_block(PivotSmem &sm, const FwDiagJob &job, int cr, int cc, int r) {
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  unsigned *Dg = static_cast<unsigned *>(job.D);
+  const unsigned INF = Dist<uint32_t>::inf();
+  auto inside = [&](int gi, int gj) { return gi < job.size && gj < job.size; };
+  unsigned av[4][4], cv[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int li = ty * 4 + i;
+    unsigned bv[4];
+    int32_t bp[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int lj = tx * 4 + c;
+      const int ai = cr * kBlk + li, aj = r * kBlk + lj;
+      const int bi = r * kBlk + li, bj = cc * kBlk + lj;
+      const int ci = cr * kBlk + li, cj = cc * kBlk + lj;
+      av[i][c] = inside(ai, aj) ? Dg[(int64_t)ai * job.ld + aj] : INF;
+      bv[c] = inside(bi, bj) ? Dg[(int64_t)bi * job.ld + bj] : INF;
+      bp[c] = PRED && inside(bi, bj) ? job.P[(int64_t)bi * job.ld + bj] : -1;
+      if (TO_SMEM) cv[i][c] = sm.D[li][lj];
+      else cv[i][c] = inside(ci, cj) ? Dg[(int64_t)ci * job.ld + cj] : INF;
+    }
+    const unsigned id = (unsigned)(li + 1);  // B row k = li
+    *reinterpret_cast<uint4 *>(&sm.Kx[li][tx * 4]) =
+        make_uint4((min(bv[0], kPackH) << kIdxBits) | id, (min(bv[1], kPackH) << kIdxBits) | id,
+                   (min(bv[2], kPackH) << kIdxBits) | id, (min(bv[3], kPackH) << kIdxBits) | id);
+    if (PRED) *reinterpret_cast<int4 *>(&sm.Xp[li][tx * 4]) = make_int4(bp[0], bp[1], bp[2], bp[3]);
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++)  // A^T: k = column of A
+    *reinterpret_cast<uint4 *>(&sm.Kp[tx * 4 + c][ty * 4]) =
+        make_uint4(min(av[0][c], kPackH) << kIdxBits, min(av[1][c], kPackH) << kIdxBits,
+                   min(av[2][c], kPackH) << kIdxBits, min(av[3][c], kPackH) << kIdxBits);
+  __syncthreads();
+  unsigned acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[i][c] = kPackH << kIdxBits;
+#pragma unroll 4
+  for (int kk = 0; kk < kBlk; kk++) {
+    const uint4 a4 = *reinterpret_cast<const uint4 *>(&sm.Kp[kk][ty * 4]);
+    const uint4 b4 = *reinterpret_cast<const uint4 *>(&sm.Kx[kk][tx * 4]);
+    const unsigned a[4] = {a4.x, a4.y, a4.z, a4.w};
+    const unsigned b[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc[i][c] = __viaddmin_u32(a[i], b[c], acc[i][c]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int li = ty * 4 + i;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int lj = tx * 4 + c;
+      const unsigned key = min(min(cv[i][c], kPackH) << kIdxBits, acc[i][c]);
+      const unsigned idx = key & kIdxMask;
+      if (idx == 0) continue;
+      if (TO_SMEM) {
+        sm.D[li][lj] = key >> kIdxBits;
+        if (PRED) sm.P[li][lj] = sm.Xp[idx - 1][lj];
+      } else {
+        const int ci = cr * kBlk + li, cj = cc * kBlk + lj;
+        if (!inside(ci, cj)) continue;
+        Dg[(int64_t)ci * job.ld + cj] = key >> kIdxBits;
+        if (PRED) job.P[(int64_t)ci * job.ld + cj] = sm.Xp[idx - 1][lj];
+      }
+    }
+  }
+  __syncthreads();  // scratch free again
+}
+
 template <bool PRED>
 __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2)
     fw_pivot_kernel(const FwDiagJob *__restrict__ jobs) {
@@ -1406,13 +1505,36 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
     if (PRED && role == 0)
       pivot_load_block<true>(reinterpret_cast<unsigned *>(&sm.Xp[0][0]), job, r, panel_block(pi));
   };
-  // The first panel block's copy lands during the closure.
-  if (sub < npanel) load_values(sub);
-  cp_async_commit();
-  if (sub < npanel) load_preds(sub);
-  cp_async_commit();
+  // Lookahead: the update of round job.prev to this block row and column
+  // (left out by that round's remaining-tile launch) comes first -- CTA 0
+  // applies it to the pivot block before the closure, the others to the
+  // panel blocks meanwhile.  Without it the first panel block's copy lands
+  // during the closure; with it, after the cluster barrier that publishes
+  // those updates.
+  const int prev = job.prev;
+  auto first_copy = [&]() {
+    if (sub < npanel) load_values(sub);
+    cp_async_commit();
+    if (sub < npanel) load_preds(sub);
+    cp_async_commit();
+  };
+  if (prev < 0) first_copy();
 
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  if (rank != 0 && prev >= 0) {
+    const int lo = min(r, prev), hi = max(r, prev);
+    auto other = [&](int t) {  // t-th block other than r and prev
+      int b = t;
+      if (b >= lo) b++;
+      if (b >= hi) b++;
+      return b;
+    };
+    const int nother = nb - 2;
+    for (int t = rank - 1; t < 2 * nother; t += kPivotCtas - 1) {
+      if (t < nother) pivot_prev_block<PRED, false>(sm, job, r, other(t), prev);
+      else pivot_prev_block<PRED, false>(sm, job, other(t - nother), r, prev);
+    }
+  }
   if (rank == 0) {
     unsigned *Dg = static_cast<unsigned *>(job.D);
     const int base = r * kBlk;
@@ -1424,6 +1546,7 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
       if (PRED) sm.P[i][j] = ok ? job.P[(int64_t)gi * job.ld + gj] : -1;
     }
     __syncthreads();
+    if (prev >= 0) pivot_prev_block<PRED, true>(sm, job, r, r, prev);
     close_block<uint32_t, PRED>(sm.D, sm.P);
     for (int idx = threadIdx.x; idx < kBlk * kBlk; idx += kThreads) {
       const int i = idx >> 6, j = idx & 63;
@@ -1434,7 +1557,8 @@ __global__ void __cluster_dims__(kPivotCtas, 1, 1) __launch_bounds__(kThreads, 2
       }
     }
   }
-  cluster.sync();  // the closed pivot block is in CTA 0's shared memory
+  cluster.sync();  // the closed pivot block is in CTA 0's shared memory (and the lookahead updates are in memory)
+  if (prev >= 0) first_copy();
   if (rank != 0) {
     const unsigned *rD = cluster.map_shared_rank(&sm.D[0][0], 0);
     const int32_t *rP = cluster.map_shared_rank(&sm.P[0][0], 0);
