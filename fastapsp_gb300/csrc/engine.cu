@@ -460,6 +460,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         pl.max_mp_k = std::max(pl.max_mp_k, bdy);
         int c = 0;
         while (c < ncls && bdy > fapk::minplus_strip_class_k(c)) c++;
+        if (n >= (1 << 24)) c = ncls;  // the strip form needs leading dimensions below 2^24
         if (c < ncls) mps_cls[c].push_back(s);
         else mps_wide.push_back(s);
       }
@@ -1390,7 +1391,8 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
              (Cpath == nullptr || K <= fapk::max_packed_k());
   }
   const MpSegment *dseg = reinterpret_cast<const MpSegment *>(base + o_seg);
-  if (packed && K <= fapk::minplus_strip_max_k())
+  // the strip form addresses C rows with 32-bit offsets within a 128-row strip
+  if (packed && K <= fapk::minplus_strip_max_k() && ldc < (1 << 24) && (!Cpath || ldcp < (1 << 24)))
     FAP_CUDA(fapk::launch_minplus_strips(Cpath != nullptr, dseg, 1, mp_strips_of(s), K, st));
   else
     FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr, dseg, 1, tiles, packed, st));

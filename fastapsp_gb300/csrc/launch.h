@@ -21,7 +21,8 @@ int &launch_count();
 cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, int nseg,
                                  int tiles, bool packed, cudaStream_t st, int tile0 = 0);
 // Strip form of the packed min-plus: segments that do not accumulate into C
-// (init_from_c = 0), every K <= max_k <= minplus_strip_max_k(), CTAs numbered by
+// (init_from_c = 0), C's leading dimensions below 2^24, every
+// K <= max_k <= minplus_strip_max_k(), CTAs numbered by
 // MpSegment::strip_begin (ceil(M / 128) x ceil(tiles_x / minplus_strip_tiles())
 // strips per segment).  Same preconditions as the packed tile form.
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,

@@ -667,6 +667,15 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
   const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
   const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
   const bool vec_c = vec_stores_ok<PRED>(s);
+  // The epilogue's view of C in registers (the descriptor is in shared memory,
+  // which the compiler reads again after every barrier): this thread's rows
+  // are the same for every tile of the strip.
+  // (Row offsets within a strip are below 2^31 elements: callers send no
+  // leading dimension of 2^24 or more here.)
+  const int m_rows = s.M, n_cols = s.N;
+  const int ldc = (int)s.ldc, ldcp = (int)s.ldcp;
+  unsigned *const c_thr = static_cast<unsigned *>(s.C) + (int64_t)(row0 + ty * 4) * s.ldc;
+  int32_t *const p_thr = PRED ? s.Cp + (int64_t)(row0 + ty * 4) * s.ldcp : nullptr;
 
   auto load_flags = [&](int col0, int fb) {  // column flags of a tile, into parity fb
     if (threadIdx.x < TN) {
@@ -882,15 +891,16 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     }
 #pragma unroll
     for (int r = 0; r < 8; r++) {
-      const int row = row0 + (r >> 2) * kBlk + ty * 4 + (r & 3);
-      if (row >= s.M) continue;
-      unsigned *crow = static_cast<unsigned *>(s.C) + (int64_t)row * s.ldc;
-      int32_t *prow = PRED ? s.Cp + (int64_t)row * s.ldcp : nullptr;
+      const int rr = (r >> 2) * kBlk + (r & 3);  // row offset from this thread's first row
+      const int row = row0 + ty * 4 + rr;
+      if (row >= m_rows) continue;
+      unsigned *crow = c_thr + rr * ldc;
+      int32_t *prow = PRED ? p_thr + rr * ldcp : nullptr;
 #pragma unroll
       for (int h = 0; h < CH; h++) {
         const int sc0 = h * kBlk + tx * 4;
         const int col0 = colbase + sc0;
-        if (col0 >= s.N) continue;
+        if (col0 >= n_cols) continue;
         unsigned d[4] = {INF, INF, INF, INF};
         int32_t p[4] = {-1, -1, -1, -1};
         // a quad of unreached outputs (the common case on sparse graphs) needs
@@ -921,13 +931,13 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
             }
           }
         }
-        if (vec_c && col0 + 3 < s.N) {  // streaming stores: the rows are not read again here
+        if (vec_c && col0 + 3 < n_cols) {  // streaming stores: the rows are not read again here
           __stcs(reinterpret_cast<uint4 *>(crow + col0), make_uint4(d[0], d[1], d[2], d[3]));
           if (PRED) __stcs(reinterpret_cast<int4 *>(prow + col0), make_int4(p[0], p[1], p[2], p[3]));
         } else {
 #pragma unroll
           for (int q = 0; q < 4; q++)
-            if (col0 + q < s.N) {
+            if (col0 + q < n_cols) {
               crow[col0 + q] = d[q];
               if (PRED) prow[col0 + q] = p[q];
             }
