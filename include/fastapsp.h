@@ -24,7 +24,10 @@
  *  - Result buffers may be host memory (pageable or pinned) or device memory
  *    of the engine's GPU; the engine detects which.  Streams are passed as
  *    `void *` (a cudaStream_t) so that this header needs no CUDA headers;
- *    NULL means the engine's own stream.
+ *    NULL means the engine's own stream.  Work issued on a caller's stream
+ *    is ordered on that stream: the Floyd-Warshall phase of the packed int32
+ *    form forks part of its launches to an internal stream of the engine
+ *    and joins it back on the caller's stream before the next phase.
  */
 #ifndef FASTAPSP_H_
 #define FASTAPSP_H_
