@@ -136,3 +136,23 @@ def test_solve_into_page_locked_host_rows(gpu, name, mode, with_pred):
             assert torch.equal(dh, dd.cpu())
             if with_pred:
                 assert torch.equal(ph, pd.cpu())
+
+
+def test_batched_solve_repeats_bit_for_bit(gpu):
+    """The batched form's overlapped launches (FW lookahead on two streams)
+    give the same distances and predecessors on every replay of the captured
+    graph, and the same as the plain form."""
+    from fastapsp_gb300 import graphs
+
+    g = graphs.geometric_knn(n=6144, k=3, seed=11)
+    n = g.n
+    with gpu.Engine(n, g.row_offset, g.col_val, g.weight, 6, dtype=gpu.DTYPE_I32) as eng:
+        outs = []
+        for mode in (1, 1, 1, 0):
+            d = torch.empty((n, n), dtype=torch.int32, device="cuda")
+            p = torch.empty((n, n), dtype=torch.int32, device="cuda")
+            eng.solve(d, p, mode)
+            torch.cuda.synchronize()
+            outs.append((d.cpu(), p.cpu()))
+    for d, p in outs[1:]:
+        assert torch.equal(d, outs[0][0]) and torch.equal(p, outs[0][1])
