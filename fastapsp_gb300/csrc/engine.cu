@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -126,6 +127,10 @@ struct Plan {
     // row and column r + 1 (which pivot step r + 1 updates itself), strip form
     std::vector<const MpSegment *> rest2;
     std::vector<int> rest2_nseg, rest2_strips;
+    // boundary rows in their own buffer (host results): per part {element
+    // offset in the results, element offset in the buffer, elements}, copied
+    // out as soon as the SSSP has written them
+    std::vector<std::array<int64_t, 3>> bnd_copies;
     // min-plus
     const MpSegment *mp = nullptr;
     int mp_nseg = 0, mp_tiles = 0;
@@ -198,6 +203,8 @@ struct fap_engine {
   cudaEvent_t ev[6] = {};
   cudaEvent_t ev_sync[2] = {};
   cudaEvent_t ev_fw[3] = {};      // FW lookahead: [0] after pivot step r, [1 + r % 2] after round r's tiles
+  cudaStream_t copy = nullptr;    // early copy-out of boundary rows (host results)
+  cudaEvent_t ev_copy[2] = {};    // [0] SSSP rows written, [1] their copy-out done
   // work buffers
   DevBuf fw_d, fw_p;           // FW matrices arena
   DevBuf sssp_scratch, sssp_bits;
@@ -434,7 +441,9 @@ int build_plan(fap_engine *e, Plan &pl) {
       d.ld = ldv[idx];
       d.mat_off = mat_off[idx];
       d.row_off = boff;
+      d.dec_off = roff;  // the decode writes the result rows themselves
       pdesc.push_back(d);
+      if (pl.bdist && bdy > 0) G.bnd_copies.push_back({roff, boff, (int64_t)bdy * n});
       row_begin.push_back(row_begin.back() + d.ld);
       dec_begin.push_back(dec_begin.back() + bdy);
       pl.max_sub = std::max(pl.max_sub, sub);
@@ -662,6 +671,24 @@ struct Issuer {
     Plan::Group &G = pl.groups[g];
     fapk::BuildArgs ba = build_args(e, pl, G);
     FAP_CUDA(fapk::launch_build(f32, pred, ba, st));
+    if (!G.bnd_copies.empty()) {
+      // Boundary rows in their own buffer (results in host memory): their
+      // columns outside the part are final after the SSSP, so they cross the
+      // host link now, while the FW runs; the decode then writes the part's
+      // own columns straight into the result rows, after this copy.
+      FAP_CUDA(cudaEventRecord(e->ev_copy[0], st));
+      FAP_CUDA(cudaStreamWaitEvent(e->copy, e->ev_copy[0], 0));
+      for (const auto &c : G.bnd_copies) {
+        FAP_CUDA(cudaMemcpyAsync(static_cast<char *>(pl.dist) + c[0] * 4,
+                                 static_cast<const char *>(pl.bdist) + c[1] * 4, (size_t)c[2] * 4,
+                                 cudaMemcpyDefault, e->copy));
+        if (pred)
+          FAP_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(pl.pred) + c[0] * 4,
+                                   reinterpret_cast<const char *>(pl.bpred) + c[1] * 4,
+                                   (size_t)c[2] * 4, cudaMemcpyDefault, e->copy));
+      }
+      FAP_CUDA(cudaEventRecord(e->ev_copy[1], e->copy));
+    }
     if (last) FAP_CUDA(rec(2));
     const int rounds = (int)G.diag.size();
     for (int r = 0; r < rounds; r++) {
@@ -700,8 +727,8 @@ struct Issuer {
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, packed, st));
     }
     if (last) FAP_CUDA(rec(4));
-    FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.bdist ? pl.bdist : pl.dist,
-                                 pl.bdist ? pl.bpred : pl.pred, st));
+    if (!G.bnd_copies.empty()) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_copy[1], 0));
+    FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, st));
     if (last) FAP_CUDA(rec(5));
     return FAP_OK;
   }
@@ -957,6 +984,8 @@ int init_device(fap_engine *e, int device) {
   for (auto &ev : e->ev) FAP_CUDA(cudaEventCreate(&ev));
   for (auto &ev : e->ev_sync) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   for (auto &ev : e->ev_fw) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  FAP_CUDA(cudaStreamCreateWithFlags(&e->copy, cudaStreamNonBlocking));
+  for (auto &ev : e->ev_copy) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   // status words: [0] error flags, [1]/[2] maxima for the packed-form bound
   FAP_CUDA(cudaMalloc(&e->d_status, 4 * sizeof(unsigned)));
   FAP_CUDA(cudaMemset(e->d_status, 0, 4 * sizeof(unsigned)));
@@ -1194,6 +1223,9 @@ int fap_destroy(fap_engine *e) {
       if (ev) cudaEventDestroy(ev);
     for (auto &ev : e->ev_fw)
       if (ev) cudaEventDestroy(ev);
+    for (auto &ev : e->ev_copy)
+      if (ev) cudaEventDestroy(ev);
+    if (e->copy) cudaStreamDestroy(e->copy);
     if (e->stream) cudaStreamDestroy(e->stream);
     if (e->side) cudaStreamDestroy(e->side);
     (void)cudaGetLastError();
@@ -1263,7 +1295,8 @@ static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_
   // Page-locked host results: the kernels write the inner rows straight into
   // them (no device copy of the n x n result, and the copy-out overlaps the
   // min-plus); the boundary rows, which the FW build and the min-plus read
-  // back, stay in a device buffer and are copied out at the end.
+  // back, stay in a device buffer, copied out right after the SSSP (during
+  // the FW), and the decode then writes their own-part columns in place.
   void *hd = dev_d ? nullptr : mapped_host_ptr(dist);
   void *hp = (pred && !dev_p) ? mapped_host_ptr(pred) : nullptr;
   if (!dev_d && hd && (pred == nullptr || hp)) {
@@ -1280,17 +1313,6 @@ static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_
     if ((rc = run_parts(e, mode, hd, static_cast<int32_t *>(hp), parts, offs, st, e->bnd_d.p, bp,
                         boffs)) != FAP_OK)
       return rc;
-    for (size_t i = 0; i < parts.size(); i++) {
-      const size_t rb = (size_t)e->bdy_num[parts[i]] * e->n * 4;
-      if (rb == 0) continue;
-      FAP_CUDA(cudaMemcpyAsync(static_cast<char *>(dist) + offs[i] * 4,
-                               static_cast<char *>(e->bnd_d.p) + boffs[i] * 4, rb,
-                               cudaMemcpyDeviceToHost, st));
-      if (pred)
-        FAP_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(pred) + offs[i] * 4,
-                                 static_cast<char *>(e->bnd_p.p) + boffs[i] * 4, rb,
-                                 cudaMemcpyDeviceToHost, st));
-    }
   } else {
     void *dd = dist;
     int32_t *dp = pred;

@@ -97,7 +97,8 @@ struct PartDesc {
   int32_t sub, bdy, start;  // part size, boundary count, first sorted position
   int32_t ld;               // leading dimension of the part's FW matrix
   int64_t mat_off;          // element offset of the FW matrix in the arena
-  int64_t row_off;          // element offset of the part's first result row
+  int64_t row_off;          // element offset of the part's first boundary row (SSSP output, build input)
+  int64_t dec_off;          // element offset of the part's first row where the decode writes
 };
 struct BuildArgs {
   int32_t n;

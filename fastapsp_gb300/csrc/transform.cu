@@ -101,8 +101,8 @@ __global__ void __launch_bounds__(128) decode_kernel(BuildArgs a, T *rows, int32
   if (i >= pd.bdy) return;
   const T *D = static_cast<const T *>(a.mat) + pd.mat_off + (int64_t)i * pd.ld;
   const int32_t *P = PRED ? a.matp + pd.mat_off + (int64_t)i * pd.ld : nullptr;
-  T *dst = rows + pd.row_off + (int64_t)i * a.ldr;
-  int32_t *dstp = PRED ? rowsp + pd.row_off + (int64_t)i * a.ldr : nullptr;
+  T *dst = rows + pd.dec_off + (int64_t)i * a.ldr;
+  int32_t *dstp = PRED ? rowsp + pd.dec_off + (int64_t)i * a.ldr : nullptr;
   for (int j = threadIdx.x; j < pd.sub; j += blockDim.x) {
     const int v = a.st2ed[pd.start + j];
     dst[v] = D[j];
