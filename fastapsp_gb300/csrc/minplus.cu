@@ -959,8 +959,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
 // the segment's row list (A = D_ir resident) and the column tiles of up to
 // kFwStripTiles block pairs of its column list.  Everything a tile needs is
 // in flight before it is needed: B (= D_rj) double-buffered, the current
-// tile's C staged behind its DPX loop, B's predecessors staged behind the
-// next tile's loop.  The product starts from "unreached" and C joins in the
+// tile's C and B's predecessors staged behind its DPX loop.  The product starts from "unreached" and C joins in the
 // epilogue with index 0, which gives the same minimum and tie rule as
 // starting from C.
 constexpr int kFwStripTiles = 4;  // block pairs (128 columns) per strip
@@ -1061,10 +1060,11 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
   int2 cb = col_bases(jt0);
   fw_load_b<TN>(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
   cp_async_commit();
-  if (PRED)
-    fw_load_b<TN>(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
-                  s.ldbp, s.K, s.N, cb, vec_bp, 0xffffffffu);
-  cp_async_commit();
+  // The epilogue's view of C in registers (the descriptor is in shared memory).
+  unsigned *const c_mat = static_cast<unsigned *>(s.C);
+  int32_t *const p_mat = s.Cp;
+  const int64_t ldc = s.ldc, ldcp = s.ldcp;
+  const int m_rows = s.M, n_cols = s.N;
 
   for (int jt = jt0; jt < jt1; jt++) {
     const int buf = (jt - jt0) & 1;
@@ -1073,7 +1073,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       fw_load_b<TN>(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
                 col_bases(jt + 1), vec_b, INF);
     cp_async_commit();
-    cp_async_wait_1();  // A, this tile's B and its predecessors have landed
+    cp_async_wait_1();  // A and this tile's B have landed
     if (jt == jt0)  // A keys; a warp converts 32 entries of one step k and marks finite ones
       for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads) {
         const unsigned v = (&sm.A[0][0])[idx];
@@ -1123,6 +1123,10 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
           }
         }
       }
+      // ... and B's predecessors of this tile, read in the epilogue only
+      if (PRED)
+        fw_load_b<TN>(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
+                      s.ldbp, s.K, s.N, cb, vec_bp, 0xffffffffu);
       cp_async_commit();
     }
 
@@ -1186,7 +1190,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       }
     }
     cp_async_wait_0();
-    __syncthreads();  // C staged by every thread
+    __syncthreads();  // C and the predecessors staged by every thread
 
     // Epilogue: C joins with index 0; only strict improvements are stored.
 #pragma unroll
@@ -1194,7 +1198,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       const int m = (r >> 2) * kBlk + ty * 4 + (r & 3);
       const int rb = (r >> 2) ? rbase1 : rbase0;
       const int row = rb + ty * 4 + (r & 3);
-      if (rb < 0 || row >= s.M) continue;
+      if (rb < 0 || row >= m_rows) continue;
 #pragma unroll
       for (int h = 0; h < CH; h++) {
         const int cbh = h ? cb.y : cb.x;
@@ -1207,17 +1211,13 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
           const unsigned cq = q == 0 ? cv.x : q == 1 ? cv.y : q == 2 ? cv.z : cv.w;
           const unsigned key = min(min(cq, kPackH) << kIdxBits, acc[r][h * 4 + q]);
           const unsigned idx = key & kIdxMask;
-          if (idx == 0 || col >= s.N) continue;
-          static_cast<unsigned *>(s.C)[(int64_t)row * s.ldc + col] = key >> kIdxBits;
-          if (PRED) s.Cp[(int64_t)row * s.ldcp + col] = sm.Bp[idx - 1][sc0 + q];
+          if (idx == 0 || col >= n_cols) continue;
+          c_mat[(int64_t)row * ldc + col] = key >> kIdxBits;
+          if (PRED) p_mat[(int64_t)row * ldcp + col] = sm.Bp[idx - 1][sc0 + q];
         }
       }
     }
     __syncthreads();  // C, B[buf] and the predecessors are free again
-    if (PRED && jt + 1 < jt1)
-      fw_load_b<TN>(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
-                s.ldbp, s.K, s.N, col_bases(jt + 1), vec_bp, 0xffffffffu);
-    cp_async_commit();
   }
   cp_async_wait_0();
 }
