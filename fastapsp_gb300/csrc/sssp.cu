@@ -133,6 +133,8 @@ __device__ __forceinline__ void sssp_out_block(const SsspArgs &a,
     if (PRED) {
       int dmax = max(deg[0], deg[1]);
       if (VPW == 2) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, 16));
+      // vertices that no source of the batch reached need no scan
+      if (!__any_sync(0xffffffffu, dk[0] < INF || dk[1] < INF)) dmax = 0;
       for (int j = 0; j < dmax; j++) {
         int u[2];
         unsigned wq[2];
