@@ -6,18 +6,25 @@
 // Floyd-Warshall (floyd_CPU_path, fap/kernel/floyd.h:38-49; GPU kernels
 // fw_kernel1 / FW_kernel1A2 / fw_kernel3, fap/kernel/cuda/floyd.cu:26-267).
 //
-// Design (GB300): one generic CTA tile kernel computes C = min(C0, A (x) B)
-// for a 128x128 output tile with 256 threads, 8x8 outputs per thread held in
-// registers, k staged through shared memory in chunks of 32 by cp.async with a
-// two-stage pipeline.  The argmin is tracked as the chunk-local k of the last
-// strict improvement; after each chunk the predecessor is read from the staged
-// B-predecessor tile, so the inner loop is add / compare / two selects.  A
-// batch of segments (one per matrix or per FW panel) is served by one launch;
-// each CTA finds its segment by binary search over the segments' first tile.
+// Kernels of this file:
+//  - mp_tile_kernel (FP32 and wide int32): the generic tile form.  One CTA
+//    computes C = min(C0, A (x) B) for a 128x128 output tile with 256
+//    threads, 8x8 outputs per thread in registers, k staged in chunks of 32
+//    by cp.async with a two-stage pipeline; the argmin is the chunk-local k
+//    of the last strict improvement, resolved against the staged
+//    B-predecessor tile after each chunk.  A batch of segments (one per
+//    matrix or FW panel) is one launch; each CTA finds its segment by binary
+//    search over the segments' first tile.
+//  - mp_tile_packed_kernel, mp_strip_kernel, mp_fwstrip_kernel, fw_pivot_kernel
+//    (int32 whose finite results stay below 2^24 - 1): packed keys
+//    (d << 7) | idx, one DPX __viaddmin_u32 per add-min, which gives the
+//    minimum and, on ties, the smallest idx -- the current value (idx 0)
+//    first, then the first k.  The strip kernels keep A resident for a strip
+//    of column tiles and skip the steps k whose A column or B row has no
+//    finite entry in the tile (such a candidate never wins).
 //
-// Floyd-Warshall over 64-wide pivot blocks uses the same tile kernel for the
-// panel and remaining-tile phases: once the pivot block is closed (shortest
-// paths through its own vertices, zero diagonal), the row panel is
+// Floyd-Warshall over 64-wide pivot blocks: once the pivot block is closed
+// (shortest paths through its own vertices, zero diagonal), the row panel is
 // D_rr (x) D_rj, the column panel D_ir (x) D_rr and every other tile
 // min(D_ij, D_ir (x) D_rj).  Ties keep the current value, so predecessors
 // follow P[i][j] = P[k][j] on strict improvement as in the reference.
