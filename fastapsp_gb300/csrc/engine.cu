@@ -122,7 +122,7 @@ struct Plan {
     std::vector<const MpSegment *> panel;
     std::vector<int> panel_nseg, panel_tiles;
     std::vector<const MpSegment *> rest;
-    std::vector<int> rest_nseg, rest_tiles, rest_strips;
+    std::vector<int> rest_nseg, rest_tiles;
     // packed form with lookahead: the remaining tiles of round r without block
     // row and column r + 1 (which pivot step r + 1 updates itself), strip form
     std::vector<const MpSegment *> rest2;
@@ -511,7 +511,6 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.panel_tiles.assign(maxnb, 0);
     G.rest_nseg.assign(maxnb, 0);
     G.rest_tiles.assign(maxnb, 0);
-    G.rest_strips.assign(maxnb, 0);
     G.rest2_nseg.assign(maxnb, 0);
     G.rest2_strips.assign(maxnb, 0);
     O.diag.assign(maxnb, 0);
@@ -521,7 +520,7 @@ int build_plan(fap_engine *e, Plan &pl) {
     for (int r = 0; r < maxnb; r++) {
       std::vector<FwDiagJob> dj;
       std::vector<MpSegment> ps, rs, r2s;
-      int pt = 0, rt = 0, rstrips = 0, r2strips = 0;
+      int pt = 0, rt = 0, r2strips = 0;
       for (const PartDesc &d : pdesc) {
         int nb = d.ld / B;
         if (r >= nb) continue;
@@ -547,8 +546,6 @@ int build_plan(fap_engine *e, Plan &pl) {
           ps.push_back(cp);
           rest.tile_begin = rt;
           rt += a3;
-          rest.strip_begin = rstrips;
-          rstrips += fw_strips_of(rest, rest.tiles_x);
           rs.push_back(rest);
           MpSegment rest2 = rest;
           const int s2 = r + 1 < nb ? fw_rest_lookahead(rest2, nb, r) : fw_strips_of(rest, rest.tiles_x);
@@ -566,7 +563,6 @@ int build_plan(fap_engine *e, Plan &pl) {
       O.panel[r] = tb.add(ps.data(), ps.size());
       G.rest_nseg[r] = (int)rs.size();
       G.rest_tiles[r] = rt;
-      G.rest_strips[r] = rstrips;
       O.rest[r] = tb.add(rs.data(), rs.size());
       G.rest2_nseg[r] = (int)r2s.size();
       G.rest2_strips[r] = r2strips;
@@ -1441,11 +1437,11 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   cudaStream_t st = pick_stream(e, stream);
   TableBuilder tb;
   std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb);
-  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), sr(maxnb), nr2(maxnb), sr2(maxnb);
+  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), nr2(maxnb), sr2(maxnb);
   for (int r = 0; r < maxnb; r++) {
     std::vector<FwDiagJob> dj;
     std::vector<MpSegment> ps, rs, r2s;
-    int pt = 0, rt = 0, rstrips = 0, r2strips = 0;
+    int pt = 0, rt = 0, r2strips = 0;
     for (int32_t b = 0; b < count; b++) {
       int nb = (sizes[b] + Bk - 1) / Bk;
       if (r >= nb) continue;
@@ -1470,8 +1466,6 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
         ps.push_back(c);
         rest.tile_begin = rt;
         rt += t3;
-        rest.strip_begin = rstrips;
-        rstrips += fw_strips_of(rest, rest.tiles_x);
         rs.push_back(rest);
         MpSegment rest2 = rest;
         const int s2 = r + 1 < nb ? fw_rest_lookahead(rest2, nb, r) : fw_strips_of(rest, rest.tiles_x);
@@ -1482,7 +1476,6 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
         }
       }
     }
-    sr[r] = rstrips;
     nr2[r] = (int)r2s.size();
     sr2[r] = r2strips;
     or2[r] = tb.add(r2s.data(), r2s.size());
