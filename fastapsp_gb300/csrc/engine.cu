@@ -747,13 +747,13 @@ int check_status(fap_engine *e);
 std::vector<const void *> buffer_signature(const fap_engine *e);
 
 // SSSP step autotuner: times the plan's SSSP phase (every group) with a few
-// near-far steps -- multiples of the mean edge weight, and plain frontier
-// Bellman-Ford -- and keeps the fastest.  The step only orders the work, so
+// near-far steps -- multiples of the mean edge weight from 4 to 128, and
+// plain frontier Bellman-Ford -- and keeps the fastest.  The step only orders the work, so
 // every candidate produces the same rows.  Runs once per engine, on the first
 // run of a plan, when the step was left automatic.
 int autotune_sssp(fap_engine *e, Plan &pl, cudaStream_t st) {
   const double unit = e->f32() ? e->wmean : std::max(1.0, e->wmean);
-  const double factors[] = {2.0, 8.0, 32.0, 128.0, 0.0};
+  const double factors[] = {4.0, 8.0, 16.0, 24.0, 32.0, 48.0, 64.0, 128.0, 0.0};
   double best = 0, best_ms = 1e300;
   cudaEvent_t t0 = e->ev_sync[0], t1 = e->ev_sync[1];
   cudaEvent_t a, b;
