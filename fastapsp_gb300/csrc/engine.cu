@@ -713,6 +713,17 @@ struct Issuer {
     }
     if (packed && rounds > 0) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (rounds - 1) % 2], 0));  // join
     if (last) FAP_CUDA(rec(3));
+    // Host results: the decode (own-part columns of the boundary rows, written
+    // straight into the host rows) runs on the copy stream beside the
+    // min-plus, after the FW and after the boundary rows' copy-out; the
+    // min-plus reads neither those rows nor anything the decode writes.
+    const bool decode_aside = !G.bnd_copies.empty();
+    if (decode_aside) {
+      FAP_CUDA(cudaEventRecord(e->ev_copy[0], st));
+      FAP_CUDA(cudaStreamWaitEvent(e->copy, e->ev_copy[0], 0));
+      FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, e->copy));
+      FAP_CUDA(cudaEventRecord(e->ev_copy[1], e->copy));
+    }
     if (packed) {  // strip form for the small-K segments, tiles for the rest
       for (int c = 0; c < G.mp_ncls; c++)
         FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
@@ -723,8 +734,8 @@ struct Issuer {
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, packed, st));
     }
     if (last) FAP_CUDA(rec(4));
-    if (!G.bnd_copies.empty()) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_copy[1], 0));
-    FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, st));
+    if (decode_aside) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_copy[1], 0));  // join
+    else FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, st));
     if (last) FAP_CUDA(rec(5));
     return FAP_OK;
   }
