@@ -979,11 +979,14 @@ int init_device(fap_engine *e, int device) {
   }
   if (device < 0 || device >= count) return set_error(FAP_ERR_INVALID, "device ordinal out of range");
   FAP_CUDA(cudaSetDevice(device));
-  cudaDeviceProp prop;
-  FAP_CUDA(cudaGetDeviceProperties(&prop, device));
-  if (prop.major < 10) return set_error(FAP_ERR_NO_DEVICE, "the engine is built for sm_103a (Blackwell Ultra) only");
+  // two attributes, not cudaGetDeviceProperties (which queries every property
+  // and costs milliseconds per engine)
+  int major = 0, sms = 0;
+  FAP_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device));
+  FAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  if (major < 10) return set_error(FAP_ERR_NO_DEVICE, "the engine is built for sm_103a (Blackwell Ultra) only");
   e->device = device;
-  e->sm_count = prop.multiProcessorCount;
+  e->sm_count = sms;
   int prio_low = 0, prio_high = 0;
   FAP_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
   FAP_CUDA(cudaStreamCreateWithPriority(&e->stream, cudaStreamNonBlocking, prio_high));
