@@ -269,8 +269,9 @@ __device__ __forceinline__ void tile_wide(MpSmem<T> &sm, const MpSegment &s, con
     cp_async_commit();
     cp_async_wait_1();
     __syncthreads();
+    const int kn = min(kBK, s.K - ch * kBK);  // steps of this chunk (the rest is fill)
 #pragma unroll 2
-    for (int kk = 0; kk < kBK; kk++) {
+    for (int kk = 0; kk < kn; kk++) {
       T a[8], b[8];
 #pragma unroll
       for (int r = 0; r < 8; r++) a[r] = sm.A[buf][smem_row(g, r)][kk];
@@ -443,8 +444,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     if (ch == 0 && stage_bp) cp_async_wait_2(); else cp_async_wait_1();
     keys_from_values(sm, buf, ch * kBK);
     __syncthreads();
+    const int kn = min(kBK, s.K - ch * kBK);  // steps of this chunk (the rest is fill)
 #pragma unroll 2
-    for (int kk = 0; kk < kBK; kk++) {
+    for (int kk = 0; kk < kn; kk++) {
       unsigned a[8], b[8];
 #pragma unroll
       for (int r = 0; r < 8; r++) a[r] = sm.A[buf][smem_row(g, r)][kk];
