@@ -92,9 +92,10 @@ __device__ __forceinline__ int list_len(int skip, int skip2, int fix, int nblock
   return len;
 }
 
-// Stages k-chunk [k0, k0+32) of A (128 rows) and B (128 columns), and of B's
-// predecessors when WITH_BP, with 4-byte cp.async; entries outside the
-// matrices are written directly as "unreached" / -1.
+// Stages k-chunk [k0, k0+32) of A (128 rows, 4-byte cp.async into the padded
+// rows) and B (128 columns), and of B's predecessors when WITH_BP (16-byte
+// cp.async of 4 columns where aligned); entries outside the matrices are
+// written directly as "unreached" / -1.
 template <typename T, bool WITH_BP, typename SM>
 __device__ __forceinline__ void load_chunk(SM &sm, int buf, const MpSegment &s, const int rbase[2],
                                            const int cbase[2], int k0) {
@@ -117,23 +118,42 @@ __device__ __forceinline__ void load_chunk(SM &sm, int buf, const MpSegment &s, 
       }
     }
   }
-  // B (and its predecessors): 32 k x 128 columns; threads run along columns.
+  // B (and its predecessors): 32 k x 128 columns; a warp takes one row k,
+  // 4 consecutive columns a lane (keys_from_values relies on this mapping).
   {
-    const int j = t & 127;
-    const int cb = cbase[j >> 6];
-    const int col = cb + (j & 63);
-    const bool colok = cb >= 0 && col < s.N;
+    const int j4 = (t & 31) * 4;
+    const int cb = cbase[j4 >> 6];
+    const int col = cb + (j4 & 63);
+    const bool full = cb >= 0 && col + 3 < s.N;
+    const bool vec = full && (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
+    const bool vecp = WITH_BP && full && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
 #pragma unroll 4
-    for (int it = 0; it < kBK / 2; it++) {
-      const int kk = (t >> 7) + 2 * it;
+    for (int it = 0; it < kBK / 8; it++) {
+      const int kk = (t >> 5) + 8 * it;
       const int kg = k0 + kk;
-      T *dst = &sm.B[buf][kk][j];
-      if (colok && kg < s.K) {
-        cp_async4(dst, static_cast<const T *>(s.B) + (int64_t)kg * s.ldb + col);
-        if constexpr (WITH_BP) cp_async4(&sm.Bp[buf][kk][j], s.Bp + (int64_t)kg * s.ldbp + col);
+      T *dst = &sm.B[buf][kk][j4];
+      const T *src = static_cast<const T *>(s.B) + (int64_t)kg * s.ldb + col;
+      if (kg < s.K && vec) {
+        cp_async16(dst, src);
       } else {
-        *dst = INF;
-        if constexpr (WITH_BP) sm.Bp[buf][kk][j] = -1;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (cb >= 0 && col + q < s.N && kg < s.K) cp_async4(dst + q, src + q);
+          else dst[q] = INF;
+        }
+      }
+      if constexpr (WITH_BP) {
+        int32_t *dp = &sm.Bp[buf][kk][j4];
+        const int32_t *sp = s.Bp + (int64_t)kg * s.ldbp + col;
+        if (kg < s.K && vecp) {
+          cp_async16(dp, sp);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            if (cb >= 0 && col + q < s.N && kg < s.K) cp_async4(dp + q, sp + q);
+            else dp[q] = -1;
+          }
+        }
       }
     }
   }
@@ -351,8 +371,8 @@ struct KeySmem {
 };
 
 // Stages B-predecessor rows [k0, k0+32) into Bp[k0..] (not double-buffered:
-// every row of the whole K range keeps its own slot), same thread mapping as
-// the B loads of load_chunk.
+// every row of the whole K range keeps its own slot); read only after a
+// barrier, so any thread mapping does.
 __device__ __forceinline__ void load_bp_rows(KeySmem &sm, const MpSegment &s, const int cbase[2],
                                              int k0) {
   const int t = threadIdx.x;
@@ -383,12 +403,18 @@ __device__ __forceinline__ void keys_from_values(KeySmem &sm, int buf, int k0) {
     }
   }
   {
-    const int j = t & 127;
+    const int j4 = (t & 31) * 4;
 #pragma unroll 4
-    for (int it = 0; it < kBK / 2; it++) {
-      const int kk = (t >> 7) + 2 * it;
-      const unsigned idx = (unsigned)((k0 + kk) & kMaxPackedK) + 1u;
-      sm.B[buf][kk][j] = (min(sm.B[buf][kk][j], kPackH) << kIdxBits) | (idx & kIdxMask);
+    for (int it = 0; it < kBK / 8; it++) {
+      const int kk = (t >> 5) + 8 * it;
+      const unsigned idx = ((unsigned)((k0 + kk) & kMaxPackedK) + 1u) & kIdxMask;
+      uint4 *p = reinterpret_cast<uint4 *>(&sm.B[buf][kk][j4]);
+      uint4 v = *p;
+      v.x = (min(v.x, kPackH) << kIdxBits) | idx;
+      v.y = (min(v.y, kPackH) << kIdxBits) | idx;
+      v.z = (min(v.z, kPackH) << kIdxBits) | idx;
+      v.w = (min(v.w, kPackH) << kIdxBits) | idx;
+      *p = v;
     }
   }
 }
