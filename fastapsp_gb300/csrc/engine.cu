@@ -724,10 +724,10 @@ struct Issuer {
       FAP_CUDA(fapk::launch_decode(f32, pred, ba, pl.dist, pl.pred, e->copy));
       FAP_CUDA(cudaEventRecord(e->ev_copy[1], e->copy));
     }
-    if (packed) {  // strip form for the small-K segments, tiles for the rest
+    if (packed || f32) {  // strip form for the segments with K <= 100, tiles for the rest
       for (int c = 0; c < G.mp_ncls; c++)
         FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
-                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st));
+                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st, f32));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles - G.mp_strip_tiles,
                                           packed, st, G.mp_strip_tiles));
     } else {
@@ -1424,8 +1424,9 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
   }
   const MpSegment *dseg = reinterpret_cast<const MpSegment *>(base + o_seg);
   // the strip form addresses C rows with 32-bit offsets within a 128-row strip
-  if (packed && K <= fapk::minplus_strip_max_k() && ldc < (1 << 24) && (!Cpath || ldcp < (1 << 24)))
-    FAP_CUDA(fapk::launch_minplus_strips(Cpath != nullptr, dseg, 1, mp_strips_of(s), K, st));
+  if ((packed || (!i32 && K > 0)) && K <= fapk::minplus_strip_max_k() && ldc < (1 << 24) &&
+      (!Cpath || ldcp < (1 << 24)))
+    FAP_CUDA(fapk::launch_minplus_strips(Cpath != nullptr, dseg, 1, mp_strips_of(s), K, st, !i32));
   else
     FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr, dseg, 1, tiles, packed, st));
   FAP_CUDA(cudaStreamSynchronize(st));

@@ -25,8 +25,9 @@ cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, i
 // K <= max_k <= minplus_strip_max_k(), CTAs numbered by
 // MpSegment::strip_begin (ceil(M / 128) x ceil(tiles_x / minplus_strip_tiles())
 // strips per segment).  Same preconditions as the packed tile form.
+// f32: FP32 distances (any range) instead of the packed int32 form.
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                                  int max_k, cudaStream_t st);
+                                  int max_k, cudaStream_t st, bool f32 = false);
 int minplus_strip_tiles();
 // Strip form of the FW remaining-tile phase (packed int32, init_from_c = 1,
 // K <= 64): CTAs numbered by MpSegment::strip_begin, tiles_y x

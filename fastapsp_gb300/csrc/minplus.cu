@@ -640,7 +640,9 @@ __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *s
 // Turns the B values this thread copied (same mapping as strip_load_rows)
 // into keys (d << 7) | (k + 1), and sets bit k of kmask (a 128-bit mask in
 // shared memory) for every row k that has a finite entry in the tile.
-template <int TN>
+// F32: the values stay (FP32 bits, "unreached" = the bits of 1e8); only the
+// row bits are set.
+template <int TN, bool F32 = false>
 __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kmask) {
   constexpr int TPR = TN / 4;
   const int t = threadIdx.x;
@@ -649,6 +651,11 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
     uint4 *p = reinterpret_cast<uint4 *>(Bs + kk * TN + j);
     const unsigned idx = (unsigned)(kk & kMaxPackedK) + 1u;
     uint4 v = *p;
+    if (F32) {
+      if (min(min(v.x, v.y), min(v.z, v.w)) < __float_as_uint(Dist<float>::inf()))
+        atomicOr(&kmask[kk >> 5], 1u << (kk & 31));
+      continue;
+    }
     const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < kPackH;
     v.x = (min(v.x, kPackH) << kIdxBits) | idx;
     v.y = (min(v.y, kPackH) << kIdxBits) | idx;
@@ -659,11 +666,31 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
   }
 }
 
+// One add-min of the strip kernel: packed keys (one DPX instruction), or
+// FP32 bits with the step idx of the last strict improvement kept in `arg`.
+template <bool F32>
+__device__ __forceinline__ void strip_addmin(unsigned &acc, int &arg, unsigned a, unsigned b, int idx) {
+  if constexpr (F32) {
+    const unsigned v = __float_as_uint(__uint_as_float(a) + __uint_as_float(b));
+    bool keep;
+    acc = __vibmin_u32(acc, v, &keep);
+    arg = keep ? arg : idx;
+  } else {
+    acc = __viaddmin_u32(a, b, acc);
+  }
+}
+
 // TN = 64 (the class K <= 48): 128x64 tiles, 8x4 outputs per thread, up to
 // three CTAs per SM.  TN = 128 (the class K <= 100): 128x128 tiles, 8x8
 // outputs per thread, up to two CTAs per SM.
-template <bool PRED, int TN>
-__global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
+// F32: FP32 distances (any range).  The product keeps each output's value
+// bits and the step idx (k + 1, 0 = none) of its last strict improvement in
+// two registers: fl(a + b), then __vibmin_u32 for the minimum and whether the
+// current value was kept (non-negative floats order like their bits) -- the
+// reference's strict-<, ascending-k rule, as in the packed form.  TN = 64
+// only, two CTAs per SM.
+template <bool PRED, int TN, bool F32 = false>
+__global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
     mp_strip_kernel(const MpSegment *__restrict__ segs, int nseg, int ks) {
   constexpr int CH = TN / 64;  // 64-column halves of a thread's outputs
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -697,7 +724,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
   const int jt1 = min(jt0 + kStripTiles * (128 / TN), (s.N + TN - 1) / TN);
   const int row0 = rt * kTile;
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-  const unsigned INF = Dist<uint32_t>::inf();
+  const unsigned INF = F32 ? __float_as_uint(Dist<float>::inf()) : Dist<uint32_t>::inf();
   const int kseg = (s.K + 3) & ~3;  // this segment's K rounded up to 4 (<= ks)
   const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
   const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
@@ -784,12 +811,12 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     if (jt == jt0)  // A keys; a warp converts 32 entries of one step k and marks finite ones
       for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
         const unsigned v = As[idx];
-        As[idx] = min(v, kPackH) << kIdxBits;
+        if (!F32) As[idx] = min(v, kPackH) << kIdxBits;
         const int kk = idx >> 7;
-        if (__any_sync(0xffffffffu, v < kPackH) && (threadIdx.x & 31) == 0)
+        if (__any_sync(0xffffffffu, F32 ? v < INF : v < kPackH) && (threadIdx.x & 31) == 0)
           atomicOr(&s_amask[kk >> 5], 1u << (kk & 31));
       }
-    strip_keys_b<TN>(Bcur, kseg, s_kmask[buf]);
+    strip_keys_b<TN, F32>(Bcur, kseg, s_kmask[buf]);
     // List the tile's own columns (threads 0..TN-1 copied their column's
     // flags; slots are taken in any order through a counter).
     if (threadIdx.x == 0) s_own[buf ^ 1] = 0;  // used by the next tile
@@ -846,10 +873,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
     cp_async_commit();
 
     unsigned acc[8][4 * CH];
+    int arg[8][4 * CH];  // F32: step idx of the last strict improvement (0: none)
 #pragma unroll
     for (int r = 0; r < 8; r++)
 #pragma unroll
-      for (int c = 0; c < 4 * CH; c++) acc[r][c] = kPackH << kIdxBits;
+      for (int c = 0; c < 4 * CH; c++) {
+        acc[r][c] = F32 ? INF : kPackH << kIdxBits;
+        arg[r][c] = 0;
+      }
     // When every step is active the loop runs over all k (unrolled);
     // otherwise it walks the set bits of the mask -- on graphs with limited
     // reachability most steps are skipped.  Either way the next step's
@@ -874,7 +905,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
 #pragma unroll
           for (int r = 0; r < 8; r++)
 #pragma unroll
-            for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+            for (int c = 0; c < 4 * CH; c++) strip_addmin<F32>(acc[r][c], arg[r][c], a[r], b[c], kk + 1);
         }
       } else if (nact > 0) {
         auto next_k = [&]() {  // lowest remaining step, or -1
@@ -898,6 +929,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
         while (kk >= 0) {
           const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
           const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
+          const int cur = kk;
           kk = next_k();
           const int kn = kk >= 0 ? kk : 0;
           na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
@@ -907,7 +939,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
 #pragma unroll
           for (int r = 0; r < 8; r++)
 #pragma unroll
-            for (int c = 0; c < 4 * CH; c++) acc[r][c] = __viaddmin_u32(a[r], b[c], acc[r][c]);
+            for (int c = 0; c < 4 * CH; c++) strip_addmin<F32>(acc[r][c], arg[r][c], a[r], b[c], cur + 1);
         }
       }
     }
@@ -942,13 +974,18 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 2 : 3)
         // no decode and no predecessor gathers
         const unsigned qmin = min(min(acc[r][h * 4], acc[r][h * 4 + 1]),
                                   min(acc[r][h * 4 + 2], acc[r][h * 4 + 3]));
-        if (qmin < (kPackH << kIdxBits)) {
+        if (qmin < (F32 ? INF : kPackH << kIdxBits)) {
 #pragma unroll
           for (int q = 0; q < 4; q++) {
             const unsigned key = acc[r][h * 4 + q];
-            const unsigned dist = key >> kIdxBits;
-            d[q] = dist >= kPackH ? INF : dist;
-            if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
+            if (F32) {
+              d[q] = key >= INF ? INF : key;
+              if (PRED) p[q] = Bps[arg[r][h * 4 + q] * TN + sc0 + q];
+            } else {
+              const unsigned dist = key >> kIdxBits;
+              d[q] = dist >= kPackH ? INF : dist;
+              if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
+            }
           }
         }
         if ((ownmask >> (h * 4)) & 0xfu) {
@@ -1711,11 +1748,11 @@ cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int tiles, int ti
   return cudaGetLastError();
 }
 
-template <bool PRED, int TN>
+template <bool PRED, int TN, bool F32 = false>
 cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks, cudaStream_t st) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
   ++launch_count();
-  mp_strip_kernel<PRED, TN><<<strips, kThreads, strip_smem_bytes<TN>(ks), st>>>(d_segs, nseg, ks);
+  mp_strip_kernel<PRED, TN, F32><<<strips, kThreads, strip_smem_bytes<TN>(ks), st>>>(d_segs, nseg, ks);
   return cudaGetLastError();
 }
 
@@ -1753,9 +1790,12 @@ cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, i
 }
 
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                                  int max_k, cudaStream_t st) {
+                                  int max_k, cudaStream_t st, bool f32) {
   if (max_k < 0 || max_k > kStripMaxK) return cudaErrorInvalidValue;
   const int ks = (max_k + 3) & ~3;
+  if (f32)  // 128 x 64 tiles at every K (the argmin registers leave no room for 128 x 128)
+    return pred ? launch_strip_t<true, 64, true>(d_segs, nseg, strips, ks, st)
+                : launch_strip_t<false, 64, true>(d_segs, nseg, strips, ks, st);
   if (max_k <= kStripClassK[0])
     return pred ? launch_strip_t<true, kStripClassTN[0]>(d_segs, nseg, strips, ks, st)
                 : launch_strip_t<false, kStripClassTN[0]>(d_segs, nseg, strips, ks, st);
@@ -1828,6 +1868,13 @@ cudaError_t init_minplus_kernels() {
     return e;
   if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, kStripClassTN[0]>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smax0)) != cudaSuccess)
+    return e;
+  const int smaxf = (int)strip_smem_bytes<64>((kStripMaxK + 3) & ~3);
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 64, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smaxf)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 64, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smaxf)) != cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, kStripClassTN[1]>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smax1)) != cudaSuccess)
