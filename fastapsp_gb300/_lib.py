@@ -28,6 +28,7 @@ MAXVALUE_F32 = 1e8
 OPT_SSSP_FP64 = 1
 OPT_SSSP_DELTA = 2
 OPT_AUTOTUNE = 3
+OPT_SSSP_LANES = 4
 INF_I32 = 1 << 30
 
 _i32 = C.c_int32

@@ -190,6 +190,7 @@ struct fap_engine {
   int sssp_fp64 = 0;       // FP32 engines: search in FP64
   double sssp_delta = 0;   // near-far threshold step; 0 = auto (tuned on first solve)
   int autotune = 1;        // tune the SSSP step on the first solve
+  int sssp_lanes = 0;      // sources per SSSP batch: 16, 32, 0 = chosen per solve
   double delta_try = 0;    // step under trial while tuning
   double tuned_ms = 0;     // SSSP time of the chosen step during tuning
   // device graph
@@ -209,6 +210,7 @@ struct fap_engine {
   DevBuf fw_d, fw_p;           // FW matrices arena
   DevBuf sssp_scratch, sssp_bits;
   int sssp_slots_alloc = 0;
+  bool sssp_wide = false;       // the scratch holds FP64 32-lane slots
   DevBuf res_d, res_p;         // device results when the caller passes host memory
   DevBuf bnd_d, bnd_p;         // boundary rows when the inner rows go straight to mapped host memory
   DevBuf small;                // tables of standalone calls
@@ -230,19 +232,27 @@ double sssp_delta_of(const fap_engine *e) {
   return e->f32() ? std::max(d, 1e-30) : std::max(1.0, std::floor(d));
 }
 
-int max_sssp_slots(fap_engine *e) {
+int max_sssp_slots(fap_engine *e, bool wide = false) {
   // Two 512-thread CTAs per SM, bounded by a 16 GiB scratch budget.
   int slots = std::max(1, 2 * e->sm_count);
-  size_t per = fapk::sssp_slot_bytes(e->n) + fapk::sssp_bits_bytes(e->n);
+  size_t per = fapk::sssp_slot_bytes(e->n, wide) + fapk::sssp_bits_bytes(e->n);
   size_t budget = (size_t)16 << 30;
   slots = (int)std::max<size_t>(1, std::min<size_t>((size_t)slots, budget / std::max<size_t>(per, 1)));
   return slots;
 }
 
-int ensure_sssp_scratch(fap_engine *e, int slots) {
+// wide: slots of the FP64 search with 32 lanes (twice the distance table);
+// sssp_slots_alloc counts slots of the layout last ensured.
+int ensure_sssp_scratch(fap_engine *e, int slots, bool wide = false) {
+  if (wide != e->sssp_wide) {
+    e->sssp_wide = wide;
+    size_t fit = e->sssp_scratch.bytes / fapk::sssp_slot_bytes(e->n, wide);
+    if (fapk::sssp_bits_bytes(e->n) > 0) fit = std::min(fit, e->sssp_bits.bytes / fapk::sssp_bits_bytes(e->n));
+    e->sssp_slots_alloc = (int)fit;
+  }
   if (slots <= e->sssp_slots_alloc) return FAP_OK;
   int st;
-  if ((st = e->sssp_scratch.ensure(fapk::sssp_slot_bytes(e->n) * slots)) != FAP_OK) return st;
+  if ((st = e->sssp_scratch.ensure(fapk::sssp_slot_bytes(e->n, wide) * slots)) != FAP_OK) return st;
   if ((st = e->sssp_bits.ensure(std::max<size_t>(fapk::sssp_bits_bytes(e->n) * slots, 4))) != FAP_OK)
     return st;
   e->sssp_slots_alloc = slots;
@@ -850,6 +860,7 @@ std::vector<const void *> buffer_signature(const fap_engine *e) {
   return {e->fw_d.p, e->fw_p.p, e->sssp_scratch.p, e->sssp_bits.p,
           reinterpret_cast<const void *>((intptr_t)e->sssp_slots_alloc),
           reinterpret_cast<const void *>((intptr_t)e->sssp_fp64),
+          reinterpret_cast<const void *>((intptr_t)e->sssp_lanes),
           reinterpret_cast<const void *>(dbits)};
 }
 
@@ -873,20 +884,21 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   int rc;
   // work buffers
   size_t fw_elems = 0;
-  int64_t batches32 = 0, sources = 0;
+  int64_t batches32 = 0;
   for (int p : parts) {
     size_t ld = align_up((size_t)e->ver_num[p], (size_t)fapk::fw_block());
     fw_elems += ld * ld;
     batches32 += (e->bdy_num[p] + 31) / 32;
-    sources += e->bdy_num[p];
   }
-  const int lanes = (e->f32() && e->sssp_fp64) ? 16 : fapk::sssp_lanes_for(sources, batches32, e->sm_count);
+  const int lanes = e->sssp_lanes ? e->sssp_lanes
+                                   : fapk::sssp_lanes_for(batches32, e->sm_count, e->f32() && e->sssp_fp64);
+  const bool wide = e->f32() && e->sssp_fp64 && lanes == 32;
   int max_batches = 0;
   for (int p : parts) max_batches += (e->bdy_num[p] + lanes - 1) / lanes;
   if ((rc = e->fw_d.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
   if (pred && (rc = e->fw_p.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
-  int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e));
-  if ((rc = ensure_sssp_scratch(e, slots)) != FAP_OK) return rc;
+  int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e, wide));
+  if ((rc = ensure_sssp_scratch(e, slots, wide)) != FAP_OK) return rc;
 
   Plan *pl = find_plan(e, mode, dist, pred, parts, offs, bdist, bpred);
   if (!pl) {
@@ -1561,9 +1573,9 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   std::lock_guard<std::mutex> lk(e->mu);
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
-  const int lanes = (e->f32() && e->sssp_fp64)
-                        ? 16
-                        : fapk::sssp_lanes_for(num_sources, (num_sources + 31) / 32, e->sm_count);
+  const bool acc64 = e->f32() && e->sssp_fp64;
+  const int lanes = e->sssp_lanes ? e->sssp_lanes : fapk::sssp_lanes_for((num_sources + 31) / 32, e->sm_count, acc64);
+  const bool wide = acc64 && lanes == 32;
   std::vector<SsspBatch> batches;
   for (int b0 = 0; b0 < num_sources; b0 += lanes) {
     SsspBatch sb{};
@@ -1575,8 +1587,8 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
     batches.push_back(sb);
   }
   int rc;
-  int slots = std::min((int)batches.size(), max_sssp_slots(e));
-  if ((rc = ensure_sssp_scratch(e, slots)) != FAP_OK) return rc;
+  int slots = std::min((int)batches.size(), max_sssp_slots(e, wide));
+  if ((rc = ensure_sssp_scratch(e, slots, wide)) != FAP_OK) return rc;
   if ((rc = e->small.ensure(batches.size() * sizeof(SsspBatch))) != FAP_OK) return rc;
   FAP_CUDA(cudaMemcpyAsync(e->small.p, batches.data(), batches.size() * sizeof(SsspBatch),
                            cudaMemcpyHostToDevice, st));
@@ -1599,7 +1611,7 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   sa.maxd = nullptr;
   sa.iter_cap = 8 * e->n + 64;
   sa.lanes = lanes;
-  sa.acc64 = e->f32() && e->sssp_fp64;
+  sa.acc64 = acc64;
   sa.delta = sssp_delta_of(e);
   FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
   FAP_CUDA(cudaStreamSynchronize(st));
@@ -1668,6 +1680,11 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
     case FAP_OPT_AUTOTUNE:
       e->autotune = value != 0.0 ? 1 : 0;
       return FAP_OK;
+    case FAP_OPT_SSSP_LANES:
+      if (value != 0.0 && value != 16.0 && value != 32.0)
+        return set_error(FAP_ERR_INVALID, "SSSP lanes must be 0, 16 or 32");
+      e->sssp_lanes = (int)value;
+      return FAP_OK;
     default:
       return set_error(FAP_ERR_INVALID, "unknown option");
   }
@@ -1679,6 +1696,7 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_SSSP_FP64: *value = e->sssp_fp64; return FAP_OK;
     case FAP_OPT_SSSP_DELTA: *value = sssp_delta_of(e); return FAP_OK;
     case FAP_OPT_AUTOTUNE: *value = e->autotune; return FAP_OK;
+    case FAP_OPT_SSSP_LANES: *value = e->sssp_lanes; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");
   }
 }

@@ -69,7 +69,7 @@ struct SsspArgs {
   int32_t nbatches;
   void *dist;                 // output base (rows addressed by SsspBatch::row_off)
   int32_t *pred;              // may be null
-  void *scratch;              // per-slot scratch, sssp_slot_bytes(n) each
+  void *scratch;              // per-slot scratch, sssp_slot_bytes(n, acc64 && lanes == 32) each
   int32_t slots;              // number of CTAs (= scratch slots)
   void *bits;                 // slots * sssp_bits_bytes(n): frontier bitmaps that do
                               // not fit in shared memory (null when that is 0)
@@ -77,7 +77,7 @@ struct SsspArgs {
   unsigned *maxd;             // largest finite int32 distance written (atomicMax), may be null
   int32_t iter_cap;           // steps (near-frontier sweeps + far splits) per batch
   int32_t lanes;              // sources per batch: 16 or 32 (batches hold <= lanes)
-  int32_t acc64;              // FP32 weights searched in FP64 (lanes must be 16)
+  int32_t acc64;              // FP32 weights searched in FP64 (8-byte entries)
   double delta;               // near-far threshold step (> 0; huge = plain Bellman-Ford)
   unsigned long long *stats;  // may be null: [near steps, far splits, frontier
                               // vertices relaxed, far entries scanned, batches]
@@ -86,10 +86,10 @@ struct SsspArgs {
 // delta value that puts every vertex in the near frontier (plain frontier BF)
 constexpr double kSsspNoDelta = 2147483647.0;
 cudaError_t init_sssp_kernels();
-size_t sssp_slot_bytes(int32_t n);
+size_t sssp_slot_bytes(int32_t n, bool wide = false);  // wide: FP64 search with 32 lanes
 size_t sssp_bits_bytes(int32_t n);  // per slot; 0 when the bitmaps fit in shared memory
-// Batch width to use given the number of 32-source batches the work needs.
-int sssp_lanes_for(int64_t sources_total, int64_t batches32, int sm_count);
+// Batch width (16 or 32 sources) given the 32-source batches the work needs.
+int sssp_lanes_for(int64_t batches32, int sm_count, bool acc64);
 int sssp_threads();
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st);
 

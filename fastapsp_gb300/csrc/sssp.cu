@@ -52,10 +52,11 @@ constexpr int kSsspThreads = 512;
 constexpr int kSsspWarps = kSsspThreads / 32;
 constexpr int kOutThreads = 256;  // the separate output kernel
 
-// dvm (n x 32 four-byte or n x 16 eight-byte entries) + near/far frontiers
-// (2 + 2), n ints each.
-__host__ __device__ inline size_t slot_bytes(int32_t n) {
-  size_t b = (size_t)n * 32 * 4 + (size_t)n * 4 * 4;
+// dvm (n x 32 four-byte or n x 16 eight-byte entries; wide: n x 32
+// eight-byte entries) + near/far frontiers (2 + 2), n ints each.
+__host__ __device__ inline size_t dvm_bytes(int32_t n, bool wide) { return (size_t)n * (wide ? 256 : 128); }
+__host__ __device__ inline size_t slot_bytes(int32_t n, bool wide = false) {
+  size_t b = dvm_bytes(n, wide) + (size_t)n * 4 * 4;
   return (b + 255) & ~(size_t)255;
 }
 
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(kOutThreads)
   OutTile<LANES> &tile = reinterpret_cast<OutTile<LANES> *>(out_smem_raw)[warp];
   const int b = blockIdx.y;
   const K *dvm = reinterpret_cast<const K *>(static_cast<const unsigned char *>(a.scratch) +
-                                             (size_t)b * slot_bytes(a.n));
+                                             (size_t)b * slot_bytes(a.n, ACC64 && LANES == 32));
   const int cnt = a.batches[b].count;
   const int sl = lane % LANES;
   const int my_src = sl < cnt ? a.batches[b].src[sl] : -1;
@@ -235,10 +236,11 @@ __global__ void __launch_bounds__(kSsspThreads)
   const int sub = lane / LANES, sl = lane % LANES;
   const unsigned group_mask = LANES == 32 ? 0xffffffffu : (0xffffu << (16 * sub));
   const int32_t n = a.n;
-  unsigned char *base = static_cast<unsigned char *>(a.scratch) + (size_t)blockIdx.x * slot_bytes(n);
+  constexpr bool kWide = ACC64 && LANES == 32;
+  unsigned char *base = static_cast<unsigned char *>(a.scratch) + (size_t)blockIdx.x * slot_bytes(n, kWide);
   K *dvm = reinterpret_cast<K *>(base);
   // near frontiers at nearq0 + {0, n}, far lists at farq0 + {0, n}
-  int32_t *const nearq0 = reinterpret_cast<int32_t *>(base + (size_t)n * 32 * 4);
+  int32_t *const nearq0 = reinterpret_cast<int32_t *>(base + dvm_bytes(n, kWide));
   int32_t *const farq0 = nearq0 + 2 * (size_t)n;
   const unsigned *wb = static_cast<const unsigned *>(a.w);
   const K INF = A::inf();
@@ -494,7 +496,8 @@ cudaError_t launch_one(const SsspArgs &a0, cudaStream_t st) {
 template <typename T, bool PRED>
 cudaError_t launch_t(const SsspArgs &a, cudaStream_t st) {
   if (a.acc64) {
-    if constexpr (std::is_same<T, float>::value) return launch_one<float, PRED, 16, true>(a, st);
+    if constexpr (std::is_same<T, float>::value)
+      return a.lanes == 16 ? launch_one<float, PRED, 16, true>(a, st) : launch_one<float, PRED, 32, true>(a, st);
     return cudaErrorInvalidValue;
   }
   if (a.lanes == 16) return launch_one<T, PRED, 16, false>(a, st);
@@ -513,7 +516,7 @@ cudaError_t set_attr() {
 
 }  // namespace
 
-size_t sssp_slot_bytes(int32_t n) { return slot_bytes(n); }
+size_t sssp_slot_bytes(int32_t n, bool wide) { return slot_bytes(n, wide); }
 size_t sssp_bits_bytes(int32_t n) { return bitmap_bytes(n) <= kBitmapSmemMax ? 0 : bitmap_bytes(n); }
 int sssp_threads() { return kSsspThreads; }
 
@@ -531,6 +534,8 @@ cudaError_t init_sssp_kernels() {
   FAP_SSSP_ATTR(uint32_t, false, 32, false)
   FAP_SSSP_ATTR(float, true, 16, true)
   FAP_SSSP_ATTR(float, false, 16, true)
+  FAP_SSSP_ATTR(float, true, 32, true)
+  FAP_SSSP_ATTR(float, false, 32, true)
 #undef FAP_SSSP_ATTR
   return cudaSuccess;
 }
@@ -538,17 +543,20 @@ cudaError_t init_sssp_kernels() {
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st) {
   if (a.nbatches <= 0 || a.slots <= 0) return cudaSuccess;
   if (a.lanes != 16 && a.lanes != 32) return cudaErrorInvalidValue;
-  if (a.acc64 && (!f32 || a.lanes != 16)) return cudaErrorInvalidValue;
+  if (a.acc64 && !f32) return cudaErrorInvalidValue;
   if (!(a.delta > 0.0)) return cudaErrorInvalidValue;
   const bool pred = a.pred != nullptr;
   if (f32) return pred ? launch_t<float, true>(a, st) : launch_t<float, false>(a, st);
   return pred ? launch_t<uint32_t, true>(a, st) : launch_t<uint32_t, false>(a, st);
 }
 
-int sssp_lanes_for(int64_t sources_total, int64_t batches32, int sm_count) {
+int sssp_lanes_for(int64_t batches32, int sm_count, bool acc64) {
   // Half-warp batches double the CTA count and the frontier vertices a warp
-  // relaxes at once; worth it while 32-source batches leave SMs idle.
-  (void)sources_total;
+  // relaxes at once; worth it while 32-source batches leave SMs idle.  The
+  // FP64 search always takes 16: on the 114,599-vertex road-like graph with
+  // 128 parts, 129 batches of 32 in one wave searched in 431 ms against
+  // 225 ms for 258 batches of 16 in two waves.
+  if (acc64) return 16;
   return batches32 < 2LL * sm_count ? 16 : 32;
 }
 

@@ -163,10 +163,14 @@ int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode,
  *                      (multiples of the mean edge weight, and plain
  *                      Bellman-Ford) and keeps the fastest; fap_get_option
  *                      then reports the chosen step.  0 = 8 x the mean weight.
+ *   FAP_OPT_SSSP_LANES sources per SSSP batch (one CTA each): 16 or 32, or 0
+ *                      (default) = chosen per solve from the batch count.
+ *                      Changes speed only, never results.
  * Setting an option takes effect from the next solve. */
 #define FAP_OPT_SSSP_FP64 1
 #define FAP_OPT_SSSP_DELTA 2
 #define FAP_OPT_AUTOTUNE 3
+#define FAP_OPT_SSSP_LANES 4
 int fap_set_option(fap_engine *e, int32_t option, double value);
 int fap_get_option(const fap_engine *e, int32_t option, double *value);
 

@@ -137,8 +137,8 @@ def test_sssp_matches_dijkstra_bit_for_bit(gpu, oracle_lib, kind):
 
 @pytest.mark.parametrize("kind", ["grid", "road_f32"])
 def test_sssp_result_independent_of_near_far_step(gpu, oracle_lib, kind):
-    """The near-far step only orders the work: any step gives the reference
-    Dijkstra's distances and predecessors."""
+    """The near-far step and the batch width only order the work: any of
+    them gives the reference Dijkstra's distances and predecessors."""
     if kind == "grid":
         g, dtype = graphs.grid_graph(30, 30, seed=2), gpu.DTYPE_I32
     else:
@@ -147,8 +147,10 @@ def test_sssp_result_independent_of_near_far_step(gpu, oracle_lib, kind):
     dt = torch.int32 if dtype == gpu.DTYPE_I32 else torch.float32
     outs = []
     with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=dtype) as eng:
-        for delta in (1e-3 if dtype == gpu.DTYPE_F32 else 1, 0.0, 1e9):
+        lo = 1e-3 if dtype == gpu.DTYPE_F32 else 1
+        for delta, lanes in ((lo, 0), (0.0, 0), (1e9, 0), (0.0, 16), (0.0, 32)):
             eng.set_option(gpu._lib.OPT_SSSP_DELTA, delta)
+            eng.set_option(gpu._lib.OPT_SSSP_LANES, lanes)
             d = torch.empty((len(src), g.n), dtype=dt, device="cuda")
             p = torch.empty((len(src), g.n), dtype=torch.int32, device="cuda")
             eng.sssp(src, d, p)
@@ -182,12 +184,15 @@ def test_sssp_large_graph_bitmaps_in_global_memory(gpu, oracle_lib):
         assert np.array_equal(p[i], rp), f"pred row {i}"
 
 
-def test_sssp_fp64_option_rounds_once(gpu, oracle_lib):
-    """With FP64 search the FP32 output is the FP64 distance rounded once."""
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_sssp_fp64_option_rounds_once(gpu, oracle_lib, lanes):
+    """With FP64 search the FP32 output is the FP64 distance rounded once
+    (16-source batches by default, 32-source batches forced)."""
     g = graphs.road_like(4000, seed=8)
     src = np.random.default_rng(2).choice(g.n, size=33, replace=False).astype(np.int32)
     with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=gpu.DTYPE_F32) as eng:
         eng.set_option(gpu._lib.OPT_SSSP_FP64, 1)
+        eng.set_option(gpu._lib.OPT_SSSP_LANES, lanes)
         d = torch.empty((len(src), g.n), dtype=torch.float32, device="cuda")
         p = torch.empty((len(src), g.n), dtype=torch.int32, device="cuda")
         eng.sssp(src, d, p)
@@ -203,11 +208,13 @@ def test_sssp_fp64_option_rounds_once(gpu, oracle_lib):
     check_pred_tight(d.astype(np.float64), p, src, n, g.row_offset, g.col_val, g.weight, rtol=1e-6)
 
 
-def test_engine_fp64_sssp_option_meets_1e6_on_road_graph(gpu, oracle_lib):
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_engine_fp64_sssp_option_meets_1e6_on_road_graph(gpu, oracle_lib, lanes):
     g = graphs.road_like(6000, seed=12)
     K = 8
     with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, K, dtype=gpu.DTYPE_F32) as eng:
         eng.set_option(gpu._lib.OPT_SSSP_FP64, 1)
+        eng.set_option(gpu._lib.OPT_SSSP_LANES, lanes)
         n = g.n
         d = torch.empty((n, n), dtype=torch.float32, device="cuda")
         p = torch.empty((n, n), dtype=torch.int32, device="cuda")
