@@ -29,6 +29,7 @@ OPT_SSSP_FP64 = 1
 OPT_SSSP_DELTA = 2
 OPT_AUTOTUNE = 3
 OPT_SSSP_LANES = 4
+OPT_TILE_COLS = 5
 INF_I32 = 1 << 30
 
 _i32 = C.c_int32

@@ -142,6 +142,7 @@ struct Plan {
     int mp_ncls = 0, mp_strip_tiles = 0;
     int mp_cls_first[kMaxCls] = {}, mp_cls_nseg[kMaxCls] = {};
     int mp_cls_strips[kMaxCls] = {}, mp_cls_max_k[kMaxCls] = {};
+    int mp_cls_cols[kMaxCls] = {};  // tile columns the tuner chose (0: the class default)
     int max_sub = 0;  // largest part of the group (bound of the packed form)
   };
   std::vector<Group> groups;
@@ -191,6 +192,7 @@ struct fap_engine {
   double sssp_delta = 0;   // near-far threshold step; 0 = auto (tuned on first solve)
   int autotune = 1;        // tune the SSSP step on the first solve
   int sssp_lanes = 0;      // sources per SSSP batch: 16, 32, 0 = chosen per solve
+  int tile_cols = 0;       // min-plus strip tile columns: 64, 128, 0 = per class
   double delta_try = 0;    // step under trial while tuning
   double tuned_ms = 0;     // SSSP time of the chosen step during tuning
   // device graph
@@ -737,7 +739,8 @@ struct Issuer {
     if (packed || f32) {  // strip form for the segments with K <= 100, tiles for the rest
       for (int c = 0; c < G.mp_ncls; c++)
         FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
-                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st, f32));
+                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st, f32,
+                                             e->tile_cols ? e->tile_cols : G.mp_cls_cols[c]));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles - G.mp_strip_tiles,
                                           packed, st, G.mp_strip_tiles));
     } else {
@@ -813,6 +816,61 @@ int autotune_sssp(fap_engine *e, Plan &pl, cudaStream_t st) {
   return FAP_OK;
 }
 
+// Tile autotuner of the packed min-plus (strip form): on a plan's first run,
+// once the product's inputs are in place (closed FW matrices, boundary
+// rows), times every strip class launch of every group with 128 x 64 and
+// 128 x 128 tiles (best of two launches each) and keeps the faster for the
+// plan's later runs and its CUDA graph.  The product is a pure function of
+// those inputs -- the part's own columns come from its FW matrix, every
+// other output from the product, whatever the output held -- so the trial
+// launches rewrite the same rows.  Not run for results in mapped host
+// memory, where the host link bounds every tile width.
+int autotune_tiles(fap_engine *e, Plan &pl, cudaStream_t st) {
+  if (pl.pack != 1 || pl.bdist != nullptr) return FAP_OK;
+  const bool pred = pl.pred != nullptr;
+  cudaEvent_t a, b;
+  FAP_CUDA(cudaEventCreate(&a));
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return set_error(FAP_ERR_CUDA, "autotune: event failed");
+  }
+  int rc = FAP_OK;
+  for (auto &G : pl.groups) {
+    for (int c = 0; c < G.mp_ncls && rc == FAP_OK; c++) {
+      if (G.mp_cls_strips[c] <= 0) continue;
+      float best_ms = 1e30f;
+      int best = 0;
+      for (int cols : {64, 128}) {
+        float t = 1e30f;
+        for (int rep = 0; rep < 2 && rc == FAP_OK; rep++) {
+          cudaError_t ce = cudaEventRecord(a, st);
+          if (ce == cudaSuccess)
+            ce = fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
+                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st, false, cols);
+          if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
+          if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
+          float ms = 0;
+          if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, a, b);
+          if (ce != cudaSuccess) {
+            rc = set_error(FAP_ERR_CUDA, std::string("tile autotune: ") + cudaGetErrorString(ce));
+            break;
+          }
+          t = std::min(t, ms);
+        }
+        if (rc == FAP_OK && t < best_ms) {
+          best_ms = t;
+          best = cols;
+        }
+      }
+      G.mp_cls_cols[c] = best;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc != FAP_OK) return rc;
+  return check_status(e);
+}
+
 // Decides the packed int32 form for a plan on its first run: runs every
 // group's SSSP, reads back the largest finite SSSP distance, and checks the
 // bound of every finite result: a path inside a part to its first boundary
@@ -861,6 +919,7 @@ std::vector<const void *> buffer_signature(const fap_engine *e) {
           reinterpret_cast<const void *>((intptr_t)e->sssp_slots_alloc),
           reinterpret_cast<const void *>((intptr_t)e->sssp_fp64),
           reinterpret_cast<const void *>((intptr_t)e->sssp_lanes),
+          reinterpret_cast<const void *>((intptr_t)e->tile_cols),
           reinterpret_cast<const void *>(dbits)};
 }
 
@@ -920,7 +979,9 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   }
   if (pl->pack < 0) {
     if (e->autotune && e->sssp_delta <= 0 && (rc = autotune_sssp(e, *pl, st)) != FAP_OK) return rc;
-    return first_run(e, *pl, st);
+    if ((rc = first_run(e, *pl, st)) != FAP_OK) return rc;
+    if (e->autotune && e->tile_cols == 0) return autotune_tiles(e, *pl, st);
+    return FAP_OK;
   }
   if (mode == FAP_MODE_BATCHED) {
     if (!pl->exec) {
@@ -1438,7 +1499,8 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
   // the strip form addresses C rows with 32-bit offsets within a 128-row strip
   if ((packed || (!i32 && K > 0)) && K <= fapk::minplus_strip_max_k() && ldc < (1 << 24) &&
       (!Cpath || ldcp < (1 << 24)))
-    FAP_CUDA(fapk::launch_minplus_strips(Cpath != nullptr, dseg, 1, mp_strips_of(s), K, st, !i32));
+    FAP_CUDA(fapk::launch_minplus_strips(Cpath != nullptr, dseg, 1, mp_strips_of(s), K, st, !i32,
+                                         e->tile_cols));
   else
     FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr, dseg, 1, tiles, packed, st));
   FAP_CUDA(cudaStreamSynchronize(st));
@@ -1685,6 +1747,11 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
         return set_error(FAP_ERR_INVALID, "SSSP lanes must be 0, 16 or 32");
       e->sssp_lanes = (int)value;
       return FAP_OK;
+    case FAP_OPT_TILE_COLS:
+      if (value != 0.0 && value != 64.0 && value != 128.0)
+        return set_error(FAP_ERR_INVALID, "tile columns must be 0, 64 or 128");
+      e->tile_cols = (int)value;
+      return FAP_OK;
     default:
       return set_error(FAP_ERR_INVALID, "unknown option");
   }
@@ -1697,6 +1764,7 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_SSSP_DELTA: *value = sssp_delta_of(e); return FAP_OK;
     case FAP_OPT_AUTOTUNE: *value = e->autotune; return FAP_OK;
     case FAP_OPT_SSSP_LANES: *value = e->sssp_lanes; return FAP_OK;
+    case FAP_OPT_TILE_COLS: *value = e->tile_cols; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");
   }
 }

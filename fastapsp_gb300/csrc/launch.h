@@ -26,8 +26,11 @@ cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, i
 // MpSegment::strip_begin (ceil(M / 128) x ceil(tiles_x / minplus_strip_tiles())
 // strips per segment).  Same preconditions as the packed tile form.
 // f32: FP32 distances (any range) instead of the packed int32 form.
+// tile_cols (packed form): 64 or 128-column tiles, 0 = the default of the
+// K class (minplus_strip_class_cols); the FP32 form always takes 64.
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                                  int max_k, cudaStream_t st, bool f32 = false);
+                                  int max_k, cudaStream_t st, bool f32 = false, int tile_cols = 0);
+int minplus_strip_class_cols(int c);
 int minplus_strip_tiles();
 // Strip form of the FW remaining-tile phase (packed int32, init_from_c = 1,
 // K <= 64): CTAs numbered by MpSegment::strip_begin, tiles_y x

@@ -1790,17 +1790,20 @@ cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, i
 }
 
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                                  int max_k, cudaStream_t st, bool f32) {
+                                  int max_k, cudaStream_t st, bool f32, int tile_cols) {
   if (max_k < 0 || max_k > kStripMaxK) return cudaErrorInvalidValue;
   const int ks = (max_k + 3) & ~3;
   if (f32)  // 128 x 64 tiles at every K (the argmin registers leave no room for 128 x 128)
     return pred ? launch_strip_t<true, 64, true>(d_segs, nseg, strips, ks, st)
                 : launch_strip_t<false, 64, true>(d_segs, nseg, strips, ks, st);
-  if (max_k <= kStripClassK[0])
-    return pred ? launch_strip_t<true, kStripClassTN[0]>(d_segs, nseg, strips, ks, st)
-                : launch_strip_t<false, kStripClassTN[0]>(d_segs, nseg, strips, ks, st);
-  return pred ? launch_strip_t<true, kStripClassTN[1]>(d_segs, nseg, strips, ks, st)
-              : launch_strip_t<false, kStripClassTN[1]>(d_segs, nseg, strips, ks, st);
+  const int tn = tile_cols ? tile_cols : kStripClassTN[max_k <= kStripClassK[0] ? 0 : 1];
+  if (tn == 64)
+    return pred ? launch_strip_t<true, 64>(d_segs, nseg, strips, ks, st)
+                : launch_strip_t<false, 64>(d_segs, nseg, strips, ks, st);
+  if (tn == 128)
+    return pred ? launch_strip_t<true, 128>(d_segs, nseg, strips, ks, st)
+                : launch_strip_t<false, 128>(d_segs, nseg, strips, ks, st);
+  return cudaErrorInvalidValue;
 }
 
 int minplus_strip_tiles() { return kStripTiles; }
@@ -1814,6 +1817,7 @@ int fw_strip_tiles() { return kFwStripTiles; }
 int minplus_strip_max_k() { return kStripMaxK; }
 int minplus_strip_classes() { return kStripClasses; }
 int minplus_strip_class_k(int c) { return c >= 0 && c < kStripClasses ? kStripClassK[c] : -1; }
+int minplus_strip_class_cols(int c) { return c >= 0 && c < kStripClasses ? kStripClassTN[c] : -1; }
 
 cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cudaStream_t st) {
   if (nmats <= 0) return cudaSuccess;
@@ -1861,12 +1865,14 @@ cudaError_t init_minplus_kernels() {
   if ((e = set_mp_attr<uint32_t, false>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<true>()) != cudaSuccess) return e;
   if ((e = set_packed_attr<false>()) != cudaSuccess) return e;
-  const int smax0 = (int)strip_smem_bytes<kStripClassTN[0]>((kStripClassK[0] + 3) & ~3);
-  const int smax1 = (int)strip_smem_bytes<kStripClassTN[1]>((kStripClassK[1] + 3) & ~3);
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, kStripClassTN[0]>,
+  // either tile width serves any K of the strip form (tile_cols)
+  static_assert(kStripClassTN[0] == 64 && kStripClassTN[1] == 128, "strip tile widths");
+  const int smax0 = (int)strip_smem_bytes<64>((kStripMaxK + 3) & ~3);
+  const int smax1 = (int)strip_smem_bytes<128>((kStripMaxK + 3) & ~3);
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 64>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smax0)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, kStripClassTN[0]>,
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 64>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smax0)) != cudaSuccess)
     return e;
   const int smaxf = (int)strip_smem_bytes<64>((kStripMaxK + 3) & ~3);
@@ -1876,10 +1882,10 @@ cudaError_t init_minplus_kernels() {
   if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 64, true>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smaxf)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, kStripClassTN[1]>,
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 128>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smax1)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, kStripClassTN[1]>,
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 128>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smax1)) != cudaSuccess)
     return e;
 

@@ -166,11 +166,18 @@ int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode,
  *   FAP_OPT_SSSP_LANES sources per SSSP batch (one CTA each): 16 or 32, or 0
  *                      (default) = chosen per solve from the batch count.
  *                      Changes speed only, never results.
+ *   FAP_OPT_TILE_COLS  column width of the packed int32 min-plus tiles (128
+ *                      rows): 64 or 128, or 0 (default) = chosen per K class
+ *                      of each plan: while FAP_OPT_AUTOTUNE is on, the first
+ *                      run times both widths and keeps the faster (not for
+ *                      results in mapped host memory); otherwise 64 for
+ *                      K <= 48 and 128 above.  Changes speed only.
  * Setting an option takes effect from the next solve. */
 #define FAP_OPT_SSSP_FP64 1
 #define FAP_OPT_SSSP_DELTA 2
 #define FAP_OPT_AUTOTUNE 3
 #define FAP_OPT_SSSP_LANES 4
+#define FAP_OPT_TILE_COLS 5
 int fap_set_option(fap_engine *e, int32_t option, double value);
 int fap_get_option(const fap_engine *e, int32_t option, double *value);
 
