@@ -109,6 +109,10 @@ struct Plan {
     // SSSP
     const SsspBatch *batches = nullptr;
     int nbatches = 0;
+    // the same sources in batches of the other width (sssp_lanes_alt), for
+    // the autotuner; swapped with the above when that width wins
+    const SsspBatch *batches_alt = nullptr;
+    int nbatches_alt = 0;
     // build / decode
     const PartDesc *pdesc = nullptr;
     const int64_t *row_begin = nullptr;
@@ -151,6 +155,7 @@ struct Plan {
   int max_mp_k = 0;     // largest min-plus K (boundary count) of the plan
   int pack = -1;        // packed int32 form: -1 undecided, 0 no, 1 yes
   int sssp_lanes = 32;  // sources per SSSP batch
+  int sssp_lanes_alt = 0;  // the other width the autotuner tries (0: none)
   int launches = 0;     // kernels one run of the plan launches
   // graph (batched mode)
   cudaGraphExec_t exec = nullptr;
@@ -192,6 +197,7 @@ struct fap_engine {
   double sssp_delta = 0;   // near-far threshold step; 0 = auto (tuned on first solve)
   int autotune = 1;        // tune the SSSP step on the first solve
   int sssp_lanes = 0;      // sources per SSSP batch: 16, 32, 0 = chosen per solve
+  int sssp_lanes_tuned = 0;  // the width the autotuner chose (0: none yet)
   int tile_cols = 0;       // min-plus strip tile columns: 64, 128, 0 = per class
   double delta_try = 0;    // step under trial while tuning
   double tuned_ms = 0;     // SSSP time of the chosen step during tuning
@@ -412,7 +418,7 @@ int build_plan(fap_engine *e, Plan &pl) {
 
   TableBuilder tb;
   struct GroupOffs {
-    size_t batches, pdesc, row_begin, dec_begin, mp;
+    size_t batches, batches_alt, pdesc, row_begin, dec_begin, mp;
     std::vector<size_t> diag, panel, rest, rest2;
   };
   std::vector<GroupOffs> goffs(groups.size());
@@ -421,7 +427,7 @@ int build_plan(fap_engine *e, Plan &pl) {
     Plan::Group &G = pl.groups[g];
     GroupOffs &O = goffs[g];
     // SSSP batches: per part, its boundary vertices in mapping order.
-    std::vector<SsspBatch> batches;
+    std::vector<SsspBatch> batches, batches_alt;
     std::vector<PartDesc> pdesc;
     std::vector<int64_t> row_begin(1, 0), dec_begin(1, 0);
     // min-plus segments: the strip form's classes of K in order, then those
@@ -434,15 +440,17 @@ int build_plan(fap_engine *e, Plan &pl) {
       int sub = e->ver_num[p], bdy = e->bdy_num[p], start = e->ver_offset[p];
       int64_t roff = pl.row_offs[idx];
       int64_t boff = pl.bdist ? pl.brow_offs[idx] : roff;  // first boundary row
-      const int L = pl.sssp_lanes;
-      for (int b0 = 0; b0 < bdy; b0 += L) {
-        SsspBatch sb{};
-        sb.count = std::min(L, bdy - b0);
-        for (int l = 0; l < sb.count; l++) {
-          sb.src[l] = e->st2ed[start + b0 + l];
-          sb.row_off[l] = boff + (int64_t)(b0 + l) * n;
+      for (int w = 0; w < 2; w++) {
+        const int L = w == 0 ? pl.sssp_lanes : pl.sssp_lanes_alt;
+        for (int b0 = 0; L > 0 && b0 < bdy; b0 += L) {
+          SsspBatch sb{};
+          sb.count = std::min(L, bdy - b0);
+          for (int l = 0; l < sb.count; l++) {
+            sb.src[l] = e->st2ed[start + b0 + l];
+            sb.row_off[l] = boff + (int64_t)(b0 + l) * n;
+          }
+          (w == 0 ? batches : batches_alt).push_back(sb);
         }
-        batches.push_back(sb);
       }
       if (sub == 0) continue;
       G.max_sub = std::max(G.max_sub, sub);
@@ -488,6 +496,8 @@ int build_plan(fap_engine *e, Plan &pl) {
     }
     G.nbatches = (int)batches.size();
     O.batches = tb.add(batches.data(), batches.size());
+    G.nbatches_alt = (int)batches_alt.size();
+    O.batches_alt = tb.add(batches_alt.data(), batches_alt.size());
     G.nparts = (int)pdesc.size();
     G.total_rows = row_begin.back();
     G.dec_rows = dec_begin.back();
@@ -589,6 +599,7 @@ int build_plan(fap_engine *e, Plan &pl) {
     Plan::Group &G = pl.groups[g];
     GroupOffs &O = goffs[g];
     G.batches = reinterpret_cast<const SsspBatch *>(base + O.batches);
+    G.batches_alt = reinterpret_cast<const SsspBatch *>(base + O.batches_alt);
     G.pdesc = reinterpret_cast<const PartDesc *>(base + O.pdesc);
     G.row_begin = reinterpret_cast<const int64_t *>(base + O.row_begin);
     G.dec_begin = reinterpret_cast<const int64_t *>(base + O.dec_begin);
@@ -770,40 +781,67 @@ struct Issuer {
 int check_status(fap_engine *e);
 std::vector<const void *> buffer_signature(const fap_engine *e);
 
-// SSSP step autotuner: times the plan's SSSP phase (every group) with a few
+// SSSP autotuner: times the plan's SSSP phase (every group) with a few
 // near-far steps -- multiples of the mean edge weight from 4 to 128, and
-// plain frontier Bellman-Ford -- and keeps the fastest.  The step only orders the work, so
-// every candidate produces the same rows.  Runs once per engine, on the first
-// run of a plan, when the step was left automatic.
+// plain frontier Bellman-Ford -- and keeps the fastest; then, when the plan
+// carries batches of the other width (16 sources, two lane groups a warp, or
+// 32, one), times both widths at that step (best of two runs each) and keeps
+// the faster.  Step and width only order the work, so every candidate
+// produces the same rows.  Runs once per engine, on the first run of a plan,
+// when the step was left automatic; later plans take the chosen step and width.
 int autotune_sssp(fap_engine *e, Plan &pl, cudaStream_t st) {
   const double unit = e->f32() ? e->wmean : std::max(1.0, e->wmean);
   const double factors[] = {4.0, 8.0, 16.0, 24.0, 32.0, 48.0, 64.0, 128.0, 0.0};
   double best = 0, best_ms = 1e300;
-  cudaEvent_t t0 = e->ev_sync[0], t1 = e->ev_sync[1];
   cudaEvent_t a, b;
   FAP_CUDA(cudaEventCreate(&a));
-  FAP_CUDA(cudaEventCreate(&b));
-  (void)t0;
-  (void)t1;
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return set_error(FAP_ERR_CUDA, "autotune: event failed");
+  }
   int rc = FAP_OK;
+  auto time_phase = [&](double d, float &ms) {  // the SSSP phase at step d
+    e->delta_try = d;
+    Issuer is{e, pl, st, false};
+    if (cudaEventRecord(a, st) != cudaSuccess) return set_error(FAP_ERR_CUDA, "autotune: event failed");
+    for (size_t g = 0; g < pl.groups.size(); g++) {
+      int r = is.sssp(g);
+      if (r != FAP_OK) return r;
+    }
+    if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+      return set_error(FAP_ERR_CUDA, "autotune: event failed");
+    return FAP_OK;
+  };
   for (double f : factors) {
     double d = f > 0 ? f * unit : fapk::kSsspNoDelta;
     if (!e->f32()) d = std::max(1.0, std::floor(d));
-    e->delta_try = d;
-    Issuer is{e, pl, st, false};
-    if (cudaEventRecord(a, st) != cudaSuccess) { rc = FAP_ERR_CUDA; break; }
-    for (size_t g = 0; g < pl.groups.size() && rc == FAP_OK; g++) rc = is.sssp(g);
-    if (rc != FAP_OK) break;
-    if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) {
-      rc = set_error(FAP_ERR_CUDA, "autotune: event failed");
-      break;
-    }
     float ms = 0;
-    cudaEventElapsedTime(&ms, a, b);
+    if ((rc = time_phase(d, ms)) != FAP_OK) break;
     if (ms < best_ms) {
       best_ms = ms;
       best = d;
     }
+  }
+  if (rc == FAP_OK && pl.sssp_lanes_alt > 0) {
+    auto swap_width = [&]() {
+      std::swap(pl.sssp_lanes, pl.sssp_lanes_alt);
+      for (auto &G : pl.groups) {
+        std::swap(G.batches, G.batches_alt);
+        std::swap(G.nbatches, G.nbatches_alt);
+      }
+    };
+    float t[2] = {1e30f, 1e30f};  // [this width, the other]
+    for (int w = 0; w < 2 && rc == FAP_OK; w++) {
+      if (w == 1) swap_width();
+      for (int rep = 0; rep < 2 && rc == FAP_OK; rep++) {
+        float ms = 0;
+        if ((rc = time_phase(best, ms)) == FAP_OK) t[w] = std::min(t[w], ms);
+      }
+    }
+    if (rc == FAP_OK && t[1] >= t[0]) swap_width();  // back to the first width
+    best_ms = std::min(t[0], t[1]);
+    e->sssp_lanes_tuned = pl.sssp_lanes;
   }
   e->delta_try = 0;
   cudaEventDestroy(a);
@@ -949,11 +987,18 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     fw_elems += ld * ld;
     batches32 += (e->bdy_num[p] + 31) / 32;
   }
-  const int lanes = e->sssp_lanes ? e->sssp_lanes
-                                   : fapk::sssp_lanes_for(batches32, e->sm_count, e->f32() && e->sssp_fp64);
-  const bool wide = e->f32() && e->sssp_fp64 && lanes == 32;
+  const bool acc64 = e->f32() && e->sssp_fp64;
+  const int lanes = e->sssp_lanes                        ? e->sssp_lanes
+                    : (e->sssp_lanes_tuned && !acc64) ? e->sssp_lanes_tuned
+                                                      : fapk::sssp_lanes_for(batches32, e->sm_count, acc64);
+  // The SSSP autotuner also tries the other batch width (not for the FP64
+  // search, whose 32-source slots have another layout); scratch for the
+  // larger batch count of the two.
+  const bool tune_lanes = e->autotune && e->sssp_delta <= 0 && e->sssp_lanes == 0 && !acc64;
+  const bool wide = acc64 && lanes == 32;
+  const int count_lanes = tune_lanes ? 16 : lanes;
   int max_batches = 0;
-  for (int p : parts) max_batches += (e->bdy_num[p] + lanes - 1) / lanes;
+  for (int p : parts) max_batches += (e->bdy_num[p] + count_lanes - 1) / count_lanes;
   if ((rc = e->fw_d.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
   if (pred && (rc = e->fw_p.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
   int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e, wide));
@@ -973,6 +1018,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     np->brow_offs = boffs;
     np->sig = buffer_signature(e);
     np->sssp_lanes = lanes;
+    np->sssp_lanes_alt = tune_lanes ? (lanes == 16 ? 32 : 16) : 0;
     if ((rc = build_plan(e, *np)) != FAP_OK) return rc;
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
@@ -1746,6 +1792,7 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
       if (value != 0.0 && value != 16.0 && value != 32.0)
         return set_error(FAP_ERR_INVALID, "SSSP lanes must be 0, 16 or 32");
       e->sssp_lanes = (int)value;
+      e->sssp_lanes_tuned = 0;
       return FAP_OK;
     case FAP_OPT_TILE_COLS:
       if (value != 0.0 && value != 64.0 && value != 128.0)
@@ -1763,7 +1810,7 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_SSSP_FP64: *value = e->sssp_fp64; return FAP_OK;
     case FAP_OPT_SSSP_DELTA: *value = sssp_delta_of(e); return FAP_OK;
     case FAP_OPT_AUTOTUNE: *value = e->autotune; return FAP_OK;
-    case FAP_OPT_SSSP_LANES: *value = e->sssp_lanes; return FAP_OK;
+    case FAP_OPT_SSSP_LANES: *value = e->sssp_lanes ? e->sssp_lanes : e->sssp_lanes_tuned; return FAP_OK;
     case FAP_OPT_TILE_COLS: *value = e->tile_cols; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");
   }

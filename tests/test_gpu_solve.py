@@ -178,23 +178,30 @@ def test_solve_bit_exact_with_either_tile_width(gpu, name, cols):
     assert np.array_equal(p[m], z["path"][m])
 
 
-def test_tile_autotuner_keeps_results(gpu):
+def test_autotuners_keep_results(gpu):
     """Tuned, 64-column and 128-column min-plus tiles give the same rows, in
     both forms, on graphs whose parts fall in both K classes of the strip form
-    (the tuner's trial launches rewrite the rows of the first run)."""
+    (the tuner's trial launches rewrite the rows of the first run), and the
+    same as an engine with the autotuners off; the SSSP tuner reports the
+    batch width it chose."""
     from fastapsp_gb300 import graphs
 
     for g, K in ((graphs.geometric_knn(n=6144, k=3, seed=11), 6), (graphs.grid_graph(64, 64, seed=3), 4)):
         n = g.n
         outs = []
-        with gpu.Engine(n, g.row_offset, g.col_val, g.weight, K, dtype=gpu.DTYPE_I32) as eng:
-            for cols, mode in ((0, 1), (64, 1), (128, 1), (0, 0)):
-                eng.set_option(gpu._lib.OPT_TILE_COLS, cols)
-                d = torch.empty((n, n), dtype=torch.int32, device="cuda")
-                p = torch.empty((n, n), dtype=torch.int32, device="cuda")
-                eng.solve(d, p, mode)
-                eng.solve(d, p, mode)  # the second run uses the tuned widths
-                torch.cuda.synchronize()
-                outs.append((d.cpu(), p.cpu()))
+        for tune in (1, 0):
+            with gpu.Engine(n, g.row_offset, g.col_val, g.weight, K, dtype=gpu.DTYPE_I32) as eng:
+                eng.set_option(gpu._lib.OPT_AUTOTUNE, tune)
+                runs = ((0, 1), (64, 1), (128, 1), (0, 0)) if tune else ((0, 1),)
+                for cols, mode in runs:
+                    eng.set_option(gpu._lib.OPT_TILE_COLS, cols)
+                    d = torch.empty((n, n), dtype=torch.int32, device="cuda")
+                    p = torch.empty((n, n), dtype=torch.int32, device="cuda")
+                    eng.solve(d, p, mode)
+                    eng.solve(d, p, mode)  # the second run uses the tuned widths
+                    torch.cuda.synchronize()
+                    outs.append((d.cpu(), p.cpu()))
+                lanes = eng.get_option(gpu._lib.OPT_SSSP_LANES)
+                assert lanes in ((16, 32) if tune else (0,))
         for d, p in outs[1:]:
             assert torch.equal(d, outs[0][0]) and torch.equal(p, outs[0][1])
