@@ -211,7 +211,8 @@ struct fap_engine {
   cudaStream_t side = nullptr;    // lowest priority: the FW remaining tiles beside that chain
   cudaEvent_t ev[6] = {};
   cudaEvent_t ev_sync[2] = {};
-  cudaEvent_t ev_fw[3] = {};      // FW lookahead: [0] after pivot step r, [1 + r % 2] after round r's tiles
+  cudaEvent_t ev_fw[3] = {};      // FW lookahead: [0] after pivot step r, [1 + r % 2] after round r's tiles;
+                                  // then [0] / [1] fork and join the min-plus classes
   cudaStream_t copy = nullptr;    // early copy-out of boundary rows (host results)
   cudaEvent_t ev_copy[2] = {};    // [0] SSSP rows written, [1] their copy-out done
   // work buffers
@@ -748,12 +749,27 @@ struct Issuer {
       FAP_CUDA(cudaEventRecord(e->ev_copy[1], e->copy));
     }
     if (packed || f32) {  // strip form for the segments with K <= 100, tiles for the rest
+      // The first class on the issuing stream, the later ones (a few parts
+      // with larger K) on the low-priority side stream, whose CTAs take the
+      // SMs the first launch leaves as it drains.  They write other parts'
+      // rows and read only the FW matrices and the boundary rows.
+      bool fork = false;
+      for (int c = 1; c < G.mp_ncls; c++) fork = fork || (G.mp_cls_strips[c] > 0 && G.mp_cls_strips[0] > 0);
+      if (fork) {
+        FAP_CUDA(cudaEventRecord(e->ev_fw[0], st));
+        FAP_CUDA(cudaStreamWaitEvent(e->side, e->ev_fw[0], 0));
+      }
       for (int c = 0; c < G.mp_ncls; c++)
         FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
-                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st, f32,
+                                             G.mp_cls_strips[c], G.mp_cls_max_k[c],
+                                             fork && c > 0 ? e->side : st, f32,
                                              e->tile_cols ? e->tile_cols : G.mp_cls_cols[c]));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles - G.mp_strip_tiles,
                                           packed, st, G.mp_strip_tiles));
+      if (fork) {  // join
+        FAP_CUDA(cudaEventRecord(e->ev_fw[1], e->side));
+        FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1], 0));
+      }
     } else {
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles, packed, st));
     }
