@@ -223,8 +223,11 @@ __device__ __forceinline__ void clear_bit(unsigned *bits, int v) {
   atomicAnd(&bits[v >> 5], ~(1u << (v & 31)));
 }
 
+// The FP64 search at two CTAs per SM (64 registers, a few spills): on the
+// 114,599-vertex road-like graph with 128 parts its 220 batches then run in
+// one wave (search 225 -> 179 ms).
 template <typename T, bool PRED, int LANES, bool ACC64>
-__global__ void __launch_bounds__(kSsspThreads)
+__global__ void __launch_bounds__(kSsspThreads, ACC64 ? 2 : 1)
     sssp_kernel(SsspArgs a) {
   using A = Acc<T, ACC64>;
   using V = typename A::V;
@@ -555,7 +558,8 @@ int sssp_lanes_for(int64_t batches32, int sm_count, bool acc64) {
   // relaxes at once; worth it while 32-source batches leave SMs idle.  The
   // FP64 search always takes 16: on the 114,599-vertex road-like graph with
   // 128 parts, 129 batches of 32 in one wave searched in 431 ms against
-  // 225 ms for 258 batches of 16 in two waves.
+  // 225 ms for 220 batches of 16 in two waves (one CTA per SM; 179 ms in
+  // one wave at two per SM).
   if (acc64) return 16;
   return batches32 < 2LL * sm_count ? 16 : 32;
 }
