@@ -35,7 +35,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-MP_TRAFFIC_PER_OUTPUT_BYTE = 1.116  # DRAM read+write per algorithmic byte of the min-plus launch (ncu)
+MP_TRAFFIC_PER_OUTPUT_BYTE = 1.136  # DRAM read+write per algorithmic byte of the min-plus launch (ncu)
 METRIC = "APSP distances/s"
 UNIT = "distances/s"
 HBM_PEAK_FALLBACK = 6800.0
