@@ -242,7 +242,9 @@ double sssp_delta_of(const fap_engine *e) {
 }
 
 int max_sssp_slots(fap_engine *e, bool wide = false) {
-  // Two 512-thread CTAs per SM, bounded by a 16 GiB scratch budget.
+  // Up to two 512-thread CTAs per SM (the FP64 search runs two, the others
+  // one at their register count: further batches wait for a free slot),
+  // bounded by a 16 GiB scratch budget.
   int slots = std::max(1, 2 * e->sm_count);
   size_t per = fapk::sssp_slot_bytes(e->n, wide) + fapk::sssp_bits_bytes(e->n);
   size_t budget = (size_t)16 << 30;
