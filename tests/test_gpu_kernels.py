@@ -230,3 +230,15 @@ def test_engine_fp64_sssp_option_meets_1e6_on_road_graph(gpu, oracle_lib, lanes)
         assert np.array_equal(f, dd[i] < 1e8)
         worst = max(worst, float(np.max(np.abs(dd[i][f] - d64[f]) / np.maximum(d64[f], 1e-30))))
     assert worst <= 1e-6, worst
+
+
+def test_speed_options_reject_unsupported_widths(gpu):
+    """Batch and tile widths are limited to the kernels that exist; a rejected
+    value leaves the option as it was."""
+    g = graphs.grid_graph(16, 16, seed=4)
+    with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=gpu.DTYPE_I32) as eng:
+        for opt, bad, good in ((gpu._lib.OPT_SSSP_LANES, 8, 32), (gpu._lib.OPT_TILE_COLS, 48, 128)):
+            eng.set_option(opt, good)
+            with pytest.raises(gpu._lib.FapError):
+                eng.set_option(opt, bad)
+            assert eng.get_option(opt) == good
