@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
       arg[r][c] = 0;
     }
   for (int it = 0; it < iters; it++) {
-    if (MODE == 4 || MODE == 5) {
+    if constexpr (MODE == 4 || MODE == 5) {
 #pragma unroll
       for (int s = 0; s < 4; s += 2)
 #pragma unroll
@@ -80,29 +80,27 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
               acc[r][c] = (T)min3_f32((float)acc[r][c], v.x, v.y);
             }
           }
+    } else {
 #pragma unroll
-      for (int i = 0; i < 16; i++) b[it & 3][i] = b[it & 3][i] - (T)1;
-      continue;
-    }
+      for (int s = 0; s < 4; s++) {
 #pragma unroll
-    for (int s = 0; s < 4; s++) {
+        for (int r = 0; r < 4; r++)
 #pragma unroll
-      for (int r = 0; r < 4; r++)
-#pragma unroll
-        for (int c = 0; c < 16; c++) {
-          const T x = a[s][r], y = b[s][c];
-          if (MODE == 0) {
-            acc[r][c] = (T)__viaddmin_u32((unsigned)x, (unsigned)y, (unsigned)acc[r][c]);
-          } else if (MODE == 1) {
-            acc[r][c] = fminf((float)x + (float)y, (float)acc[r][c]);
-          } else {
-            const T v = x + y;
-            if (v < acc[r][c]) {
-              acc[r][c] = v;
-              arg[r][c] = s;
+          for (int c = 0; c < 16; c++) {
+            const T x = a[s][r], y = b[s][c];
+            if (MODE == 0) {
+              acc[r][c] = (T)__viaddmin_u32((unsigned)x, (unsigned)y, (unsigned)acc[r][c]);
+            } else if (MODE == 1) {
+              acc[r][c] = fminf((float)x + (float)y, (float)acc[r][c]);
+            } else {
+              const T v = x + y;
+              if (v < acc[r][c]) {
+                acc[r][c] = v;
+                arg[r][c] = s;
+              }
             }
           }
-        }
+      }
     }
 #pragma unroll
     for (int i = 0; i < 16; i++) b[it & 3][i] = b[it & 3][i] - (T)1;
