@@ -2,7 +2,6 @@
 declared symbol, the MatrixMarket reader, the partitioner, the boundary /
 reorder step, argument validation, and the multi-rank sharding logic."""
 import re
-from pathlib import Path
 
 import numpy as np
 import pytest

@@ -6,7 +6,6 @@ distance data in the product; the gather here is only the test's check."""
 import os
 
 import numpy as np
-import pytest
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
