@@ -58,12 +58,17 @@ SIGNATURES = {
     "fap_part_info": (C.c_int, [_p, _i32, _pi32, _pi32, _pi32]),
     "fap_solve_part": (C.c_int, [_p, _i32, _p, _p, _p]),
     "fap_solve": (C.c_int, [_p, _p, _p, _i32, _p]),
+    "fap_solve_all": (C.c_int, [_p, _p, _p, _p]),
+    "fap_solve_batched": (C.c_int, [_p, _p, _p, _p]),
+    "fap_set_partition": (C.c_int, [_p, _p]),
+    "fap_precondition": (C.c_int, [_p]),
     "fap_last_times": (C.c_int, [_p, C.POINTER(C.c_double)]),
     "fap_last_launches": (C.c_int, [_p, C.POINTER(C.c_int64)]),
     "fap_minplus_counters": (C.c_int, [_p, C.POINTER(C.c_uint64), _i32]),
     "fap_minplus": (C.c_int, [_p, _i32, _i32, _i32, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i64,
                               _p, _i64, _p]),
     "fap_floyd_batched": (C.c_int, [_p, _i32, _i32, _p, _p, _p, _p, _p]),
+    "fap_fw_batched": (C.c_int, [_p, _i32, _i32, _p, _p, _p, _p, _p]),
     "fap_sssp": (C.c_int, [_p, _p, _i32, _p, _p, _i64, _p]),
     "fap_backward": (C.c_int, [_p, _p, _i32, _p, _p, _p, _p, _p]),
     "fap_backward_dense": (C.c_int, [_p, _i32, _p, _p, _p, _p, _i32, _p, _p, _p, _p, _p]),

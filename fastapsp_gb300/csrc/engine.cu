@@ -1497,6 +1497,61 @@ int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode, void *stre
   return solve_common(e, parts, e->n, dist, pred, mode, stream);
 }
 
+int fap_solve_all(fap_engine *e, void *dist, int32_t *pred, void *stream) {
+  return fap_solve(e, dist, pred, FAP_MODE_PLAIN, stream);
+}
+
+int fap_solve_batched(fap_engine *e, void *dist, int32_t *pred, void *stream) {
+  return fap_solve(e, dist, pred, FAP_MODE_BATCHED, stream);
+}
+
+// Boundary marks and vertex order from graph_id (n entries, 1..K), and the
+// device tables that depend on them; the engine's cached plans are dropped.
+static int apply_partition(fap_engine *e, const int32_t *graph_id) {
+  const int32_t n = e->n, K = e->K;
+  for (int32_t i = 0; i < n; i++)
+    if (graph_id[i] < 1 || graph_id[i] > K) return set_error(FAP_ERR_INVALID, "part id outside 1..K");
+  std::vector<int32_t> gid(graph_id, graph_id + n), st2ed(n), ed2st(n);
+  std::vector<int32_t> vn(K + 1), vo(K + 1), bn(K + 1), bo(K + 1);
+  int rc = fapi::preprocess(K, n, gid.data(), e->ro.data(), e->col.data(), st2ed.data(), ed2st.data(),
+                            vn.data(), vo.data(), bn.data(), bo.data(), nullptr);
+  if (rc != FAP_OK) return rc;
+  DeviceGuard g(e->device);
+  // every solve ends with its streams joined and synchronized; this waits for
+  // anything still queued on the engine's own stream
+  FAP_CUDA(cudaStreamSynchronize(e->stream));
+  e->plans.clear();
+  if (n > 0) {
+    const size_t bytes = (size_t)n * sizeof(int32_t);
+    FAP_CUDA(cudaMemcpy(e->d_gid, gid.data(), bytes, cudaMemcpyHostToDevice));
+    FAP_CUDA(cudaMemcpy(e->d_st2ed, st2ed.data(), bytes, cudaMemcpyHostToDevice));
+    FAP_CUDA(cudaMemcpy(e->d_ed2st, ed2st.data(), bytes, cudaMemcpyHostToDevice));
+  }
+  e->graph_id.swap(gid);
+  e->st2ed.swap(st2ed);
+  e->ed2st.swap(ed2st);
+  e->ver_num.swap(vn);
+  e->ver_offset.swap(vo);
+  e->bdy_num.swap(bn);
+  e->bdy_offset.swap(bo);
+  return FAP_OK;
+}
+
+int fap_set_partition(fap_engine *e, const int32_t *graph_id) {
+  if (!e || !graph_id) return set_error(FAP_ERR_INVALID, "null argument");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  std::lock_guard<std::mutex> lk(e->mu);
+  return apply_partition(e, graph_id);
+}
+
+int fap_precondition(fap_engine *e) {
+  if (!e) return set_error(FAP_ERR_INVALID, "null argument");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  std::lock_guard<std::mutex> lk(e->mu);
+  const std::vector<int32_t> gid = e->graph_id;
+  return apply_partition(e, gid.data());
+}
+
 int fap_last_times(const fap_engine *e, double *times5) {
   if (!e || !times5) return set_error(FAP_ERR_INVALID, "null argument");
   for (int i = 0; i < 5; i++) times5[i] = e->times[i];
@@ -1569,6 +1624,11 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
     FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr, dseg, 1, tiles, packed, st));
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);
+}
+
+int fap_fw_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t *sizes,
+                   void *const *D, const int64_t *ld, int32_t *const *P, void *stream) {
+  return fap_floyd_batched(e, dtype, count, sizes, D, ld, P, stream);
 }
 
 int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t *sizes,

@@ -141,6 +141,17 @@ class Engine:
     def solve_part(self, part: int, dist, pred=None, stream=None):
         check(lib().fap_solve_part(self._h, int(part), ptr(dist), ptr(pred), stream), "fap_solve_part")
 
+    def set_partition(self, graph_id):
+        """New partition (n part ids, 1..K) for this graph; boundary and
+        vertex order are recomputed, later solves use the new parts."""
+        gid = np.ascontiguousarray(graph_id, dtype=np.int32)
+        if gid.shape != (self.n,):
+            raise ValueError("graph_id needs one part id per vertex")
+        check(lib().fap_set_partition(self._h, ptr(gid)), "fap_set_partition")
+
+    def precondition(self):
+        check(lib().fap_precondition(self._h), "fap_precondition")
+
     def last_times(self):
         t = (C.c_double * 5)()
         check(lib().fap_last_times(self._h, t), "fap_last_times")

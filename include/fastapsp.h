@@ -150,6 +150,25 @@ int fap_solve_part(fap_engine *e, int32_t part, void *dist, int32_t *pred,
 int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode,
               void *stream);
 
+/* fap_solve in each mode by name: solve() part by part
+ * (fap/fap.cpp:507-518), and the batched form. */
+int fap_solve_all(fap_engine *e, void *dist, int32_t *pred, void *stream);
+int fap_solve_batched(fap_engine *e, void *dist, int32_t *pred, void *stream);
+
+/* Replaces the partition the fapGraph constructor reads
+ * (fap/utils/readIdFile.h:79-304 fills graph_id) for an existing engine:
+ * graph_id (n entries, 1..K, host memory) becomes the engine's partition and
+ * the boundary marks and vertex order are recomputed as in fap_precondition;
+ * cached plans are dropped, later solves use the new parts.  Do not call it
+ * while another call on this engine is in flight. */
+int fap_set_partition(fap_engine *e, const int32_t *graph_id);
+
+/* Replaces fapGraph::preCondition() (fap/fap.cpp:100-114: findBoundry and
+ * sort_and_encode, fap/utils/util_preprocess.h:32-106) on an engine:
+ * recomputes the boundary marks and the vertex order (fap_mapping) from the
+ * engine's partition.  fap_create already does it; the call is idempotent. */
+int fap_precondition(fap_engine *e);
+
 /* Engine options (no reference counterpart).
  *   FAP_OPT_SSSP_FP64  (FP32 engines) 1 = run the boundary SSSP in FP64 and
  *                      round once, which keeps FP32 results within an ulp or
@@ -223,6 +242,10 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K,
 int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count,
                       const int32_t *sizes, void *const *D, const int64_t *ld,
                       int32_t *const *P, void *stream);
+/* The same call under the name fap_fw_batched. */
+int fap_fw_batched(fap_engine *e, int32_t dtype, int32_t count,
+                   const int32_t *sizes, void *const *D, const int64_t *ld,
+                   int32_t *const *P, void *stream);
 
 /* Replaces handle_boundry_path_data_on_gpu (fap/kernel/batch_sssp.h:254-278,
  * multi_source_Nvidia_sssp_data_on_gpu, fap/kernel/cuda/batch_sssp.cu:

@@ -205,3 +205,39 @@ def test_autotuners_keep_results(gpu):
                 assert lanes in ((16, 32) if tune else (0,))
         for d, p in outs[1:]:
             assert torch.equal(d, outs[0][0]) and torch.equal(p, outs[0][1])
+
+
+def test_set_partition_matches_a_fresh_engine(gpu):
+    """fap_set_partition on a solved engine gives the mapping and the rows of
+    an engine created with that partition; fap_precondition keeps them;
+    fap_solve_all / fap_solve_batched are fap_solve in each mode."""
+    from fastapsp_gb300 import graphs
+    from fastapsp_gb300._lib import check, ptr
+
+    g = graphs.geometric_knn(n=4096, k=3, seed=5)
+    n, K = g.n, 4
+    gid_a, _ = gpu.partition(g.row_offset, g.col_val, K)
+    gid_b = (np.arange(n) * K // n + 1).astype(np.int32)  # contiguous id blocks
+    outs = []
+    with gpu.Engine(n, g.row_offset, g.col_val, g.weight, K, graph_id=gid_a, dtype=gpu.DTYPE_I32) as eng:
+        d = torch.empty((n, n), dtype=torch.int32, device="cuda")
+        p = torch.empty((n, n), dtype=torch.int32, device="cuda")
+        eng.solve(d, p, 1)
+        eng.set_partition(gid_b)
+        assert np.array_equal(eng.graph_id(), gid_b)
+        mapping = eng.mapping()
+        eng.precondition()
+        assert np.array_equal(eng.mapping(), mapping)
+        for fn in ("fap_solve_batched", "fap_solve_all"):
+            check(getattr(gpu.lib(), fn)(eng._h, ptr(d), ptr(p), None), fn)
+            torch.cuda.synchronize()
+            outs.append((d.cpu(), p.cpu()))
+    with gpu.Engine(n, g.row_offset, g.col_val, g.weight, K, graph_id=gid_b, dtype=gpu.DTYPE_I32) as ref:
+        assert np.array_equal(ref.mapping(), mapping)
+        d2 = torch.empty((n, n), dtype=torch.int32, device="cuda")
+        p2 = torch.empty((n, n), dtype=torch.int32, device="cuda")
+        ref.solve(d2, p2, 1)
+        torch.cuda.synchronize()
+        d2, p2 = d2.cpu(), p2.cpu()
+    for d, p in outs:
+        assert torch.equal(d, d2) and torch.equal(p, p2)
