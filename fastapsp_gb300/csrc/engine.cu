@@ -999,22 +999,25 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   int rc;
   // work buffers
   size_t fw_elems = 0;
-  int64_t batches32 = 0;
+  int64_t batches8 = 0, batches32 = 0;
   for (int p : parts) {
     size_t ld = align_up((size_t)e->ver_num[p], (size_t)fapk::fw_block());
     fw_elems += ld * ld;
+    batches8 += (e->bdy_num[p] + 7) / 8;
     batches32 += (e->bdy_num[p] + 31) / 32;
   }
   const bool acc64 = e->f32() && e->sssp_fp64;
-  const int lanes = e->sssp_lanes                        ? e->sssp_lanes
-                    : (e->sssp_lanes_tuned && !acc64) ? e->sssp_lanes_tuned
-                                                      : fapk::sssp_lanes_for(batches32, e->sm_count, acc64);
-  // The SSSP autotuner also tries the other batch width (not for the FP64
-  // search, whose 32-source slots have another layout); scratch for the
-  // larger batch count of the two.
+  int lanes = e->sssp_lanes                        ? e->sssp_lanes
+              : (e->sssp_lanes_tuned && !acc64) ? e->sssp_lanes_tuned
+                                                : fapk::sssp_lanes_for(batches8, batches32, e->sm_count, acc64);
+  if (acc64 && lanes == 8) lanes = 16;  // the FP64 search has no 8-source form
+  // The SSSP autotuner also tries a second batch width (8 -> 16, 16 -> 32,
+  // 32 -> 16; not for the FP64 search, whose 32-source slots have another
+  // layout); scratch for the larger batch count of the two.
   const bool tune_lanes = e->autotune && e->sssp_delta <= 0 && e->sssp_lanes == 0 && !acc64;
+  const int alt_lanes = lanes == 16 ? 32 : 16;
   const bool wide = acc64 && lanes == 32;
-  const int count_lanes = tune_lanes ? 16 : lanes;
+  const int count_lanes = tune_lanes ? std::min(lanes, alt_lanes) : lanes;
   int max_batches = 0;
   for (int p : parts) max_batches += (e->bdy_num[p] + count_lanes - 1) / count_lanes;
   if ((rc = e->fw_d.ensure(std::max<size_t>(fw_elems, 1) * 4)) != FAP_OK) return rc;
@@ -1036,7 +1039,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     np->brow_offs = boffs;
     np->sig = buffer_signature(e);
     np->sssp_lanes = lanes;
-    np->sssp_lanes_alt = tune_lanes ? (lanes == 16 ? 32 : 16) : 0;
+    np->sssp_lanes_alt = tune_lanes ? alt_lanes : 0;
     if ((rc = build_plan(e, *np)) != FAP_OK) return rc;
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
@@ -1760,7 +1763,9 @@ int fap_sssp(fap_engine *e, const int32_t *sources, int32_t num_sources, void *d
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
   const bool acc64 = e->f32() && e->sssp_fp64;
-  const int lanes = e->sssp_lanes ? e->sssp_lanes : fapk::sssp_lanes_for((num_sources + 31) / 32, e->sm_count, acc64);
+  int lanes = e->sssp_lanes ? e->sssp_lanes
+                            : fapk::sssp_lanes_for((num_sources + 7) / 8, (num_sources + 31) / 32, e->sm_count, acc64);
+  if (acc64 && lanes == 8) lanes = 16;  // the FP64 search has no 8-source form
   const bool wide = acc64 && lanes == 32;
   std::vector<SsspBatch> batches;
   for (int b0 = 0; b0 < num_sources; b0 += lanes) {
@@ -1867,8 +1872,8 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
       e->autotune = value != 0.0 ? 1 : 0;
       return FAP_OK;
     case FAP_OPT_SSSP_LANES:
-      if (value != 0.0 && value != 16.0 && value != 32.0)
-        return set_error(FAP_ERR_INVALID, "SSSP lanes must be 0, 16 or 32");
+      if (value != 0.0 && value != 8.0 && value != 16.0 && value != 32.0)
+        return set_error(FAP_ERR_INVALID, "SSSP lanes must be 0, 8, 16 or 32");
       e->sssp_lanes = (int)value;
       e->sssp_lanes_tuned = 0;
       return FAP_OK;

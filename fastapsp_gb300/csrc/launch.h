@@ -79,7 +79,8 @@ struct SsspArgs {
   unsigned *status;           // device status word (error flags are or-ed in)
   unsigned *maxd;             // largest finite int32 distance written (atomicMax), may be null
   int32_t iter_cap;           // steps (near-frontier sweeps + far splits) per batch
-  int32_t lanes;              // sources per batch: 16 or 32 (batches hold <= lanes)
+  int32_t lanes;              // sources per batch: 8, 16 or 32 (batches hold <= lanes;
+                              // 16 or 32 with acc64)
   int32_t acc64;              // FP32 weights searched in FP64 (8-byte entries)
   double delta;               // near-far threshold step (> 0; huge = plain Bellman-Ford)
   unsigned long long *stats;  // may be null: [near steps, far splits, frontier
@@ -91,8 +92,8 @@ constexpr double kSsspNoDelta = 2147483647.0;
 cudaError_t init_sssp_kernels();
 size_t sssp_slot_bytes(int32_t n, bool wide = false);  // wide: FP64 search with 32 lanes
 size_t sssp_bits_bytes(int32_t n);  // per slot; 0 when the bitmaps fit in shared memory
-// Batch width (16 or 32 sources) given the 32-source batches the work needs.
-int sssp_lanes_for(int64_t batches32, int sm_count, bool acc64);
+// Batch width (8, 16 or 32 sources) given the batches the work needs at 8 and 32.
+int sssp_lanes_for(int64_t batches8, int64_t batches32, int sm_count, bool acc64);
 int sssp_threads();
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st);
 

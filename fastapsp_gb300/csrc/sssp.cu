@@ -6,7 +6,7 @@
 // 177-288, 361-414) on the GPU, which runs one source at a time with a host
 // round trip per relaxation sweep and computes no predecessors.
 //
-// Design (GB300): one CTA owns a batch of LANES (16 or 32) sources, one per
+// Design (GB300): one CTA owns a batch of LANES (8, 16 or 32) sources, one per
 // lane of a lane group; a warp relaxes 32 / LANES frontier vertices at once.
 // Distances live in a vertex-major scratch table dvm[v][lane], so relaxing an
 // edge u->v for the whole batch touches one 64- or 128-byte line.
@@ -133,7 +133,8 @@ __device__ __forceinline__ void sssp_out_block(const SsspArgs &a,
     }
     if (PRED) {
       int dmax = max(deg[0], deg[1]);
-      if (VPW == 2) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, 16));
+#pragma unroll
+      for (int o = LANES; o < 32; o <<= 1) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
       // vertices that no source of the batch reached need no scan
       if (!__any_sync(0xffffffffu, dk[0] < INF || dk[1] < INF)) dmax = 0;
       for (int j = 0; j < dmax; j++) {
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(kSsspThreads, ACC64 ? 2 : 1)
   constexpr int G = 8;             // edges per lane group in flight (<= LANES)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / LANES, sl = lane % LANES;
-  const unsigned group_mask = LANES == 32 ? 0xffffffffu : (0xffffu << (16 * sub));
+  const unsigned group_mask = LANES == 32 ? 0xffffffffu : (((1u << LANES) - 1u) << (LANES * sub));
   const int32_t n = a.n;
   constexpr bool kWide = ACC64 && LANES == 32;
   unsigned char *base = static_cast<unsigned char *>(a.scratch) + (size_t)blockIdx.x * slot_bytes(n, kWide);
@@ -331,8 +332,9 @@ __global__ void __launch_bounds__(kSsspThreads, ACC64 ? 2 : 1)
             eb[i] = e0 - pre[i];
           }
           const int tot = pre[R];
-          int tmax = tot;
-          if (VPW == 2) tmax = max(tot, __shfl_xor_sync(0xffffffffu, tot, 16));
+          int tmax = tot;  // the longest edge walk of the warp's lane groups
+#pragma unroll
+          for (int o = LANES; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
           for (int t0 = 0; t0 < tmax; t0 += G) {
             int v[G];
             V c[G];
@@ -503,6 +505,7 @@ cudaError_t launch_t(const SsspArgs &a, cudaStream_t st) {
       return a.lanes == 16 ? launch_one<float, PRED, 16, true>(a, st) : launch_one<float, PRED, 32, true>(a, st);
     return cudaErrorInvalidValue;
   }
+  if (a.lanes == 8) return launch_one<T, PRED, 8, false>(a, st);
   if (a.lanes == 16) return launch_one<T, PRED, 16, false>(a, st);
   return launch_one<T, PRED, 32, false>(a, st);
 }
@@ -527,6 +530,10 @@ cudaError_t init_sssp_kernels() {
   cudaError_t e;
 #define FAP_SSSP_ATTR(T, P, L, A) \
   if ((e = set_attr<T, P, L, A>()) != cudaSuccess) return e;
+  FAP_SSSP_ATTR(float, true, 8, false)
+  FAP_SSSP_ATTR(float, false, 8, false)
+  FAP_SSSP_ATTR(uint32_t, true, 8, false)
+  FAP_SSSP_ATTR(uint32_t, false, 8, false)
   FAP_SSSP_ATTR(float, true, 16, false)
   FAP_SSSP_ATTR(float, true, 32, false)
   FAP_SSSP_ATTR(float, false, 16, false)
@@ -545,22 +552,24 @@ cudaError_t init_sssp_kernels() {
 
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st) {
   if (a.nbatches <= 0 || a.slots <= 0) return cudaSuccess;
-  if (a.lanes != 16 && a.lanes != 32) return cudaErrorInvalidValue;
-  if (a.acc64 && !f32) return cudaErrorInvalidValue;
+  if (a.lanes != 8 && a.lanes != 16 && a.lanes != 32) return cudaErrorInvalidValue;
+  if (a.acc64 && (!f32 || a.lanes == 8)) return cudaErrorInvalidValue;
   if (!(a.delta > 0.0)) return cudaErrorInvalidValue;
   const bool pred = a.pred != nullptr;
   if (f32) return pred ? launch_t<float, true>(a, st) : launch_t<float, false>(a, st);
   return pred ? launch_t<uint32_t, true>(a, st) : launch_t<uint32_t, false>(a, st);
 }
 
-int sssp_lanes_for(int64_t batches32, int sm_count, bool acc64) {
+int sssp_lanes_for(int64_t batches8, int64_t batches32, int sm_count, bool acc64) {
   // Half-warp batches double the CTA count and the frontier vertices a warp
-  // relaxes at once; worth it while 32-source batches leave SMs idle.  The
+  // relaxes at once; worth it while 32-source batches leave SMs idle, and
+  // quarter-warp batches again while they still fit in one wave.  The
   // FP64 search always takes 16: on the 114,599-vertex road-like graph with
   // 128 parts, 129 batches of 32 in one wave searched in 431 ms against
   // 225 ms for 220 batches of 16 in two waves (one CTA per SM; 179 ms in
   // one wave at two per SM).
   if (acc64) return 16;
+  if (batches8 <= sm_count) return 8;
   return batches32 < 2LL * sm_count ? 16 : 32;
 }
 

@@ -182,14 +182,14 @@ int fap_precondition(fap_engine *e);
  *                      (multiples of the mean edge weight, and plain
  *                      Bellman-Ford) and keeps the fastest; fap_get_option
  *                      then reports the chosen step.  0 = 8 x the mean weight.
- *   FAP_OPT_SSSP_LANES sources per SSSP batch (one CTA each; 16 = two lane
- *                      groups a warp, 32 = one): 16 or 32, or 0 (default) =
- *                      automatic: while the step is tuned (above), the first
- *                      run also times both widths at the chosen step and
+ *   FAP_OPT_SSSP_LANES sources per SSSP batch (one CTA each; 8 = four lane
+ *                      groups a warp, 16 = two, 32 = one): 8, 16 or 32, or 0
+ *                      (default) = automatic: chosen from the batch count,
+ *                      and while the step is tuned (above), the first run
+ *                      also times a second width at the chosen step and
  *                      keeps the faster, which fap_get_option then reports
- *                      (not with FAP_OPT_SSSP_FP64, which takes 16);
- *                      otherwise chosen from the batch count.  Changes speed
- *                      only, never results.
+ *                      (not with FAP_OPT_SSSP_FP64, which takes 16 unless 32
+ *                      is set).  Changes speed only, never results.
  *   FAP_OPT_TILE_COLS  column width of the packed int32 min-plus tiles (128
  *                      rows): 64 or 128, or 0 (default) = chosen per K class
  *                      of each plan: while FAP_OPT_AUTOTUNE is on, the first

@@ -148,7 +148,7 @@ def test_sssp_result_independent_of_near_far_step(gpu, oracle_lib, kind):
     outs = []
     with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=dtype) as eng:
         lo = 1e-3 if dtype == gpu.DTYPE_F32 else 1
-        for delta, lanes in ((lo, 0), (0.0, 0), (1e9, 0), (0.0, 16), (0.0, 32)):
+        for delta, lanes in ((lo, 0), (0.0, 0), (1e9, 0), (0.0, 8), (0.0, 16), (0.0, 32)):
             eng.set_option(gpu._lib.OPT_SSSP_DELTA, delta)
             eng.set_option(gpu._lib.OPT_SSSP_LANES, lanes)
             d = torch.empty((len(src), g.n), dtype=dt, device="cuda")
@@ -237,7 +237,7 @@ def test_speed_options_reject_unsupported_widths(gpu):
     value leaves the option as it was."""
     g = graphs.grid_graph(16, 16, seed=4)
     with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=gpu.DTYPE_I32) as eng:
-        for opt, bad, good in ((gpu._lib.OPT_SSSP_LANES, 8, 32), (gpu._lib.OPT_TILE_COLS, 48, 128)):
+        for opt, bad, good in ((gpu._lib.OPT_SSSP_LANES, 12, 8), (gpu._lib.OPT_TILE_COLS, 48, 128)):
             eng.set_option(opt, good)
             with pytest.raises(gpu._lib.FapError):
                 eng.set_option(opt, bad)
