@@ -1,21 +1,26 @@
 """Benchmark of the Fast-APSP hot path on GB300.
 
-Workload (default): a directed 3-nearest-neighbour geometric graph of 65,536
-uniform points in the unit square with integer weights U[1,1000] (seeded),
-split into K=64 parts by the engine's partitioner, all parts solved (the rows
-of solveSubGraph(1..64)), int32 distances + predecessors.  Inputs are synthetic;
-there is no public dataset in this workload.
+Workload (default, --config c4): the road-like graph of 114,599 vertices
+(perturbed planar grid thinned to a near-tree and subdivided by degree-2
+chains, ~239k directed entries, FP32 weights U[0.1,10], seeded), split into
+K=128 parts, full all-pairs solve with FP32 distances and int32 predecessors,
+the boundary SSSP in exact arithmetic (the FP64 option), so results are within
+1e-6 of FP64 Dijkstra.  Inputs are synthetic; no dataset is involved.  The
+parts come from a committed partition (tests/golden/partitions/partition_*.npz) that both
+arms use.  --config c1 / c2 print the same line for the 128x128 grid and the
+65,536-vertex geometric graph; c3 / c5 print their own lines.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c4]
 
 ours:      one JSON line: device-resident throughput (value), the end-to-end
            number through the public C ABI with host buffers (e2e), the
-           min-plus kernel's add-min roofline, the SSSP kernel's HBM roofline,
-           the plain-form comparison, clocks and the CPU baseline.
+           min-plus kernel's roofline, the FW and SSSP rates, the plain-form
+           comparison, clocks and the CPU baseline.
 reference: the reference's CPU algorithm (the oracle restatement of its
            fapGraph::run CPU branch, pinned bit-for-bit to the reference's own
-           fap.cpp) on a bounded sample of the same workload, on all host cores.
-Under torchrun (N>1) every rank solves its own instance (seed + rank), no
+           fap.cpp) on a bounded sample of the same workload, on all host
+           cores, without loading the engine's library.
+Under torchrun (N>1) every rank solves its own copy of the graph, no
 collective on the data path; rank 0 prints.
 """
 from __future__ import annotations
@@ -35,19 +40,80 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-MP_TRAFFIC_PER_OUTPUT_BYTE = 1.136  # DRAM read+write per algorithmic byte of the min-plus launch (ncu)
 METRIC = "APSP distances/s"
 UNIT = "distances/s"
 HBM_PEAK_FALLBACK = 6800.0
+# DRAM read+write bytes per algorithmic byte of the min-plus launch, from ncu
+# captures of the same kernel on smaller cases of each workload (scaled by the
+# output bytes, which grow with the work); None where no capture was taken.
+MP_TRAFFIC_PER_BYTE = {"c2": 1.136, "c4": None, "c1": None}
+
+# Solve workloads: the synthetic graph, its part count, the engine's distance
+# type, the committed partition (tests/golden/partitions/make_partitions.py) and, for
+# FP32 graphs, the SSSP arithmetic the spec bar needs.
+WORKLOADS = {
+    "c4": dict(gen="road_like", K=128, dtype="f32", part="road_like_n114599_K128", fp64_sssp=1,
+               desc="road-like graph (perturbed planar grid thinned to a near-tree, degree-2 chain "
+                    "subdivision), n=114,599, ~239k directed entries, FP32 weights U[0.1,10], K=128 parts, "
+                    "full APSP (solve), FP32 dist + int32 pred"),
+    "c2": dict(gen="geometric_knn", K=64, dtype="i32", part="geometric_knn_n65536_K64", fp64_sssp=0,
+               desc="directed 3-NN geometric graph, n=65,536, int weights U[1,1000], K=64 parts, all parts "
+                    "solved (solveSubGraph 1..64 rows), int32 dist + pred"),
+    "c1": dict(gen="grid_graph", K=16, dtype="i32", part="grid_n16384_K16", fp64_sssp=0,
+               desc="128x128 grid (random spanning tree + each other edge with p=0.6), unweighted, "
+                    "K=16 parts, full APSP (solve), int32 hop counts + pred"),
+}
 
 
-N_DEFAULT, K_DEFAULT = 65536, 64
+def load_graphs_module():
+    """The seeded workload generators (pure numpy), loaded from their file
+    without importing the engine package, so the reference arm maps no part
+    of the engine."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("fap_workload_graphs", ROOT / "fastapsp_gb300" / "graphs.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod  # dataclasses look their module up
+    spec.loader.exec_module(mod)
+    return mod
 
 
-def workload(seed_offset=0, n=N_DEFAULT, K=K_DEFAULT):
-    from fastapsp_gb300 import graphs
+def load_workload(name):
+    """(graph, K, graph_id, edge cut) of a solve workload; the partition is
+    the committed one, checked against the generated graph."""
+    import zlib
 
-    return graphs.geometric_knn(n, 3, 1, 1000, seed=20261205 + seed_offset), K
+    wl = WORKLOADS[name]
+    g = getattr(load_graphs_module(), wl["gen"])()
+    z = np.load(ROOT / "tests" / "golden" / "partitions" / f"partition_{wl['part']}.npz")
+    crc = zlib.crc32(np.ascontiguousarray(g.row_offset, np.int32).tobytes())
+    crc = zlib.crc32(np.ascontiguousarray(g.col_val, np.int32).tobytes(), crc)
+    crc = zlib.crc32(np.ascontiguousarray(g.weight, np.float32).tobytes(), crc)
+    if int(z["n"]) != g.n or int(z["m"]) != g.m or int(z["csr_crc"]) != crc:
+        raise RuntimeError(f"partition_{wl['part']}.npz does not belong to the generated graph")
+    return g, wl["K"], z["graph_id"].astype(np.int32), int(z["edge_cut"])
+
+
+def boundary_count(g, gid):
+    """Vertices with an edge to another part (findBoundry, util_preprocess.h:32-58)."""
+    src = np.repeat(np.arange(g.n), np.diff(g.row_offset))
+    cut = gid[src] != gid[g.col_val]
+    b = np.zeros(g.n, bool)
+    b[src[cut]] = True
+    b[g.col_val[cut]] = True
+    return int(b.sum())
+
+
+def workload_config(name, g, K, gid, cut):
+    """The `config` of both arms' lines: a static description of the work."""
+    wl = WORKLOADS[name]
+    return {"workload": wl["desc"], "n": g.n, "m": int(g.m), "K": K, "edge_cut": cut,
+            "boundary_vertices": boundary_count(g, gid),
+            "partition": f"tests/golden/partitions/partition_{wl['part']}.npz (the engine's multilevel partitioner, "
+                         "committed; both arms solve the same parts)",
+            "l2": "L2 flushed (256 MiB write) before every timed step; outputs "
+                  f"{g.n * g.n * 8 / 1e9:.1f} GB",
+            "parallelism": "replicas (one instance per GPU)"}
 
 
 def read_peaks():
@@ -127,23 +193,45 @@ def part_stats(eng, K, n):
     addmin_mp = int(((subs - bdys) * bdys).sum() * n)
     ld = ((subs + 63) // 64) * 64
     addmin_fw = int((ld.astype(np.float64) ** 3).sum())
-    rounds = int(ld.max() // 64)
-    return subs, bdys, addmin_mp, addmin_fw, rounds
+    return subs, bdys, addmin_mp, addmin_fw
 
 
-def run_ours(args, rank, world, local_rank):
+def pinned_host(shape, dtype):
+    """Page-locked host rows of exactly `shape` (registered numpy memory; the
+    caching pinned allocator would round each buffer up to a power of two)."""
+    import torch
+
+    arr = np.empty(shape, dtype)
+    arr.reshape(-1)[:: max(1, 4096 // arr.itemsize)] = 0  # commit the pages before registering
+    t = torch.from_numpy(arr)
+    cr = torch.cuda.cudart()
+    if hasattr(cr, "cudaHostRegister"):
+        rc = cr.cudaHostRegister(t.data_ptr(), t.numel() * t.element_size(), 3)  # portable | mapped
+        if int(rc) == 0:
+            return t, lambda: cr.cudaHostUnregister(t.data_ptr())
+    return torch.empty(shape, dtype=t.dtype, pin_memory=True), lambda: None
+
+
+def run_solve(args, name, rank, world, local_rank):
+    """Device-resident solve of a whole workload graph (value), the same
+    through the C ABI with host buffers (e2e), rooflines, the plain form."""
     import torch
 
     import fastapsp_gb300 as fap
 
     torch.cuda.set_device(local_rank)
     dev = local_rank
-    g, K = workload(seed_offset=rank, n=args.n, K=args.K)
-    gid, cut = fap.partition(g.row_offset, g.col_val, K)
+    wl = WORKLOADS[name]
+    g, K, gid, cut = load_workload(name)
     n = g.n
-    eng = fap.Engine(n, g.row_offset, g.col_val, g.weight, K, graph_id=gid, dtype=fap.DTYPE_I32, device=dev)
-    subs, bdys, addmin_mp, addmin_fw, rounds = part_stats(eng, K, n)
-    dist = torch.empty((n, n), dtype=torch.int32, device="cuda")
+    dtype = fap.DTYPE_F32 if wl["dtype"] == "f32" else fap.DTYPE_I32
+    tdt = torch.float32 if dtype == fap.DTYPE_F32 else torch.int32
+    options = {fap._lib.OPT_SSSP_FP64: wl["fp64_sssp"]} if dtype == fap.DTYPE_F32 else {}
+    eng = fap.Engine(n, g.row_offset, g.col_val, g.weight, K, graph_id=gid, dtype=dtype, device=dev)
+    for o, v in options.items():
+        eng.set_option(o, v)
+    subs, bdys, addmin_mp, addmin_fw = part_stats(eng, K, n)
+    dist = torch.empty((n, n), dtype=tdt, device="cuda")
     pred = torch.empty((n, n), dtype=torch.int32, device="cuda")
     flush = torch.empty(64 << 20, dtype=torch.int32, device="cuda")  # 256 MiB > L2
     stream = torch.cuda.current_stream()
@@ -155,10 +243,9 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    # the first solve tuned the SSSP near-far step; later engines on the same
-    # graph (the e2e loop) reuse it instead of tuning again
-    tuned_delta = eng.get_option(fap._lib.OPT_SSSP_DELTA)
-    tuned_lanes = eng.get_option(fap._lib.OPT_SSSP_LANES)
+    # the first solve tuned the SSSP; later engines on the same graph (the
+    # e2e loop) take the tuned values instead of tuning again
+    tuned = {o: eng.get_option(o) for o in (fap._lib.OPT_SSSP_DELTA, fap._lib.OPT_SSSP_LANES)}
     step_ms, phase = [], []
     if world > 1:
         torch.distributed.barrier()
@@ -186,38 +273,38 @@ def run_ours(args, rank, world, local_rank):
     ms_per_step = total_ms / args.steps
     value = world * float(n) * n / (ms_per_step / 1e3)
 
-    # phase times (device events inside the captured graph)
     ph = {k: statistics.mean(p[k] for p in phase) for k in phase[0]}
     sssp_stats = eng.sssp_stats()
     launches_per_step = eng.last_launches()  # kernels of one solve (counted by the engine)
-    # roofline of the dominant kernel (min-plus) against the add-min issue peak
+    f32 = dtype == fap.DTYPE_F32
+    # add-min peaks from registers, measured in this run: int32 DPX add-min,
+    # and the form the min-plus runs (int32 with argmin, or FP32 with argmin)
     peak_dpx = eng_ctx_peak(fap, dev, 0)
-    peak_arg = eng_ctx_peak(fap, dev, 2)
+    peak_mp = eng_ctx_peak(fap, dev, 3 if f32 else 2)
+    peak_fw = eng_ctx_peak(fap, dev, 3 if f32 else 0)
+
     def rate(x, ms):
         return x / (ms / 1e3) if ms and ms > 0 else float("nan")
 
-    mp_rate = rate(addmin_mp, ph["min_plus"])
-    fw_rate = rate(addmin_fw, ph["floyd"])
     peaks, peak_src = read_peaks()
     hbm = float(peaks.get("hbm_gbs", HBM_PEAK_FALLBACK))
     srcs = int(bdys.sum())
     sssp_bytes = srcs * (4 * (n + 1) + 8 * g.m + 8 * n)
-    sssp_gbs = rate(sssp_bytes, ph["sssp"]) / 1e9
     mp_bytes = int(((subs - bdys) * n * 8).sum() + (bdys * n * 8).sum())  # C written + B read once
     mp_gbs = rate(mp_bytes, ph["min_plus"]) / 1e9
-    # add-min steps the strip kernel actually ran (it skips the k-steps whose B
-    # row or A column is unreached over a tile): one more solve with counters
+    # add-min steps the strip kernels actually ran (they skip the k-steps whose
+    # B row or A column is unreached over a tile): one more solve with counters
     eng.minplus_counters(reset=True)
-    eng.solve(dist, pred, fap.MODE_BATCHED, stream=sptr)
+    step()
     torch.cuda.synchronize()
     mpc = eng.minplus_counters(reset=True)
-    executed = mpc["active_steps"] * 128 * 128  # upper bound: full 128x128 tiles
+    executed = int(mpc["executed_addmins"])
 
-    # plain form (per-part launches) on the same graph, for batched-vs-plain
-    plain_ms = []
-    for _ in range(2 if args.plain else 0):
+    # plain form (one launch sequence per part, the reference's loop) on the
+    # same graph, for batched-vs-plain
+    plain_ms = float("nan")
+    if args.plain:
         eng.solve(dist, pred, fap.MODE_PLAIN, stream=sptr)
-    for _ in range(2 if args.plain else 0):
         flush.fill_(1)
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
@@ -225,91 +312,93 @@ def run_ours(args, rank, world, local_rank):
         eng.solve(dist, pred, fap.MODE_PLAIN, stream=sptr)
         b.record(stream)
         b.synchronize()
-        plain_ms.append(a.elapsed_time(b))
-    plain_ms = statistics.mean(plain_ms) if plain_ms else float("nan")
+        plain_ms = a.elapsed_time(b)
     eng.close()
     del dist, pred
     torch.cuda.empty_cache()
 
     # end to end through the public C ABI with host buffers: per step the CSR
-    # goes host->device (fap_create from pinned arrays) and the full result
-    # rows come back device->host into pinned buffers.
+    # goes host->device (fap_create from page-locked arrays) and the full
+    # result rows come back device->host into page-locked rows.
     ro_h = torch.from_numpy(g.row_offset).pin_memory()
     col_h = torch.from_numpy(g.col_val).pin_memory()
     w_h = torch.from_numpy(g.weight).pin_memory()
     gid_h = torch.from_numpy(gid).pin_memory()
-    shape = (n, n) if args.e2e_steps > 0 else (1, 1)
-    dist_h = torch.empty(shape, dtype=torch.int32, pin_memory=True)
-    pred_h = torch.empty(shape, dtype=torch.int32, pin_memory=True)
     e2e_ms = []
-    for i in range((1 + args.e2e_steps) if args.e2e_steps > 0 else 0):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e = fap.Engine(n, ro_h.numpy(), col_h.numpy(), w_h.numpy(), K, graph_id=gid_h.numpy(),
-                       dtype=fap.DTYPE_I32, device=dev)
-        e.set_option(fap._lib.OPT_SSSP_DELTA, tuned_delta)
-        e.set_option(fap._lib.OPT_SSSP_LANES, tuned_lanes)
-        e.solve(dist_h, pred_h, fap.MODE_BATCHED)
-        e.close()
-        t1 = time.perf_counter()
-        if i > 0:
-            e2e_ms.append((t1 - t0) * 1e3)
+    if args.e2e_steps > 0:
+        npdt = np.float32 if f32 else np.int32
+        dist_h, free_d = pinned_host((n, n), npdt)
+        pred_h, free_p = pinned_host((n, n), np.int32)
+        for i in range(1 + args.e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e = fap.Engine(n, ro_h.numpy(), col_h.numpy(), w_h.numpy(), K, graph_id=gid_h.numpy(),
+                           dtype=dtype, device=dev)
+            for o, v in {**options, **tuned}.items():
+                e.set_option(o, v)
+            e.solve(dist_h, pred_h, fap.MODE_BATCHED)
+            e.close()
+            t1 = time.perf_counter()
+            if i > 0:
+                e2e_ms.append((t1 - t0) * 1e3)
+        free_d()
+        free_p()
+        del dist_h, pred_h
     e2e_ms_step = statistics.mean(e2e_ms) if e2e_ms else float("nan")
     h2d = int(g.row_offset.nbytes + g.col_val.nbytes + g.weight.nbytes + gid.nbytes)
     d2h = int(n) * n * 8
 
+    traffic_scale = MP_TRAFFIC_PER_BYTE.get(name)
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {
-            "workload": f"directed 3-NN geometric graph, n={n}, int weights U[1,1000], K={K} parts, "
-                        f"all parts solved (solveSubGraph 1..{K} rows), int32 dist + pred",
-            "n": n, "m": int(g.m), "K": K, "edge_cut": cut, "boundary_vertices": srcs,
-            "mode": "batched (one launch per phase, CUDA graph)",
-            "sssp_delta": tuned_delta,
-            "sssp_lanes": int(tuned_lanes),
-            "l2": f"L2 flushed (256 MiB write) before every timed step; outputs {n * n * 8 / 1e9:.1f} GB",
-            "parallelism": f"replicas x{world}",
-        },
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if f32 else "int32", "data": "synthetic",
+        "config": workload_config(name, g, K, gid, cut),
+        "mode": "batched (one launch per phase, CUDA graph)",
+        "arithmetic": ("SSSP exact (FP64 option), rounded once to FP32; FW and min-plus in FP32" if f32 and
+                       wl["fp64_sssp"] else "f32 (the reference's)" if f32 else "int32 (exact)"),
+        "tuning": {"sssp_delta": tuned[fap._lib.OPT_SSSP_DELTA],
+                   "sssp_lanes": int(tuned[fap._lib.OPT_SSSP_LANES])},
         "e2e": {"value": world * float(n) * n / (e2e_ms_step / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms_step,
-                "what": "fap_create (CSR from pinned host) + fap_solve into pinned host rows + fap_destroy"
-                    " (SSSP step set to the value tuned on this graph)"},
+                "what": "fap_create (CSR from page-locked host arrays) + fap_solve into page-locked host rows "
+                        "(n x n distances + predecessors) + fap_destroy, SSSP settings as tuned on this graph"},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {
-            # The min-plus skips the k-steps that cannot change a tile (unreached B row
-            # or A column), so on this graph its add-min count is data-dependent and
-            # small; what it must always do is write the n x n rows: HBM-bound.
+            # What the min-plus must always do is write the n x n rows (its
+            # add-min work is data-dependent: steps that cannot change a tile
+            # are skipped), so its roofline is HBM; alu_view gives the same
+            # launch against the add-min issue rate of its arithmetic.
             "kernel": "mp_strip_kernel (min-plus of the inner rows and decode of their own-part columns)",
             "bound": "hbm",
             "achieved": mp_gbs, "peak": hbm, "unit": "GB/s", "frac": mp_gbs / hbm,
             "peak_source": peak_src,
             "algorithmic_bytes_per_launch": mp_bytes,
-            # DRAM bytes per launch: an ncu capture of the same launch at n=24,576 read + wrote
-            # this many bytes per output byte; output and work grow with n^2, so the full
-            # launch is scaled by its output bytes.
-            "traffic": MP_TRAFFIC_PER_OUTPUT_BYTE * mp_bytes,
-            "traffic_source": f"ncu capture at n=24,576 ({MP_TRAFFIC_PER_OUTPUT_BYTE} DRAM bytes per "
-                              "algorithmic byte), scaled",
+            "traffic": traffic_scale * mp_bytes if traffic_scale else None,
+            "traffic_source": (f"ncu capture of the same kernel on a smaller case of this workload "
+                               f"({traffic_scale} DRAM bytes per algorithmic byte), scaled")
+                              if traffic_scale else "no capture of this workload",
             "alu_view": {
                 "executed_addmins_per_launch": executed,
-                "achieved": rate(executed, ph["min_plus"]) / 1e9, "peak": peak_dpx / 1e9,
-                "unit": "Gaddmin/s", "frac": rate(executed, ph["min_plus"]) / peak_dpx,
+                "achieved": rate(executed, ph["min_plus"]) / 1e9, "peak": peak_mp / 1e9,
+                "unit": "Gaddmin/s", "frac": rate(executed, ph["min_plus"]) / peak_mp,
                 "dense_addmins_per_launch": addmin_mp,
-                "dense_equivalent_rate": mp_rate / 1e9,
                 "strip_tiles": mpc["tiles"], "tiles_without_active_step": mpc["empty_tiles"],
-                "peak_source": "fap_addmin_peak mode 0 (int32 DPX add-min from registers), measured in this run",
-                "peak_with_argmin": peak_arg / 1e9,
+                "peak_source": ("fap_addmin_peak mode 3 (FP32 add-min keeping the argmin)" if f32 else
+                                "fap_addmin_peak mode 2 (int32 add-min keeping the argmin)")
+                               + " from registers, measured in this run",
+                "peak_dpx_int32": peak_dpx / 1e9,
             },
         },
-        "roofline_fw": {"achieved": fw_rate / 1e9, "peak": peak_dpx / 1e9, "unit": "Gaddmin/s",
-                        "frac": fw_rate / peak_dpx, "algorithmic_addmins": addmin_fw,
-                        "note": "dense count (sum of ld^3); the remaining-tile kernel skips unreached "
-                                "steps, so this is a dense-equivalent rate"},
-        "roofline_sssp": {"bound": "hbm", "achieved": sssp_gbs, "peak": hbm, "unit": "GB/s",
-                          "frac": sssp_gbs / hbm, "algorithmic_bytes": sssp_bytes, "peak_source": peak_src},
+        "roofline_fw": {"achieved": rate(addmin_fw, ph["floyd"]) / 1e9, "peak": peak_fw / 1e9,
+                        "unit": "Gaddmin/s", "frac": rate(addmin_fw, ph["floyd"]) / peak_fw,
+                        "algorithmic_addmins": addmin_fw,
+                        "note": "dense count (sum of ld^3 over the parts' padded matrices) against "
+                                + ("fap_addmin_peak mode 3 (FP32)" if f32 else "fap_addmin_peak mode 0 (DPX)")},
+        "roofline_sssp": {"bound": "hbm", "achieved": rate(sssp_bytes, ph["sssp"]) / 1e9, "peak": hbm,
+                          "unit": "GB/s", "frac": rate(sssp_bytes, ph["sssp"]) / 1e9 / hbm,
+                          "algorithmic_bytes": sssp_bytes, "peak_source": peak_src},
         "phase_ms": ph,
         "sssp_stats": sssp_stats,
         "plain_form": {"ms_per_step": plain_ms, "batched_speedup": plain_ms / ms_per_step},
@@ -329,13 +418,10 @@ def eng_ctx_peak(fap, dev, mode):
     return _PEAK_CACHE[mode]
 
 
-def cpu_sample(part, g, K, gid, pre, rows):
+def cpu_sample(oracle, part, g, gid, pre, rows):
     """The reference's CPU algorithm on one part with the min-plus limited to
-    `rows` inner rows; returns (extrapolated part seconds, measured seconds)."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-
-    n = g.n
+    `rows` inner rows; returns (extrapolated part seconds, measured seconds,
+    part rows)."""
     sub = int(pre["ver_num"][part])
     bdy = int(pre["bdy_num"][part])
     inner = sub - bdy
@@ -348,101 +434,68 @@ def cpu_sample(part, g, K, gid, pre, rows):
     return est, measured, sub
 
 
-def run_reference(args):
+def load_oracle(threads):
     sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-
-    import fastapsp_gb300 as fap
+    import oracle  # test infrastructure: the CPU baseline, never the measured product
 
     oracle.build()
+    oracle.set_threads(threads)
+    return oracle
+
+
+def cpu_baseline(name, seconds, ref_rows):
+    """The oracle restatement of the reference's CPU path on whole parts, in
+    order, until about `seconds` of host work; distances/s extrapolated."""
     cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
-    g, K = workload()
-    gid, _ = fap.partition(g.row_offset, g.col_val, K)
+    oracle = load_oracle(cores)
+    g, K, gid, _ = load_workload(name)
+    pre = oracle.preprocess(K, gid, g.row_offset, g.col_val)
+    rows = est = meas = 0.0
+    parts = 0
+    for part in range(1, K + 1):
+        e_p, m_p, sub = cpu_sample(oracle, part, g, gid, pre, ref_rows)
+        rows, est, meas, parts = rows + sub, est + e_p, meas + m_p, parts + 1
+        if meas >= seconds:
+            break
+    return {"value": rows * g.n / est, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"parts 1..{parts} of {K}: SSSP (all boundary sources, OpenMP), full FW, min-plus on "
+                      f"{ref_rows} inner rows per part extrapolated per add-min; {meas:.1f} s measured"}
+
+
+def run_reference(args):
+    """The reference's CPU algorithm (the oracle restatement of fapGraph::run's
+    CPU branch, pinned bit for bit to the reference's own fap.cpp) on the same
+    workload and parts as the engine's line, on all host cores: per step one
+    part (SSSP from all its boundary vertices, its FW, and the min-plus on its
+    first rows, extrapolated per add-min to all of its inner rows)."""
+    name = args.config
+    cores = os.cpu_count() or 1
+    oracle = load_oracle(cores)
+    g, K, gid, cut = load_workload(name)
     pre = oracle.preprocess(K, gid, g.row_offset, g.col_val)
     rates, meas = [], []
     for i in range(args.warmup + args.steps):
         part = 1 + (i % K)
-        est, m, sub = cpu_sample(part, g, K, gid, pre, args.ref_rows)
+        est, m, sub = cpu_sample(oracle, part, g, gid, pre, args.ref_rows)
         if i >= args.warmup:
             rates.append(sub * g.n / est)
             meas.append(m)
     value = statistics.mean(rates)
-    sample = (f"per step one part of the 64: SSSP from all its boundary vertices (OpenMP), its full "
-              f"Floyd-Warshall, and the min-plus on the first {args.ref_rows} inner rows; the part's "
-              f"time is extrapolated per add-min to all its inner rows; distances/s = part rows x n "
-              f"/ part time")
+    sample = (f"per step one part of the {K} (parts in order): SSSP from all its boundary vertices (OpenMP), "
+              f"its full Floyd-Warshall, and the min-plus on its first {args.ref_rows} inner rows; the part's "
+              f"time is extrapolated per add-min to all its inner rows; distances/s = part rows x n / part time")
     res = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": statistics.mean(meas) * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (reference arithmetic; integer weights exact)",
+        "vs_baseline": None, "dtype": WORKLOADS[name]["dtype"].replace("i32", "int32"),
         "data": "synthetic",
-        "config": {"workload": f"directed 3-NN geometric graph, n={g.n}, int weights U[1,1000], K={K} parts",
-                   "n": g.n, "m": int(g.m), "K": K},
+        "config": workload_config(name, g, K, gid, cut),
+        "arithmetic": "f32 (the reference's; integer weights are exact)",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return res
-
-
-def _device_solve_rate(fap, torch, g, K, dtype, steps, warmup, mode=None, options=None):
-    """Device-resident solve of a whole graph: (ms per solve, engine, dist, pred)."""
-    mode = fap.MODE_BATCHED if mode is None else mode
-    gid, cut = fap.partition(g.row_offset, g.col_val, K)
-    eng = fap.Engine(g.n, g.row_offset, g.col_val, g.weight, K, graph_id=gid, dtype=dtype)
-    for opt, val in (options or {}).items():
-        eng.set_option(opt, val)
-    tdt = torch.int32 if dtype == fap.DTYPE_I32 else torch.float32
-    dist = torch.empty((g.n, g.n), dtype=tdt, device="cuda")
-    pred = torch.empty((g.n, g.n), dtype=torch.int32, device="cuda")
-    flush = torch.empty(64 << 20, dtype=torch.int32, device="cuda")
-    stream = torch.cuda.current_stream()
-    for _ in range(warmup):
-        eng.solve(dist, pred, mode, stream=stream.cuda_stream)
-    times = []
-    for _ in range(steps):
-        flush.fill_(1)
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        eng.solve(dist, pred, mode, stream=stream.cuda_stream)
-        b.record(stream)
-        b.synchronize()
-        times.append(a.elapsed_time(b))
-    return statistics.mean(times), eng, dist, pred, gid, cut
-
-
-def run_c1(args):
-    """128x128 grid (spanning tree + p=0.6 edges), unweighted, K=16, int32,
-    full solve(); distances checked bit for bit against the oracle's
-    Dijkstra (the reference's dijkstra_path) on sampled rows."""
-    import torch
-
-    import fastapsp_gb300 as fap
-    from fastapsp_gb300 import graphs
-
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-
-    g = graphs.grid_graph()
-    ms, eng, dist, pred, gid, cut = _device_solve_rate(fap, torch, g, 16, fap.DTYPE_I32, args.steps, args.warmup)
-    plain_ms, *_ = _device_solve_rate(fap, torch, g, 16, fap.DTYPE_I32, 2, 1, mode=fap.MODE_PLAIN)
-    mapping = eng.mapping()
-    rows = np.random.default_rng(0).choice(g.n, size=64, replace=False)
-    d = dist[torch.from_numpy(rows).cuda()].cpu().numpy()
-    exact = True
-    for i, r in enumerate(rows):
-        rd, _ = oracle.dijkstra_path(int(mapping[r]), g.row_offset, g.col_val, g.weight)
-        ref = np.where(rd >= 1e8, 1 << 30, rd).astype(np.int64)
-        exact = exact and np.array_equal(d[i].astype(np.int64), ref)
-    return {"config": "c1", "metric": METRIC, "value": g.n * g.n / (ms / 1e3), "unit": UNIT,
-            "ms_per_step": ms, "dtype": "int32", "n": g.n, "m": g.m, "K": 16, "edge_cut": cut,
-            "plain_ms": plain_ms, "batched_speedup": plain_ms / ms,
-            "parity": f"64 sampled rows bit-exact vs the reference's Dijkstra: {exact}",
-            "phase_ms": eng.last_times(), "sssp_stats": eng.sssp_stats(),
-            "sssp_delta": eng.get_option(fap._lib.OPT_SSSP_DELTA),
-            "sssp_lanes": int(eng.get_option(fap._lib.OPT_SSSP_LANES))}
 
 
 def run_c3(args):
@@ -503,53 +556,6 @@ def run_c3(args):
             "instances": len(mats), "addmins": work, "frac_of_dpx_peak": work / (ms_b / 1e3) / peak}
 
 
-def run_c4(args):
-    """Road-like FP32 graph, 114,599 vertices, K=128, full batched APSP;
-    error against FP64 Dijkstra on 4,096 sampled sources."""
-    import torch
-
-    import fastapsp_gb300 as fap
-    from fastapsp_gb300 import graphs
-
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-
-    g = graphs.road_like()
-    fp64 = 0 if args.c4_faithful else 1
-    ms, eng, dist, pred, gid, cut = _device_solve_rate(
-        fap, torch, g, 128, fap.DTYPE_F32, args.steps, args.warmup,
-        options={fap._lib.OPT_SSSP_FP64: fp64})
-    phase = eng.last_times()
-    stats = eng.sssp_stats()
-    delta = eng.get_option(fap._lib.OPT_SSSP_DELTA)
-    mapping = eng.mapping()
-    inv = np.empty_like(mapping)
-    inv[mapping] = np.arange(g.n)
-    srcs = np.random.default_rng(4).choice(g.n, size=args.c4_sources, replace=False)
-    rows = torch.from_numpy(inv[srcs].astype(np.int64)).cuda()
-    d = dist[rows].cpu().numpy()
-    eng.close()
-    del dist, pred
-    torch.cuda.empty_cache()
-    from concurrent.futures import ThreadPoolExecutor
-
-    def err(i):
-        d64 = oracle.dijkstra_f64(int(srcs[i]), g.row_offset, g.col_val, g.weight)
-        f = d64 < 1e299
-        if not np.array_equal(f, d[i] < 1e8):
-            return float("inf")
-        return float(np.max(np.abs(d[i][f] - d64[f]) / np.maximum(d64[f], 1e-30)))
-
-    with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
-        errs = list(ex.map(err, range(len(srcs))))
-    return {"config": "c4", "metric": METRIC, "value": g.n * g.n / (ms / 1e3), "unit": UNIT,
-            "ms_per_step": ms, "dtype": "f32", "n": g.n, "m": g.m, "K": 128, "edge_cut": cut,
-            "sssp": "FP64 search, rounded once" if fp64 else "FP32 (reference arithmetic)",
-            "sampled_sources": len(srcs), "max_rel_err_vs_fp64": max(errs),
-            "mean_of_row_max_rel_err": float(np.mean(errs)), "phase_ms": phase,
-            "sssp_stats": stats, "sssp_delta": delta}
-
-
 def run_c5(args):
     """256 random 4-regular digraphs (n U[256,1024], FP32 w U(0.5,2)): batched
     FW with predecessors (forward), loss = sum of D[s,t] over 10,000 pairs,
@@ -608,7 +614,7 @@ def run_c5(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -616,28 +622,29 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="host work of the cpu_baseline sample (whole parts until this is reached)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--n", type=int, default=N_DEFAULT, help="vertices (profiling cases only)")
-    ap.add_argument("--K", type=int, default=K_DEFAULT, help="parts (profiling cases only)")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
-    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
-                    help="c2 (default) is the headline workload; the others print their own line")
-    ap.add_argument("--c4-sources", type=int, default=4096)
-    ap.add_argument("--c4-faithful", action="store_true",
-                    help="c4 with FP32 SSSP arithmetic (the reference's) instead of FP64")
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c4",
+                    help="c4 (default, the largest single-GPU workload) is the headline; c1/c2 print the same "
+                         "line for their graphs, c3/c5 their own lines")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
     if args.impl == "reference":
+        if args.config not in WORKLOADS:
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched "
+                                  "standalone FW or adjoint path; c3/c5 have no reference arm"}))
+            return
         if rank == 0:
             print(json.dumps(run_reference(args)))
         return
-    if args.config != "c2":
+    if args.config not in WORKLOADS:
         import torch
 
         torch.cuda.set_device(local_rank)
-        fn = {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config]
+        fn = {"c3": run_c3, "c5": run_c5}[args.config]
         print(json.dumps(fn(args)))
         return
 
@@ -647,34 +654,10 @@ def main():
 
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
-    res = run_ours(args, rank, world, local_rank)
+    res = run_solve(args, args.config, rank, world, local_rank)
     if rank == 0:
         if not args.no_cpu_baseline:
-            sys.path.insert(0, str(ROOT / "oracle"))
-            import oracle
-
-            import fastapsp_gb300 as fap
-
-            oracle.build()
-            cores = os.cpu_count() or 1
-            oracle.set_threads(cores)
-            g, K = workload()
-            gid, _ = fap.partition(g.row_offset, g.col_val, K)
-            pre = oracle.preprocess(K, gid, g.row_offset, g.col_val)
-            # parts in order until about --cpu-seconds of host work
-            rows = est = meas = 0.0
-            parts = 0
-            for part in range(1, K + 1):
-                e_p, m_p, sub = cpu_sample(part, g, K, gid, pre, args.ref_rows)
-                rows, est, meas, parts = rows + sub, est + e_p, meas + m_p, parts + 1
-                if meas >= args.cpu_seconds:
-                    break
-            res["cpu_baseline"] = {
-                "value": rows * g.n / est, "unit": UNIT, "cores": cores, "kind": "port",
-                "sample": f"parts 1..{parts} of {K}: SSSP (all boundary sources, OpenMP), full FW, "
-                          f"min-plus on {args.ref_rows} inner rows per part extrapolated per add-min; "
-                          f"{meas:.1f} s measured",
-            }
+            res["cpu_baseline"] = cpu_baseline(args.config, args.cpu_seconds, args.ref_rows)
         print(json.dumps(res))
     if world > 1:
         import torch.distributed as dist

@@ -1520,9 +1520,10 @@ static int apply_partition(fap_engine *e, const int32_t *graph_id) {
                             vn.data(), vo.data(), bn.data(), bo.data(), nullptr);
   if (rc != FAP_OK) return rc;
   DeviceGuard g(e->device);
-  // every solve ends with its streams joined and synchronized; this waits for
-  // anything still queued on the engine's own stream
-  FAP_CUDA(cudaStreamSynchronize(e->stream));
+  // the plans and the device tables below may still be in use by work queued
+  // on any stream (the engine's own, its side and copy streams, or a caller's
+  // stream an earlier solve ran on): wait for the whole device first
+  FAP_CUDA(cudaDeviceSynchronize());
   e->plans.clear();
   if (n > 0) {
     const size_t bytes = (size_t)n * sizeof(int32_t);

@@ -575,7 +575,8 @@ __global__ void __launch_bounds__(kThreads, 2)
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
 // Work counters of the strip min-plus (diagnostics): [tiles, tiles with no
-// active step, active steps summed over tiles], summed per CTA.
+// active step, add-mins executed (active steps x the tile's 128 x TN
+// outputs, summed over tiles)], summed per CTA.
 __device__ unsigned long long g_strip_counters[3];
 
 constexpr int kStripTiles = 16;  // a strip spans kStripTiles x 128 columns
@@ -860,7 +861,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
     const int nact = __popcll(mlo) + __popcll(mhi);
     n_tiles++;
     n_empty += nact == 0;
-    n_steps += nact;
+    n_steps += (unsigned long long)nact * kTile * TN;
     if (PRED && nact == s.K && s.K > 0)  // every step active: all rows, 16-byte copies spread over the CTA
       strip_load_rows<TN>(reinterpret_cast<unsigned *>(Bps + TN), reinterpret_cast<const unsigned *>(s.Bp),
                           s.ldbp, s.K, s.N, kseg, jt * TN, vec_bp, 0xffffffffu);

@@ -15,8 +15,9 @@
 //
 // In host code the array's name is only a host-side stand-in; its device
 // address is fetched with cudaGetSymbolAddress once per device (with that
-// device current) on the first call there.  That first call should therefore
-// come before any stream capture.  All calls on a device share the array and
+// device current) on the first call there, which also raises the SSSP
+// kernels' shared-memory limits on that device.  That first call should
+// therefore come before any stream capture.  All calls on a device share the array and
 // it keeps the last call's contents, so every call clears the parts that
 // must start at zero (the status words; the kernel clears its own tables);
 // calls whose work overlaps on the GPU (different
@@ -59,6 +60,13 @@ int scratch_address(int dev, unsigned char **out, int *sms) {
     e = cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess)
       return fapi::set_error(FAP_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+    // The SSSP kernels need more dynamic shared memory than the 48 KiB
+    // default; raise their limits on this device here, since a caller of
+    // this entry point may never have created an engine (which does the same).
+    // Setting a function attribute allocates nothing.
+    e = fapk::init_sssp_kernels();
+    if (e != cudaSuccess)
+      return fapi::set_error(FAP_ERR_CUDA, std::string("SSSP kernel attributes: ") + cudaGetErrorString(e));
     g_addr[dev] = static_cast<unsigned char *>(p);
     g_sms[dev] = count;
   }

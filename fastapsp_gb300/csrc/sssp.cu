@@ -236,6 +236,7 @@ __global__ void __launch_bounds__(kSsspThreads, ACC64 ? 2 : 1)
   constexpr int VPW = 32 / LANES;  // lane groups (frontier vertices) per warp
   constexpr int R = 2;             // frontier vertices per lane group per sweep
   constexpr int G = 8;             // edges per lane group in flight (<= LANES)
+  static_assert(G <= LANES, "lane q of a group files edge target q: every edge in flight needs a lane");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / LANES, sl = lane % LANES;
   const unsigned group_mask = LANES == 32 ? 0xffffffffu : (((1u << LANES) - 1u) << (LANES * sub));

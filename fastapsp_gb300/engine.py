@@ -165,10 +165,10 @@ class Engine:
 
     def minplus_counters(self, reset: bool = True):
         """Strip min-plus work counters since the last reset: tiles, tiles with
-        no active k-step, active k-steps over all tiles."""
+        no active k-step, add-mins executed (active k-steps x tile outputs)."""
         v = (C.c_uint64 * 3)()
         check(lib().fap_minplus_counters(self._h, v, int(bool(reset))), "fap_minplus_counters")
-        return dict(zip(["tiles", "empty_tiles", "active_steps"], list(v)))
+        return dict(zip(["tiles", "empty_tiles", "executed_addmins"], list(v)))
 
     def sssp_stats(self):
         """Counters of the last solve's SSSP phase."""

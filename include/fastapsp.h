@@ -214,8 +214,9 @@ int fap_last_times(const fap_engine *e, double *times5);
 int fap_last_launches(const fap_engine *e, int64_t *count);
 /* Work counters of the min-plus strip kernel on the engine's GPU since the
  * last reset (no reference counterpart; diagnostics of the sparsity skip):
- * [128x128 tiles, tiles with no active k-step, active k-steps summed over
- * tiles].  reset != 0 clears them after reading. */
+ * [tiles, tiles with no active k-step, add-mins executed: active k-steps x
+ * the tile's outputs (128 x 64 or 128 x 128), summed over tiles].  reset != 0
+ * clears them after reading. */
 int fap_minplus_counters(fap_engine *e, uint64_t *out3, int32_t reset);
 
 /* ---- standalone kernels on caller device memory ------------------------- */
@@ -293,7 +294,8 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes,
  * scratch does not fit (about n > 460,000 vertices) are rejected with
  * FAP_ERR_RANGE.  No allocation: neither cudaMalloc/cudaFree nor an
  * allocating library call.  The first call on a device looks up the array's
- * device address (so make that first call before any stream capture).  Calls
+ * device address and raises the SSSP kernels' shared-memory limits there (so
+ * make that first call before any stream capture); no engine is needed.  Calls
  * share the array: each call clears what must start at zero, and calls that
  * overlap on the GPU race, so serialize them.  The call synchronizes
  * `stream` before returning its status. */
