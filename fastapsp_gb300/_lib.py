@@ -30,6 +30,8 @@ OPT_SSSP_DELTA = 2
 OPT_AUTOTUNE = 3
 OPT_SSSP_LANES = 4
 OPT_TILE_COLS = 5
+OPT_SSSP_METHOD = 6
+OPT_HOST_RESULTS = 7
 INF_I32 = 1 << 30
 
 _i32 = C.c_int32

@@ -102,6 +102,10 @@ struct Plan {
   void *bdist = nullptr;
   int32_t *bpred = nullptr;
   std::vector<int64_t> brow_offs;
+  // Page-locked host rows that the plan copies its results to, group by
+  // group on the copy stream as each group finishes (null: none).
+  void *hdist = nullptr;
+  int32_t *hpred = nullptr;
   std::vector<const void *> sig;  // engine work buffers the tables point into
   // device tables (one allocation)
   DevBuf tables;
@@ -113,6 +117,10 @@ struct Plan {
     // the autotuner; swapped with the above when that width wins
     const SsspBatch *batches_alt = nullptr;
     int nbatches_alt = 0;
+    // boundary-graph SSSP: step-2 jobs and each batch's sources as boundary indices
+    const fapk::BgJob *bjobs = nullptr;
+    int nbjobs = 0;
+    const int32_t *bsrc = nullptr;
     // build / decode
     const PartDesc *pdesc = nullptr;
     const int64_t *row_begin = nullptr;
@@ -148,6 +156,7 @@ struct Plan {
     int mp_cls_strips[kMaxCls] = {}, mp_cls_max_k[kMaxCls] = {};
     int mp_cls_cols[kMaxCls] = {};  // tile columns the tuner chose (0: the class default)
     int max_sub = 0;  // largest part of the group (bound of the packed form)
+    int64_t out_lo = 0, out_elems = 0;  // the group's result rows: elements [out_lo, out_lo + out_elems)
   };
   std::vector<Group> groups;
   size_t fw_elems = 0;  // FW arena elements needed
@@ -156,6 +165,7 @@ struct Plan {
   int pack = -1;        // packed int32 form: -1 undecided, 0 no, 1 yes
   int sssp_lanes = 32;  // sources per SSSP batch
   int sssp_lanes_alt = 0;  // the other width the autotuner tries (0: none)
+  int bsssp = 0;        // boundary SSSP through the boundary graph (bgraph.cu) instead of the search
   int launches = 0;     // kernels one run of the plan launches
   // graph (batched mode)
   cudaGraphExec_t exec = nullptr;
@@ -199,6 +209,17 @@ struct fap_engine {
   int sssp_lanes = 0;      // sources per SSSP batch: 16, 32, 0 = chosen per solve
   int sssp_lanes_tuned = 0;  // the width the autotuner chose (0: none yet)
   int tile_cols = 0;       // min-plus strip tile columns: 64, 128, 0 = per class
+  int host_results = 0;    // FAP_OPT_HOST_RESULTS: 0 staged when the device has room, 1 direct
+  int sssp_method = 0;     // FAP_OPT_SSSP_METHOD: 0 boundary graph where exact and it fits, 1 search
+  int fix_shift = -1;      // FP32 graphs: every weight is a multiple of 2^-fix_shift and every path
+                           // length below 2^52 of those units (-1: no such shift)
+  // boundary graph (bgraph.cu), built for the current partition on first use
+  bool bg_ready = false;
+  bool bg_ok = false;      // usable: exact arithmetic and both shared-memory tables fit
+  int bg_B = 0, bg_max_sub = 0, bg_nljobs = 0;
+  std::vector<int32_t> bg_bidx;  // vertex -> boundary index (-1: inner vertex)
+  DevBuf bg_tab, bg_L, bg_DS;
+  fapk::BgArgs bg_args{};
   double delta_try = 0;    // step under trial while tuning
   double tuned_ms = 0;     // SSSP time of the chosen step during tuning
   // device graph
@@ -267,6 +288,120 @@ int ensure_sssp_scratch(fap_engine *e, int slots, bool wide = false) {
   if ((st = e->sssp_bits.ensure(std::max<size_t>(fapk::sssp_bits_bytes(e->n) * slots, 4))) != FAP_OK)
     return st;
   e->sssp_slots_alloc = slots;
+  return FAP_OK;
+}
+
+// Host tables of the boundary graph for the current partition (bgraph.cu):
+// the parts, the boundary index of every boundary vertex (boundary vertices
+// in sorted order), each part's local CSR by sorted position with targets as
+// local indices, the cut edges between boundary vertices, the step-1 jobs,
+// and the arenas of the local rows and of the boundary-graph distances.
+// Weights are uint32 (int32 graphs) or 64-bit fixed point (FP32 graphs, in
+// units of 2^-fix_shift, exact).  Sets bg_ok when the method applies.
+int prepare_bgraph(fap_engine *e) {
+  if (e->bg_ready) return FAP_OK;
+  e->bg_ready = true;
+  e->bg_ok = false;
+  const bool wide = e->f32();
+  if (wide && e->fix_shift < 0) return FAP_OK;
+  const int32_t n = e->n, K = e->K;
+  std::vector<fapk::BgPart> parts(K);
+  std::vector<int32_t> bpart;
+  e->bg_bidx.assign(n, -1);
+  int64_t loff = 0;
+  int B = 0, max_sub = 0;
+  for (int q = 1; q <= K; q++) {
+    fapk::BgPart &P = parts[q - 1];
+    P.start = e->ver_offset[q];
+    P.sub = e->ver_num[q];
+    P.bdy = e->bdy_num[q];
+    P.boff = B;
+    P.loff = loff;
+    loff += (int64_t)P.bdy * P.sub;
+    for (int a = 0; a < P.bdy; a++) {
+      e->bg_bidx[e->st2ed[P.start + a]] = B + a;
+      bpart.push_back(q - 1);
+    }
+    B += P.bdy;
+    max_sub = std::max(max_sub, P.sub);
+  }
+  e->bg_B = B;
+  e->bg_max_sub = max_sub;
+  if (B == 0 || fapk::bg_smem_bytes(wide, max_sub) > fapk::kBgSmemMax ||
+      fapk::bg_smem_bytes(wide, B) > fapk::kBgSmemMax)
+    return FAP_OK;
+  auto weight = [&](int64_t j) -> uint64_t {
+    return wide ? (uint64_t)std::ldexp((double)e->w[j], e->fix_shift) : (uint64_t)e->w[j];
+  };
+  std::vector<int32_t> lro(n + 1, 0), lcol, cro(B + 1, 0), ccol;
+  std::vector<uint64_t> lw, cw;
+  lcol.reserve(e->m);
+  lw.reserve(e->m);
+  for (int32_t pos = 0; pos < n; pos++) {
+    const int32_t v = e->st2ed[pos], q = e->graph_id[v];
+    const int32_t start = e->ver_offset[q];
+    for (int32_t j = e->ro[v]; j < e->ro[v + 1]; j++) {
+      const int32_t u = e->col[j];
+      if (e->graph_id[u] == q) {
+        lcol.push_back(e->ed2st[u] - start);
+        lw.push_back(weight(j));
+      } else {  // a cut edge joins two boundary vertices; sorted order = boundary-index order
+        const int32_t bv = e->bg_bidx[v], bu = e->bg_bidx[u];
+        if (bv < 0 || bu < 0) return set_error(FAP_ERR_STATE, "boundary graph: cut edge at an inner vertex");
+        ccol.push_back(bu);
+        cw.push_back(weight(j));
+        cro[bv + 1]++;
+      }
+    }
+    lro[pos + 1] = (int32_t)lcol.size();
+  }
+  for (int i = 0; i < B; i++) cro[i + 1] += cro[i];
+  std::vector<fapk::BgJob> ljobs;
+  for (int q = 0; q < K; q++)
+    for (int a0 = 0; a0 < parts[q].bdy; a0 += fapk::bg_lanes())
+      ljobs.push_back({q, a0, std::min(fapk::bg_lanes(), parts[q].bdy - a0)});
+  e->bg_nljobs = (int)ljobs.size();
+  TableBuilder tb;
+  const size_t o_parts = tb.add(parts.data(), parts.size());
+  const size_t o_bpart = tb.add(bpart.data(), bpart.size());
+  const size_t o_lro = tb.add(lro.data(), lro.size());
+  const size_t o_lcol = tb.add(lcol.data(), lcol.size());
+  const size_t o_cro = tb.add(cro.data(), cro.size());
+  const size_t o_ccol = tb.add(ccol.data(), ccol.size());
+  const size_t o_ljobs = tb.add(ljobs.data(), ljobs.size());
+  size_t o_lw, o_cw;
+  if (wide) {
+    o_lw = tb.add(lw.data(), lw.size());
+    o_cw = tb.add(cw.data(), cw.size());
+  } else {
+    std::vector<uint32_t> lw32(lw.begin(), lw.end()), cw32(cw.begin(), cw.end());
+    o_lw = tb.add(lw32.data(), lw32.size());
+    o_cw = tb.add(cw32.data(), cw32.size());
+  }
+  int rc;
+  const size_t vs = wide ? 8 : 4;
+  if ((rc = e->bg_tab.ensure(std::max<size_t>(tb.bytes.size(), 64))) != FAP_OK ||
+      (rc = e->bg_L.ensure(std::max<size_t>((size_t)loff * vs, 8))) != FAP_OK ||
+      (rc = e->bg_DS.ensure((size_t)B * B * vs)) != FAP_OK)
+    return rc;
+  FAP_CUDA(cudaMemcpy(e->bg_tab.p, tb.bytes.data(), tb.bytes.size(), cudaMemcpyHostToDevice));
+  unsigned char *base = static_cast<unsigned char *>(e->bg_tab.p);
+  fapk::BgArgs &a = e->bg_args;
+  a = fapk::BgArgs{};
+  a.nparts = K;
+  a.parts = reinterpret_cast<const fapk::BgPart *>(base + o_parts);
+  a.B = B;
+  a.bpart = reinterpret_cast<const int32_t *>(base + o_bpart);
+  a.lro = reinterpret_cast<const int32_t *>(base + o_lro);
+  a.lcol = reinterpret_cast<const int32_t *>(base + o_lcol);
+  a.lw = base + o_lw;
+  a.cro = reinterpret_cast<const int32_t *>(base + o_cro);
+  a.ccol = reinterpret_cast<const int32_t *>(base + o_ccol);
+  a.cw = base + o_cw;
+  a.ljobs = reinterpret_cast<const fapk::BgJob *>(base + o_ljobs);
+  a.L = e->bg_L.p;
+  a.DS = e->bg_DS.p;
+  e->bg_ok = true;
   return FAP_OK;
 }
 
@@ -392,7 +527,23 @@ int build_plan(fap_engine *e, Plan &pl) {
   const int B = fapk::fw_block();
   const int64_t n = e->n;
   std::vector<std::vector<int>> groups;
-  if (batched) {
+  if (batched && pl.hdist) {
+    // Results copied to host rows: consecutive parts in groups of about
+    // 8 GB of rows (at most 8 groups), so that the copy of one group's rows
+    // runs while the next group computes.
+    int64_t rows = 0;
+    for (int p : pl.parts) rows += e->ver_num[p];
+    const double bytes = (double)rows * n * 4 * (pl.pred ? 2 : 1);
+    const int ng = (int)std::min<double>(8.0, std::max(1.0, std::ceil(bytes / (8.0 * (1 << 30)))));
+    const int64_t per = (rows + ng - 1) / ng;
+    int64_t acc = 0;
+    groups.emplace_back();
+    for (size_t i = 0; i < pl.parts.size(); i++) {
+      if (acc >= per * (int64_t)groups.size() && !groups.back().empty()) groups.emplace_back();
+      groups.back().push_back((int)i);
+      acc += e->ver_num[pl.parts[i]];
+    }
+  } else if (batched) {
     groups.emplace_back();
     for (size_t i = 0; i < pl.parts.size(); i++) groups[0].push_back((int)i);
   } else {
@@ -421,7 +572,7 @@ int build_plan(fap_engine *e, Plan &pl) {
 
   TableBuilder tb;
   struct GroupOffs {
-    size_t batches, batches_alt, pdesc, row_begin, dec_begin, mp;
+    size_t batches, batches_alt, pdesc, row_begin, dec_begin, mp, bjobs, bsrc;
     std::vector<size_t> diag, panel, rest, rest2;
   };
   std::vector<GroupOffs> goffs(groups.size());
@@ -497,8 +648,25 @@ int build_plan(fap_engine *e, Plan &pl) {
         else mps_wide.push_back(s);
       }
     }
+    {
+      const int first = groups[g].front(), last = groups[g].back();
+      G.out_lo = pl.row_offs[first];
+      G.out_elems = pl.row_offs[last] + (int64_t)e->ver_num[pl.parts[last]] * n - G.out_lo;
+    }
     G.nbatches = (int)batches.size();
     O.batches = tb.add(batches.data(), batches.size());
+    if (pl.bsssp) {  // boundary-graph SSSP: each batch's sources as boundary indices, step-2 jobs
+      std::vector<int32_t> bsrc((size_t)batches.size() * 32, -1);
+      std::vector<fapk::BgJob> bjobs;
+      for (size_t b = 0; b < batches.size(); b++) {
+        for (int l = 0; l < batches[b].count; l++) bsrc[b * 32 + l] = e->bg_bidx[batches[b].src[l]];
+        for (int l0 = 0; l0 < batches[b].count; l0 += fapk::bg_lanes())
+          bjobs.push_back({(int32_t)b, l0, std::min(fapk::bg_lanes(), batches[b].count - l0)});
+      }
+      G.nbjobs = (int)bjobs.size();
+      O.bjobs = tb.add(bjobs.data(), bjobs.size());
+      O.bsrc = tb.add(bsrc.data(), bsrc.size());
+    }
     G.nbatches_alt = (int)batches_alt.size();
     O.batches_alt = tb.add(batches_alt.data(), batches_alt.size());
     G.nparts = (int)pdesc.size();
@@ -603,6 +771,10 @@ int build_plan(fap_engine *e, Plan &pl) {
     GroupOffs &O = goffs[g];
     G.batches = reinterpret_cast<const SsspBatch *>(base + O.batches);
     G.batches_alt = reinterpret_cast<const SsspBatch *>(base + O.batches_alt);
+    if (pl.bsssp) {
+      G.bjobs = reinterpret_cast<const fapk::BgJob *>(base + O.bjobs);
+      G.bsrc = reinterpret_cast<const int32_t *>(base + O.bsrc);
+    }
     G.pdesc = reinterpret_cast<const PartDesc *>(base + O.pdesc);
     G.row_begin = reinterpret_cast<const int64_t *>(base + O.row_begin);
     G.dec_begin = reinterpret_cast<const int64_t *>(base + O.dec_begin);
@@ -683,6 +855,30 @@ struct Issuer {
     sa.delta = sssp_delta_of(e);
     sa.stats = e->d_stats;
     if (g == 0) FAP_CUDA(cudaMemsetAsync(e->d_stats, 0, 8 * sizeof(unsigned long long), st));
+    if (pl.bsssp) {
+      // Through the boundary graph: local rows of every part (once per
+      // solve), boundary-graph distances of this group's sources, their
+      // rows into the per-batch tables, then the search's output pass.
+      const bool wide = e->f32();
+      fapk::BgArgs ba = e->bg_args;
+      ba.bjobs = G.bjobs;
+      ba.bsrc = G.bsrc;
+      ba.status = e->d_status;
+      ba.stats = e->d_stats;
+      if (g == 0) FAP_CUDA(fapk::launch_bg_local(wide, ba, e->bg_nljobs, e->bg_max_sub, st));
+      FAP_CUDA(fapk::launch_bg_boundary(wide, ba, G.nbjobs, st));
+      fapk::BgRowArgs ra{};
+      ra.batches = G.batches;
+      ra.nbatches = G.nbatches;
+      ra.st2ed = e->d_st2ed;
+      ra.scratch = e->sssp_scratch.p;
+      ra.slot_bytes = fapk::sssp_slot_bytes(e->n, sa.acc64 && sa.lanes == 32);
+      ra.scale = wide ? std::ldexp(1.0, -e->fix_shift) : 1.0;
+      FAP_CUDA(fapk::launch_bg_rows(wide, sa.lanes, ba, ra, st));
+      sa.slots = G.nbatches;
+      FAP_CUDA(fapk::launch_sssp_output(e->f32(), sa, st));
+      return FAP_OK;
+    }
     FAP_CUDA(fapk::launch_sssp(e->f32(), sa, st));
     return FAP_OK;
   }
@@ -781,7 +977,31 @@ struct Issuer {
     if (last) FAP_CUDA(rec(5));
     return FAP_OK;
   }
-  // Plain plans interleave per part (SSSP, rest); batched plans have one group.
+  // Host results: group g's finished rows go to the host rows on the copy
+  // stream, behind the group's last launch; the issuing stream goes on with
+  // the next group.  join() makes the issuing stream wait for every copy.
+  int copy_out(size_t g) {
+    if (!pl.hdist) return FAP_OK;
+    const Plan::Group &G = pl.groups[g];
+    FAP_CUDA(cudaEventRecord(e->ev_copy[0], st));
+    FAP_CUDA(cudaStreamWaitEvent(e->copy, e->ev_copy[0], 0));
+    const size_t off = (size_t)G.out_lo * 4, bytes = (size_t)G.out_elems * 4;
+    FAP_CUDA(cudaMemcpyAsync(static_cast<char *>(pl.hdist) + off, static_cast<const char *>(pl.dist) + off,
+                             bytes, cudaMemcpyDeviceToHost, e->copy));
+    if (pl.hpred)
+      FAP_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(pl.hpred) + off,
+                               reinterpret_cast<const char *>(pl.pred) + off, bytes,
+                               cudaMemcpyDeviceToHost, e->copy));
+    return FAP_OK;
+  }
+  int join() {
+    if (!pl.hdist) return FAP_OK;
+    FAP_CUDA(cudaEventRecord(e->ev_copy[1], e->copy));
+    FAP_CUDA(cudaStreamWaitEvent(st, e->ev_copy[1], 0));
+    return FAP_OK;
+  }
+  // Plain plans interleave per part (SSSP, rest); batched plans have one
+  // group, or a few when the results go to host rows.
   int all() {
     int rc;
     const int c0 = fapk::launch_count();
@@ -790,7 +1010,9 @@ struct Issuer {
       if ((rc = sssp(g)) != FAP_OK) return rc;
       if (g + 1 == pl.groups.size()) FAP_CUDA(rec(1));
       if ((rc = rest(g, g + 1 == pl.groups.size())) != FAP_OK) return rc;
+      if ((rc = copy_out(g)) != FAP_OK) return rc;
     }
+    if ((rc = join()) != FAP_OK) return rc;
     pl.launches = fapk::launch_count() - c0;
     return FAP_OK;
   }
@@ -951,9 +1173,11 @@ int first_run(fap_engine *e, Plan &pl, cudaStream_t st) {
       (unsigned long long)maxd + (unsigned long long)std::max(pl.max_sub - 1, 0) * e->wmax;
   const bool k_ok = pl.pred == nullptr || pl.max_mp_k <= fapk::max_packed_k();
   pl.pack = (bound < fapk::pack_limit() && k_ok) ? 1 : 0;
-  for (size_t g = 0; g < pl.groups.size(); g++)
+  for (size_t g = 0; g < pl.groups.size(); g++) {
     if ((rc = is.rest(g, g + 1 == pl.groups.size())) != FAP_OK) return rc;
-  return FAP_OK;
+    if ((rc = is.copy_out(g)) != FAP_OK) return rc;
+  }
+  return is.join();
 }
 
 int check_status(fap_engine *e) {
@@ -976,16 +1200,19 @@ std::vector<const void *> buffer_signature(const fap_engine *e) {
           reinterpret_cast<const void *>((intptr_t)e->sssp_fp64),
           reinterpret_cast<const void *>((intptr_t)e->sssp_lanes),
           reinterpret_cast<const void *>((intptr_t)e->tile_cols),
+          reinterpret_cast<const void *>((intptr_t)e->sssp_method),
+          e->bg_tab.p,
           reinterpret_cast<const void *>(dbits)};
 }
 
 Plan *find_plan(fap_engine *e, int mode, void *dist, int32_t *pred,
                 const std::vector<int32_t> &parts, const std::vector<int64_t> &offs, void *bdist,
-                int32_t *bpred) {
+                int32_t *bpred, void *hdist, int32_t *hpred) {
   const std::vector<const void *> sig = buffer_signature(e);
   for (auto &p : e->plans)
     if (p->mode == mode && p->dist == dist && p->pred == pred && p->parts == parts &&
-        p->row_offs == offs && p->bdist == bdist && p->bpred == bpred && p->sig == sig)
+        p->row_offs == offs && p->bdist == bdist && p->bpred == bpred && p->hdist == hdist &&
+        p->hpred == hpred && p->sig == sig)
       return p.get();
   return nullptr;
 }
@@ -995,7 +1222,8 @@ Plan *find_plan(fap_engine *e, int mode, void *dist, int32_t *pred,
 // at element boffs[i]) and dist/pred receive only the inner rows.
 int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vector<int32_t> &parts,
               const std::vector<int64_t> &offs, cudaStream_t st, void *bdist = nullptr,
-              int32_t *bpred = nullptr, const std::vector<int64_t> &boffs = {}) {
+              int32_t *bpred = nullptr, const std::vector<int64_t> &boffs = {}, void *hdist = nullptr,
+              int32_t *hpred = nullptr) {
   int rc;
   // work buffers
   size_t fw_elems = 0;
@@ -1011,10 +1239,23 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
               : (e->sssp_lanes_tuned && !acc64) ? e->sssp_lanes_tuned
                                                 : fapk::sssp_lanes_for(batches8, batches32, e->sm_count, acc64);
   if (acc64 && lanes == 8) lanes = 16;  // the FP64 search has no 8-source form
+  // Boundary SSSP through the boundary graph where its arithmetic is exact
+  // (int32 graphs; FP32 graphs with the FP64 option and a fixed-point
+  // shift), its shared-memory tables fit and every batch of a group gets a
+  // table slot of its own; otherwise the whole-graph search.
+  bool bs = false;
+  if (e->sssp_method == 0 && (!e->f32() || acc64)) {
+    if ((rc = prepare_bgraph(e)) != FAP_OK) return rc;
+    if (e->bg_ok) {
+      int64_t nb = 0;
+      for (int p : parts) nb += (e->bdy_num[p] + lanes - 1) / lanes;
+      bs = nb <= max_sssp_slots(e, acc64 && lanes == 32);
+    }
+  }
   // The SSSP autotuner also tries a second batch width (8 -> 16, 16 -> 32,
   // 32 -> 16; not for the FP64 search, whose 32-source slots have another
   // layout); scratch for the larger batch count of the two.
-  const bool tune_lanes = e->autotune && e->sssp_delta <= 0 && e->sssp_lanes == 0 && !acc64;
+  const bool tune_lanes = e->autotune && e->sssp_delta <= 0 && e->sssp_lanes == 0 && !acc64 && !bs;
   const int alt_lanes = lanes == 16 ? 32 : 16;
   const bool wide = acc64 && lanes == 32;
   const int count_lanes = tune_lanes ? std::min(lanes, alt_lanes) : lanes;
@@ -1025,7 +1266,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e, wide));
   if ((rc = ensure_sssp_scratch(e, slots, wide)) != FAP_OK) return rc;
 
-  Plan *pl = find_plan(e, mode, dist, pred, parts, offs, bdist, bpred);
+  Plan *pl = find_plan(e, mode, dist, pred, parts, offs, bdist, bpred, hdist, hpred);
   if (!pl) {
     if (e->plans.size() >= 8) e->plans.erase(e->plans.begin());
     auto np = std::make_unique<Plan>();
@@ -1037,15 +1278,19 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     np->bdist = bdist;
     np->bpred = bpred;
     np->brow_offs = boffs;
+    np->hdist = hdist;
+    np->hpred = hpred;
     np->sig = buffer_signature(e);
     np->sssp_lanes = lanes;
     np->sssp_lanes_alt = tune_lanes ? alt_lanes : 0;
+    np->bsssp = bs ? 1 : 0;
     if ((rc = build_plan(e, *np)) != FAP_OK) return rc;
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
   }
   if (pl->pack < 0) {
-    if (e->autotune && e->sssp_delta <= 0 && (rc = autotune_sssp(e, *pl, st)) != FAP_OK) return rc;
+    if (e->autotune && e->sssp_delta <= 0 && !pl->bsssp && (rc = autotune_sssp(e, *pl, st)) != FAP_OK)
+      return rc;
     if ((rc = first_run(e, *pl, st)) != FAP_OK) return rc;
     if (e->autotune && e->tile_cols == 0) return autotune_tiles(e, *pl, st);
     return FAP_OK;
@@ -1143,7 +1388,31 @@ int init_device(fap_engine *e, int device) {
   FAP_CUDA(cudaMemset(e->d_stats, 0, 8 * sizeof(unsigned long long)));
   FAP_CUDA(fapk::init_minplus_kernels());
   FAP_CUDA(fapk::init_sssp_kernels());
+  FAP_CUDA(fapk::init_bg_kernels());
   return FAP_OK;
+}
+
+// Shift s such that every weight is an integer multiple of 2^-s and every
+// simple path stays below 2^52 such units ((n - 1) * max weight * 2^s <
+// 2^52): then path lengths are exact in 64-bit fixed point and in FP64
+// (sums of multiples of 2^-s below 2^(52 - s)).  -1 when there is none.
+int fixed_point_shift(const float *w, int64_t m, int32_t n, float wmax) {
+  int s = 0;
+  for (int64_t j = 0; j < m; j++) {
+    if (!(w[j] > 0.0f)) continue;
+    int ex = 0;
+    const float f = std::frexp(w[j], &ex);  // w = f * 2^ex, f in [0.5, 1)
+    uint32_t mant = (uint32_t)std::ldexp(f, 24);  // exact: at most 24 significant bits
+    int low = ex - 24;
+    while (!(mant & 1u)) {
+      mant >>= 1;
+      low++;
+    }
+    s = std::max(s, -low);  // w = mant * 2^low
+  }
+  if (s > 200) return -1;
+  const double bound = std::ldexp((double)wmax * (double)std::max<int32_t>(n - 1, 1), s);
+  return bound < std::ldexp(1.0, 52) ? s : -1;
 }
 
 template <typename T>
@@ -1338,6 +1607,7 @@ int fap_create(int32_t n, int64_t m, const int32_t *row_offset, const int32_t *c
     return rc;
   }
   E->wmax = dtype == FAP_DTYPE_I32 ? (uint32_t)wmax : 0u;
+  if (dtype == FAP_DTYPE_F32) E->fix_shift = fixed_point_shift(weight, m, n, wmax);
   {
     double sum = 0;
     for (int64_t j = 0; j < m; j++) sum += weight[j];
@@ -1363,6 +1633,9 @@ int fap_destroy(fap_engine *e) {
     e->bnd_d.release();
     e->bnd_p.release();
     e->small.release();
+    e->bg_tab.release();
+    e->bg_L.release();
+    e->bg_DS.release();
     void *ptrs[] = {e->d_ro, e->d_col, e->d_iro, e->d_icol, e->d_gid, e->d_st2ed, e->d_ed2st,
                     e->d_w, e->d_iw, e->d_status, e->d_stats};
     for (void *p : ptrs)
@@ -1449,7 +1722,23 @@ static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_
   // the FW), and the decode then writes their own-part columns in place.
   void *hd = dev_d ? nullptr : mapped_host_ptr(dist);
   void *hp = (pred && !dev_p) ? mapped_host_ptr(pred) : nullptr;
-  if (!dev_d && hd && (pred == nullptr || hp)) {
+  bool direct = !dev_d && hd && (pred == nullptr || hp);
+  if (direct && e->host_results == 0) {
+    // Staged instead when the device has room for a copy of the results:
+    // kernel stores into host memory reached only ~45 GB/s on the
+    // 114,599-vertex graph (rows 458 KB apart, every tile touching 128 of
+    // them), while the copy engines move the finished rows at the host
+    // link's rate.
+    const size_t need = bytes * (pred && !dev_p ? 2 : 1);
+    const size_t have = (e->res_d.bytes >= bytes ? bytes : 0) + (pred && e->res_p.bytes >= bytes ? bytes : 0);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      (void)cudaGetLastError();
+      free_b = 0;
+    }
+    if (need <= have || need - have + ((size_t)2 << 30) <= free_b) direct = false;
+  }
+  if (direct) {
     std::vector<int64_t> boffs;
     int64_t bacc = 0;
     for (int32_t p : parts) {
@@ -1474,9 +1763,17 @@ static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_
       if ((rc = e->res_p.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
       dp = static_cast<int32_t *>(e->res_p.p);
     }
-    if ((rc = run_parts(e, mode, dd, dp, parts, offs, st)) != FAP_OK) return rc;
-    if (!dev_d) FAP_CUDA(cudaMemcpyAsync(dist, dd, bytes, cudaMemcpyDeviceToHost, st));
-    if (pred && !dev_p) FAP_CUDA(cudaMemcpyAsync(pred, dp, bytes, cudaMemcpyDeviceToHost, st));
+    // Page-locked host rows (both, when there are predecessors): the plan
+    // copies each group's rows as it finishes; otherwise one copy at the end.
+    const bool plan_copies = !dev_d && hd && (pred == nullptr || (!dev_p && hp));
+    if (plan_copies) {
+      if ((rc = run_parts(e, mode, dd, dp, parts, offs, st, nullptr, nullptr, {}, dist, pred)) != FAP_OK)
+        return rc;
+    } else {
+      if ((rc = run_parts(e, mode, dd, dp, parts, offs, st)) != FAP_OK) return rc;
+      if (!dev_d) FAP_CUDA(cudaMemcpyAsync(dist, dd, bytes, cudaMemcpyDeviceToHost, st));
+      if (pred && !dev_p) FAP_CUDA(cudaMemcpyAsync(pred, dp, bytes, cudaMemcpyDeviceToHost, st));
+    }
   }
   FAP_CUDA(cudaStreamSynchronize(st));
   if (mode == FAP_MODE_BATCHED && st != e->stream) FAP_CUDA(cudaStreamSynchronize(e->stream));
@@ -1525,6 +1822,7 @@ static int apply_partition(fap_engine *e, const int32_t *graph_id) {
   // stream an earlier solve ran on): wait for the whole device first
   FAP_CUDA(cudaDeviceSynchronize());
   e->plans.clear();
+  e->bg_ready = false;  // the boundary graph is rebuilt for the new parts on first use
   if (n > 0) {
     const size_t bytes = (size_t)n * sizeof(int32_t);
     FAP_CUDA(cudaMemcpy(e->d_gid, gid.data(), bytes, cudaMemcpyHostToDevice));
@@ -1883,6 +2181,14 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
         return set_error(FAP_ERR_INVALID, "tile columns must be 0, 64 or 128");
       e->tile_cols = (int)value;
       return FAP_OK;
+    case FAP_OPT_SSSP_METHOD:
+      if (value != 0.0 && value != 1.0) return set_error(FAP_ERR_INVALID, "SSSP method must be 0 or 1");
+      e->sssp_method = (int)value;
+      return FAP_OK;
+    case FAP_OPT_HOST_RESULTS:
+      if (value != 0.0 && value != 1.0) return set_error(FAP_ERR_INVALID, "host results must be 0 or 1");
+      e->host_results = (int)value;
+      return FAP_OK;
     default:
       return set_error(FAP_ERR_INVALID, "unknown option");
   }
@@ -1896,6 +2202,8 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_AUTOTUNE: *value = e->autotune; return FAP_OK;
     case FAP_OPT_SSSP_LANES: *value = e->sssp_lanes ? e->sssp_lanes : e->sssp_lanes_tuned; return FAP_OK;
     case FAP_OPT_TILE_COLS: *value = e->tile_cols; return FAP_OK;
+    case FAP_OPT_SSSP_METHOD: *value = e->sssp_method; return FAP_OK;
+    case FAP_OPT_HOST_RESULTS: *value = e->host_results; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");
   }
 }

@@ -97,6 +97,58 @@ int sssp_lanes_for(int64_t batches8, int64_t batches32, int sm_count, bool acc64
 int sssp_threads();
 cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st);
 
+// Output pass of the whole-graph search alone, over per-batch vertex-major
+// tables that something else filled (batch b's table in scratch slot b,
+// a.slots >= a.nbatches): predecessors, rounding, row stores.  acc64: FP32
+// graphs with FP64 tables (8-byte entries, 16 or 32 lanes).
+cudaError_t launch_sssp_output(bool f32, const SsspArgs &a, cudaStream_t st);
+
+// bgraph.cu -- boundary SSSP through the boundary graph (exact arithmetic:
+// uint32 for int32 graphs, 64-bit fixed point for FP32 graphs ("wide")).
+struct BgPart {
+  int32_t start;  // first sorted position of the part
+  int32_t sub, bdy;
+  int32_t boff;   // boundary index of its first boundary vertex
+  int64_t loff;   // element offset of its local rows (bdy x sub) in the L arena
+};
+struct BgJob {    // step 1: (part, first local source, count); step 2: (batch, first lane, count)
+  int32_t unit, first, count;
+};
+struct BgArgs {
+  int32_t nparts;
+  const BgPart *parts;
+  int32_t B;                   // boundary vertices = nodes of the boundary graph
+  const int32_t *bpart;        // [B] part (index into parts) of each boundary node
+  const int32_t *lro;          // [n + 1] by sorted position: local out-edges of the vertex
+  const int32_t *lcol;         // local index (within its part) of the edge's target
+  const void *lw;              // edge weights (uint32 or 64-bit fixed point)
+  const int32_t *cro;          // [B + 1] cut out-edges of each boundary node
+  const int32_t *ccol;         // boundary index of the target
+  const void *cw;              // weights
+  const BgJob *ljobs;          // step-1 jobs
+  const BgJob *bjobs;          // step-2 jobs
+  const int32_t *bsrc;         // [batches][32] boundary index of each SSSP source (-1: none)
+  void *L;                     // local rows of every part
+  void *DS;                    // [B][B] boundary-graph distances, row = source boundary index
+  unsigned *status;
+  unsigned long long *stats;   // may be null: [rounds, -, nodes visited, -, -]
+};
+struct BgRowArgs {
+  const SsspBatch *batches;
+  int32_t nbatches;
+  const int32_t *st2ed;
+  void *scratch;               // batch b's table at scratch + b * slot_bytes
+  size_t slot_bytes;
+  double scale;                // 2^-shift (fixed point -> FP64)
+};
+constexpr size_t kBgSmemMax = 226 * 1024;  // dynamic; the 227 KB per-block limit also holds the static part
+size_t bg_smem_bytes(bool wide, int nodes);  // shared memory of steps 1 and 2 over `nodes` nodes
+int bg_lanes();                              // sources per CTA in steps 1 and 2
+cudaError_t init_bg_kernels();
+cudaError_t launch_bg_local(bool wide, const BgArgs &a, int njobs, int max_sub, cudaStream_t st);
+cudaError_t launch_bg_boundary(bool wide, const BgArgs &a, int njobs, cudaStream_t st);
+cudaError_t launch_bg_rows(bool wide, int lanes, const BgArgs &a, const BgRowArgs &r, cudaStream_t st);
+
 // transform.cu
 struct PartDesc {
   int32_t sub, bdy, start;  // part size, boundary count, first sorted position

@@ -499,6 +499,26 @@ cudaError_t launch_one(const SsspArgs &a0, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+template <typename T, bool PRED, int LANES, bool ACC64>
+cudaError_t launch_output(const SsspArgs &a, cudaStream_t st) {
+  const dim3 grid((unsigned)((a.n + kOutThreads - 1) / kOutThreads), (unsigned)a.nbatches);
+  ++launch_count();
+  sssp_output_kernel<T, PRED, LANES, ACC64><<<grid, kOutThreads, out_kernel_smem<LANES>(), st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, bool PRED>
+cudaError_t launch_output_t(const SsspArgs &a, cudaStream_t st) {
+  if (a.acc64) {
+    if constexpr (std::is_same<T, float>::value)
+      return a.lanes == 16 ? launch_output<float, PRED, 16, true>(a, st) : launch_output<float, PRED, 32, true>(a, st);
+    return cudaErrorInvalidValue;
+  }
+  if (a.lanes == 8) return launch_output<T, PRED, 8, false>(a, st);
+  if (a.lanes == 16) return launch_output<T, PRED, 16, false>(a, st);
+  return launch_output<T, PRED, 32, false>(a, st);
+}
+
 template <typename T, bool PRED>
 cudaError_t launch_t(const SsspArgs &a, cudaStream_t st) {
   if (a.acc64) {
@@ -559,6 +579,16 @@ cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st) {
   const bool pred = a.pred != nullptr;
   if (f32) return pred ? launch_t<float, true>(a, st) : launch_t<float, false>(a, st);
   return pred ? launch_t<uint32_t, true>(a, st) : launch_t<uint32_t, false>(a, st);
+}
+
+cudaError_t launch_sssp_output(bool f32, const SsspArgs &a, cudaStream_t st) {
+  if (a.nbatches <= 0) return cudaSuccess;
+  if (a.lanes != 8 && a.lanes != 16 && a.lanes != 32) return cudaErrorInvalidValue;
+  if (a.acc64 && (!f32 || a.lanes == 8)) return cudaErrorInvalidValue;
+  if (a.slots < a.nbatches) return cudaErrorInvalidValue;
+  const bool pred = a.pred != nullptr;
+  if (f32) return pred ? launch_output_t<float, true>(a, st) : launch_output_t<float, false>(a, st);
+  return pred ? launch_output_t<uint32_t, true>(a, st) : launch_output_t<uint32_t, false>(a, st);
 }
 
 int sssp_lanes_for(int64_t batches8, int64_t batches32, int sm_count, bool acc64) {

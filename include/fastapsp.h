@@ -170,11 +170,12 @@ int fap_set_partition(fap_engine *e, const int32_t *graph_id);
 int fap_precondition(fap_engine *e);
 
 /* Engine options (no reference counterpart).
- *   FAP_OPT_SSSP_FP64  (FP32 engines) 1 = run the boundary SSSP in FP64 and
- *                      round once, which keeps FP32 results within an ulp or
- *                      two of FP64 shortest distances on long paths; 0
- *                      (default) = FP32 arithmetic, bit-identical to the
- *                      reference's FP32 Dijkstra.
+ *   FAP_OPT_SSSP_FP64  (FP32 engines) 1 = run the boundary SSSP in exact or
+ *                      FP64 arithmetic and round once to FP32, which keeps
+ *                      results within an ulp or two of FP64 shortest
+ *                      distances on long paths; 0 (default) = FP32
+ *                      arithmetic, bit-identical to the reference's FP32
+ *                      Dijkstra.
  *   FAP_OPT_SSSP_DELTA near-far threshold step of the SSSP in distance units
  *                      (0 = automatic).  Changes speed only, never results.
  *   FAP_OPT_AUTOTUNE   1 (default) = while the step is automatic, the first
@@ -196,12 +197,38 @@ int fap_precondition(fap_engine *e);
  *                      run times both widths and keeps the faster (not for
  *                      results in mapped host memory); otherwise 64 for
  *                      K <= 48 and 128 above.  Changes speed only.
+ *   FAP_OPT_SSSP_METHOD how the boundary SSSP rows of a solve are made:
+ *                      0 (default) = through the boundary graph where its
+ *                      arithmetic is exact -- int32 engines, and FP32
+ *                      engines with FAP_OPT_SSSP_FP64 whose weights are
+ *                      multiples of one power of two 2^-s with
+ *                      (n-1) * max weight < 2^(52-s) (64-bit fixed point) --
+ *                      and its tables fit in shared memory (up to about
+ *                      3,200 boundary vertices for FP32, 5,800 for int32):
+ *                      local rows of every part from its boundary vertices,
+ *                      shortest paths between all boundary vertices over
+ *                      the cut edges and those rows, then a min-plus per
+ *                      part; otherwise the whole-graph search.  1 = always
+ *                      the whole-graph search.  Both give the same
+ *                      distances (int32: identical; FP32: the exactly
+ *                      rounded distance, which equals the FP64 search's
+ *                      whenever its sums are exact) and the same
+ *                      predecessor rule.
+ *   FAP_OPT_HOST_RESULTS results in page-locked host memory: 0 (default) =
+ *                      solved into a device copy that the copy engines then
+ *                      move to the host rows, when the device has room for
+ *                      it; 1 = the kernels store the inner rows straight
+ *                      into the host rows (no device copy of the n x n
+ *                      result; also the choice of 0 without room).  Same
+ *                      rows either way.
  * Setting an option takes effect from the next solve. */
 #define FAP_OPT_SSSP_FP64 1
 #define FAP_OPT_SSSP_DELTA 2
 #define FAP_OPT_AUTOTUNE 3
 #define FAP_OPT_SSSP_LANES 4
 #define FAP_OPT_TILE_COLS 5
+#define FAP_OPT_SSSP_METHOD 6
+#define FAP_OPT_HOST_RESULTS 7
 int fap_set_option(fap_engine *e, int32_t option, double value);
 int fap_get_option(const fap_engine *e, int32_t option, double *value);
 
@@ -310,8 +337,11 @@ int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m,
 /* ---- diagnostics -------------------------------------------------------- */
 
 /* Counters of the SSSP phase of the last solve (no reference counterpart):
- * [near-frontier steps, far-list splits, frontier vertices relaxed, far
- * entries scanned, batches], summed over all batches. */
+ * whole-graph search: [near-frontier steps, far-list splits, frontier
+ * vertices relaxed, far entries scanned, batches], summed over all batches;
+ * through the boundary graph (FAP_OPT_SSSP_METHOD): [Bellman-Ford rounds of
+ * the local and boundary-graph steps, 0, nodes they visited, 0, 0],
+ * summed over their CTAs. */
 int fap_sssp_stats(fap_engine *e, uint64_t *out5);
 
 /* Add-min operations per second that the GPU issues from registers alone

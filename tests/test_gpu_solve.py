@@ -115,16 +115,19 @@ def test_fapgraph_mirror_solve_and_split(gpu):
 @pytest.mark.parametrize("name", INT_CASES[:4] + F32_CASES[:1])
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("with_pred", [True, False])
-def test_solve_into_page_locked_host_rows(gpu, name, mode, with_pred):
-    """Page-locked host results take the direct path (inner rows written by
-    the kernels into host memory, boundary rows copied out): same rows as a
-    device-resident solve, on two calls in a row."""
+@pytest.mark.parametrize("direct", [0, 1])
+def test_solve_into_page_locked_host_rows(gpu, name, mode, with_pred, direct):
+    """Page-locked host results, staged (a device copy moved by the copy
+    engines) or direct (inner rows written by the kernels into host memory,
+    boundary rows copied out): same rows as a device-resident solve, on two
+    calls in a row."""
     z, g = load_golden(name)
     n = g.n
     dtype = gpu.DTYPE_F32 if name.endswith("f32") else gpu.DTYPE_I32
     tdt = torch.float32 if dtype == gpu.DTYPE_F32 else torch.int32
     with gpu.Engine(n, g.row_offset, g.col_val, g.weight, int(z["K"]), graph_id=z["graph_id"],
                     dtype=dtype) as eng:
+        eng.set_option(gpu._lib.OPT_HOST_RESULTS, direct)
         dd = torch.empty((n, n), dtype=tdt, device="cuda")
         pd = torch.empty((n, n), dtype=torch.int32, device="cuda") if with_pred else None
         eng.solve(dd, pd, mode)
@@ -182,8 +185,9 @@ def test_autotuners_keep_results(gpu):
     """Tuned, 64-column and 128-column min-plus tiles give the same rows, in
     both forms, on graphs whose parts fall in both K classes of the strip form
     (the tuner's trial launches rewrite the rows of the first run), and the
-    same as an engine with the autotuners off; the SSSP tuner reports the
-    batch width it chose."""
+    same as an engine with the autotuners off; the SSSP tuner of the
+    whole-graph search (which the boundary-graph method does not need)
+    reports the batch width it chose."""
     from fastapsp_gb300 import graphs
 
     for g, K in ((graphs.geometric_knn(n=6144, k=3, seed=11), 6), (graphs.grid_graph(64, 64, seed=3), 4)):
@@ -192,6 +196,7 @@ def test_autotuners_keep_results(gpu):
         for tune in (1, 0):
             with gpu.Engine(n, g.row_offset, g.col_val, g.weight, K, dtype=gpu.DTYPE_I32) as eng:
                 eng.set_option(gpu._lib.OPT_AUTOTUNE, tune)
+                eng.set_option(gpu._lib.OPT_SSSP_METHOD, 1)
                 runs = ((0, 1), (64, 1), (128, 1), (0, 0)) if tune else ((0, 1),)
                 for cols, mode in runs:
                     eng.set_option(gpu._lib.OPT_TILE_COLS, cols)
