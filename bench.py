@@ -200,7 +200,7 @@ def pinned_host(shape, dtype):
     """Page-locked host rows of exactly `shape` from cudaHostAlloc (the CUDA
     runtime torch loaded; the caching pinned allocator would round each
     buffer up to a power of two, and registered pageable memory measured
-    slower for kernel stores); returns (numpy array, free function)."""
+    slower for kernel stores); returns (numpy array, free function, source)."""
     import ctypes
 
     import torch
@@ -212,11 +212,11 @@ def pinned_host(shape, dtype):
         if rt.cudaHostAlloc(ctypes.byref(p), ctypes.c_size_t(nbytes), 0) == 0 and p.value:
             buf = (ctypes.c_char * nbytes).from_address(p.value)
             arr = np.frombuffer(buf, dtype=dtype).reshape(shape)
-            return arr, lambda: rt.cudaFreeHost(p)
+            return arr, lambda: rt.cudaFreeHost(p), "cudaHostAlloc"
     except OSError:
         pass
     t = torch.empty(shape, dtype=torch.from_numpy(np.empty(0, dtype)).dtype, pin_memory=True)
-    return t.numpy(), lambda: None
+    return t.numpy(), lambda: None, "torch pinned allocator"
 
 
 def run_solve(args, name, rank, world, local_rank):
@@ -332,10 +332,11 @@ def run_solve(args, name, rank, world, local_rank):
     w_h = torch.from_numpy(g.weight).pin_memory()
     gid_h = torch.from_numpy(gid).pin_memory()
     e2e_ms, e2e_parts = [], []
+    host_alloc = None
     if args.e2e_steps > 0:
         npdt = np.float32 if f32 else np.int32
-        dist_h, free_d = pinned_host((n, n), npdt)
-        pred_h, free_p = pinned_host((n, n), np.int32)
+        dist_h, free_d, host_alloc = pinned_host((n, n), npdt)
+        pred_h, free_p, _ = pinned_host((n, n), np.int32)
         for i in range(1 + args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -373,6 +374,7 @@ def run_solve(args, name, rank, world, local_rank):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms_step,
                 "create_solve_destroy_ms": [statistics.mean(x) for x in zip(*e2e_parts)] if e2e_parts else None,
+                "solve_ms_each": [round(x[1], 1) for x in e2e_parts], "host_rows": host_alloc,
                 "what": "fap_create (CSR from page-locked host arrays) + fap_solve into page-locked host rows "
                         "(n x n distances + predecessors) + fap_destroy, SSSP settings as tuned on this graph"},
         "gpu_launches": launches_per_step * args.steps,

@@ -15,6 +15,11 @@
 //   mode 4: int32, two add-mins per step: two adds and one 3-input min (DPX)
 //   mode 5: FP32, two add-mins per step: one paired add (add.f32x2) and one
 //           3-input min
+//   modes 6-9: FP32 add-min keeping the step index of the last strict
+//           improvement (the FP32 strip kernel's step), written four ways:
+//           6 __vibmin_s32 (values are non-negative floats), 7 one unsigned
+//           compare and two predicated moves, 8 a float compare, fminf and a
+//           select, 9 __vibmin_u32 (the form the FP32 kernels use)
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -43,8 +48,8 @@ __device__ __forceinline__ float2 add_f32x2(float2 a, float2 b) {
 
 template <int MODE>
 __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int iters, unsigned seed) {
-  constexpr bool F = (MODE == 1 || MODE == 3 || MODE == 5);
-  constexpr bool ARG = (MODE == 2 || MODE == 3);
+  constexpr bool F = (MODE == 1 || MODE == 3 || MODE == 5 || MODE >= 6);
+  constexpr bool ARG = (MODE == 2 || MODE == 3 || MODE >= 6);
   using T = typename std::conditional<F, float, unsigned>::type;
   T a[4][4], b[4][16], acc[4][16];
   int arg[4][16];
@@ -88,8 +93,34 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
 #pragma unroll
           for (int c = 0; c < 16; c++) {
             const T x = a[s][r], y = b[s][c];
+            const int idx = it * 4 + s + 1;
             if (MODE == 0) {
               acc[r][c] = (T)__viaddmin_u32((unsigned)x, (unsigned)y, (unsigned)acc[r][c]);
+            } else if (MODE >= 6) {
+              const float fv = (float)x + (float)y;
+              const unsigned v = __float_as_uint(fv);
+              unsigned ac = __float_as_uint((float)acc[r][c]);
+              int ag = arg[r][c];
+              if (MODE == 6) {
+                bool keep;
+                ac = (unsigned)__vibmin_s32((int)ac, (int)v, &keep);
+                ag = keep ? ag : idx;
+              } else if (MODE == 7) {
+                asm("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %2, %0;\n\t@p mov.b32 %0, %2;\n\t@p mov.b32 %1, %3;\n\t}"
+                    : "+r"(ac), "+r"(ag)
+                    : "r"(v), "r"(idx));
+              } else if (MODE == 8) {
+                const float fa = __uint_as_float(ac);
+                const bool lt = fv < fa;
+                ac = __float_as_uint(fminf(fa, fv));
+                ag = lt ? idx : ag;
+              } else {
+                bool keep;
+                ac = __vibmin_u32(ac, v, &keep);
+                ag = keep ? ag : idx;
+              }
+              acc[r][c] = (T)__uint_as_float(ac);
+              arg[r][c] = ag;
             } else if (MODE == 1) {
               acc[r][c] = fminf((float)x + (float)y, (float)acc[r][c]);
             } else {
@@ -144,7 +175,11 @@ cudaError_t measure_addmin_peak(int mode, int sm_count, double *ops_per_s) {
       case 2: e = run_mode<2>(buf, blocks, iters, 0); break;
       case 3: e = run_mode<3>(buf, blocks, iters, 0); break;
       case 4: e = run_mode<4>(buf, blocks, iters, 0); break;
-      default: e = run_mode<5>(buf, blocks, iters, 0); break;
+      case 5: e = run_mode<5>(buf, blocks, iters, 0); break;
+      case 6: e = run_mode<6>(buf, blocks, iters, 0); break;
+      case 7: e = run_mode<7>(buf, blocks, iters, 0); break;
+      case 8: e = run_mode<8>(buf, blocks, iters, 0); break;
+      default: e = run_mode<9>(buf, blocks, iters, 0); break;
     }
     cudaEventRecord(b, 0);
     if (e != cudaSuccess) break;

@@ -350,7 +350,9 @@ int fap_sssp_stats(fap_engine *e, uint64_t *out5);
  * fminf(a + b, c); 2: int32 add-min keeping the argmin; 3: FP32 add-min
  * keeping the argmin; 4: int32, two add-mins as two adds and one 3-input
  * min; 5: FP32, two add-mins as one paired add (add.f32x2) and one 3-input
- * min. */
+ * min; 6-9: FP32 add-min keeping the step of the last strict improvement,
+ * as __vibmin_s32 (6), a compare and two predicated moves (7), a float
+ * compare, fminf and a select (8), __vibmin_u32 (9). */
 int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s);
 
 #ifdef __cplusplus
