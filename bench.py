@@ -302,10 +302,13 @@ def run_solve(args, name, rank, world, local_rank):
     # add-min steps the strip kernels actually ran (they skip the k-steps whose
     # B row or A column is unreached over a tile): one more solve with counters
     eng.minplus_counters(reset=True)
+    eng.fw_counters(reset=True)
     step()
     torch.cuda.synchronize()
     mpc = eng.minplus_counters(reset=True)
+    fwc = eng.fw_counters(reset=True)
     executed = int(mpc["executed_addmins"])
+    fw_executed = int(fwc["strip_addmins"] + fwc["other_addmins"])
 
     # plain form (one launch sequence per part, the reference's loop) on the
     # same graph, for batched-vs-plain
@@ -404,11 +407,15 @@ def run_solve(args, name, rank, world, local_rank):
                 "peak_dpx_int32": peak_dpx / 1e9,
             },
         },
-        "roofline_fw": {"achieved": rate(addmin_fw, ph["floyd"]) / 1e9, "peak": peak_fw / 1e9,
-                        "unit": "Gaddmin/s", "frac": rate(addmin_fw, ph["floyd"]) / peak_fw,
-                        "algorithmic_addmins": addmin_fw,
-                        "note": "dense count (sum of ld^3 over the parts' padded matrices) against "
-                                + ("fap_addmin_peak mode 3 (FP32)" if f32 else "fap_addmin_peak mode 0 (DPX)")},
+        "roofline_fw": {"achieved": rate(fw_executed, ph["floyd"]) / 1e9, "peak": peak_fw / 1e9,
+                        "unit": "Gaddmin/s", "frac": rate(fw_executed, ph["floyd"]) / peak_fw,
+                        "executed_addmins": fw_executed, "executed_split": fwc,
+                        "dense_addmins": addmin_fw,
+                        "dense_equivalent_rate": rate(addmin_fw, ph["floyd"]) / 1e9,
+                        "note": "executed add-mins (fap_fw_counters: the remaining-tile strips' device counter "
+                                "plus the pivot or tile launches' block products) per FW phase time, against "
+                                + ("fap_addmin_peak mode 3 (FP32 add-min keeping the argmin)" if f32 else
+                                   "fap_addmin_peak mode 0 (int32 DPX add-min)")},
         "roofline_sssp": {"bound": "hbm", "achieved": rate(sssp_bytes, ph["sssp"]) / 1e9, "peak": hbm,
                           "unit": "GB/s", "frac": rate(sssp_bytes, ph["sssp"]) / 1e9 / hbm,
                           "algorithmic_bytes": sssp_bytes, "peak_source": peak_src},
@@ -636,6 +643,8 @@ def main():
                     help="host work of the cpu_baseline sample (whole parts until this is reached)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
+    ap.add_argument("--no-c3", dest="with_c3", action="store_false",
+                    help="leave out the dense batched FW of 512 instances from the solve line")
     ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c4",
                     help="c4 (default, the largest single-GPU workload) is the headline; c1/c2 print the same "
                          "line for their graphs, c3/c5 their own lines")
@@ -668,6 +677,12 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     res = run_solve(args, args.config, rank, world, local_rank)
+    if rank == 0 and args.with_c3:
+        # the dense batched FW (512 int32 instances, no step can be skipped),
+        # the FW kernels' own roofline beside the solve's
+        c3 = run_c3(argparse.Namespace(steps=3, warmup=2))
+        res["fw_dense_512"] = {k: c3[k] for k in ("value", "unit", "ms_per_step", "per_instance_ms",
+                                                   "batched_speedup", "frac_of_dpx_peak", "addmins")}
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = cpu_baseline(args.config, args.cpu_seconds, args.ref_rows)

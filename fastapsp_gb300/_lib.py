@@ -32,6 +32,7 @@ OPT_SSSP_LANES = 4
 OPT_TILE_COLS = 5
 OPT_SSSP_METHOD = 6
 OPT_HOST_RESULTS = 7
+OPT_INT32_FORM = 8
 INF_I32 = 1 << 30
 
 _i32 = C.c_int32
@@ -67,6 +68,7 @@ SIGNATURES = {
     "fap_last_times": (C.c_int, [_p, C.POINTER(C.c_double)]),
     "fap_last_launches": (C.c_int, [_p, C.POINTER(C.c_int64)]),
     "fap_minplus_counters": (C.c_int, [_p, C.POINTER(C.c_uint64), _i32]),
+    "fap_fw_counters": (C.c_int, [_p, C.POINTER(C.c_uint64), _i32]),
     "fap_minplus": (C.c_int, [_p, _i32, _i32, _i32, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i64,
                               _p, _i64, _p]),
     "fap_floyd_batched": (C.c_int, [_p, _i32, _i32, _p, _p, _p, _p, _p]),

@@ -166,6 +166,9 @@ struct Plan {
   int sssp_lanes = 32;  // sources per SSSP batch
   int sssp_lanes_alt = 0;  // the other width the autotuner tries (0: none)
   int bsssp = 0;        // boundary SSSP through the boundary graph (bgraph.cu) instead of the search
+  // FW add-mins of one run outside the remaining-tile strips: the pivot
+  // steps' 64^3 block products (packed form), or every block (tile form)
+  unsigned long long fw_pivot_work = 0, fw_tile_work = 0;
   int launches = 0;     // kernels one run of the plan launches
   // graph (batched mode)
   cudaGraphExec_t exec = nullptr;
@@ -210,6 +213,7 @@ struct fap_engine {
   int sssp_lanes_tuned = 0;  // the width the autotuner chose (0: none yet)
   int tile_cols = 0;       // min-plus strip tile columns: 64, 128, 0 = per class
   int host_results = 0;    // FAP_OPT_HOST_RESULTS: 0 staged when the device has room, 1 direct
+  int int32_form = 0;      // FAP_OPT_INT32_FORM: 0 packed keys when provably exact, 1 always wide
   int sssp_method = 0;     // FAP_OPT_SSSP_METHOD: 0 boundary graph where exact and it fits, 1 search
   int fix_shift = -1;      // FP32 graphs: every weight is a multiple of 2^-fix_shift and every path
                            // length below 2^52 of those units (-1: no such shift)
@@ -246,6 +250,7 @@ struct fap_engine {
   DevBuf small;                // tables of standalone calls
   std::vector<std::unique_ptr<Plan>> plans;
   double times[5] = {0, 0, 0, 0, 0};
+  unsigned long long fw_host_work = 0;  // fw_pivot_work / fw_tile_work of the runs since the last reset
   int64_t last_launches = 0;  // kernels the last solve launched
   std::mutex mu;
 
@@ -727,6 +732,11 @@ int build_plan(fap_engine *e, Plan &pl) {
         j.block = r;
         j.prev = r - 1;  // used by the packed form's pivot step (lookahead) only
         dj.push_back(j);
+        {  // 64^3 block products: pivot step (lookahead update, closure, panels); tile form (all blocks)
+          const unsigned long long blk = (unsigned long long)B * B * B;
+          pl.fw_pivot_work += blk * ((r > 0 ? 2ull * (nb - 2) + 1 : 0ull) + 1ull + 2ull * (nb - 1));
+          pl.fw_tile_work += blk * (unsigned long long)nb * nb;
+        }
         if (nb > 1) {
           MpSegment rp, cp, rest;
           int a1, a2, a3;
@@ -1172,7 +1182,7 @@ int first_run(fap_engine *e, Plan &pl, cudaStream_t st) {
   const unsigned long long bound =
       (unsigned long long)maxd + (unsigned long long)std::max(pl.max_sub - 1, 0) * e->wmax;
   const bool k_ok = pl.pred == nullptr || pl.max_mp_k <= fapk::max_packed_k();
-  pl.pack = (bound < fapk::pack_limit() && k_ok) ? 1 : 0;
+  pl.pack = (e->int32_form == 0 && bound < fapk::pack_limit() && k_ok) ? 1 : 0;
   for (size_t g = 0; g < pl.groups.size(); g++) {
     if ((rc = is.rest(g, g + 1 == pl.groups.size())) != FAP_OK) return rc;
     if ((rc = is.copy_out(g)) != FAP_OK) return rc;
@@ -1201,6 +1211,7 @@ std::vector<const void *> buffer_signature(const fap_engine *e) {
           reinterpret_cast<const void *>((intptr_t)e->sssp_lanes),
           reinterpret_cast<const void *>((intptr_t)e->tile_cols),
           reinterpret_cast<const void *>((intptr_t)e->sssp_method),
+          reinterpret_cast<const void *>((intptr_t)e->int32_form),
           e->bg_tab.p,
           reinterpret_cast<const void *>(dbits)};
 }
@@ -1292,6 +1303,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     if (e->autotune && e->sssp_delta <= 0 && !pl->bsssp && (rc = autotune_sssp(e, *pl, st)) != FAP_OK)
       return rc;
     if ((rc = first_run(e, *pl, st)) != FAP_OK) return rc;
+    e->fw_host_work += pl->pack == 1 ? pl->fw_pivot_work : pl->fw_tile_work;
     if (e->autotune && e->tile_cols == 0) return autotune_tiles(e, *pl, st);
     return FAP_OK;
   }
@@ -1329,6 +1341,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     Issuer is{e, *pl, st, false};
     if ((rc = is.all()) != FAP_OK) return rc;
   }
+  e->fw_host_work += pl->pack == 1 ? pl->fw_pivot_work : pl->fw_tile_work;
   e->last_launches = pl->launches;
   return FAP_OK;
 }
@@ -1870,6 +1883,18 @@ int fap_minplus_counters(fap_engine *e, uint64_t *out3, int32_t reset) {
   return FAP_OK;
 }
 
+int fap_fw_counters(fap_engine *e, uint64_t *out2, int32_t reset) {
+  if (!e || !out2) return set_error(FAP_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard g(e->device);
+  unsigned long long strip = 0;
+  FAP_CUDA(fapk::fw_strip_counter(&strip, reset != 0));
+  out2[0] = strip;
+  out2[1] = e->fw_host_work;
+  if (reset) e->fw_host_work = 0;
+  return FAP_OK;
+}
+
 int fap_last_launches(const fap_engine *e, int64_t *count) {
   if (!e || !count) return set_error(FAP_ERR_INVALID, "null argument");
   *count = e->last_launches;
@@ -2189,6 +2214,10 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
       if (value != 0.0 && value != 1.0) return set_error(FAP_ERR_INVALID, "host results must be 0 or 1");
       e->host_results = (int)value;
       return FAP_OK;
+    case FAP_OPT_INT32_FORM:
+      if (value != 0.0 && value != 1.0) return set_error(FAP_ERR_INVALID, "int32 form must be 0 or 1");
+      e->int32_form = (int)value;
+      return FAP_OK;
     default:
       return set_error(FAP_ERR_INVALID, "unknown option");
   }
@@ -2204,6 +2233,7 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_TILE_COLS: *value = e->tile_cols; return FAP_OK;
     case FAP_OPT_SSSP_METHOD: *value = e->sssp_method; return FAP_OK;
     case FAP_OPT_HOST_RESULTS: *value = e->host_results; return FAP_OK;
+    case FAP_OPT_INT32_FORM: *value = e->int32_form; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");
   }
 }

@@ -2,14 +2,18 @@
 // MatrixMarket reader, the K-way partitioner and the boundary/reorder step.
 // Pure C++ (no CUDA); exported through the C ABI in include/fastapsp.h.
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fap_internal.h"
@@ -72,9 +76,134 @@ bool next_double(Buf &b, double &v) {
   return true;
 }
 
+// Binary CSR cache beside the .mtx file (<path>.fapcsr): the reader's
+// output for one (directed, weighted) reading of one version of the file,
+// so that later reads skip the text parse.  Layout (host byte order):
+//   char magic[8] = "FAPCSR01"; int32 directed, weighted; uint64 source size;
+//   int64 source mtime (s), mtime (ns); int32 n; int64 header m; int64 m;
+//   int32 row_offset[n + 1]; int32 col_val[m]; float weight[m].
+// A cache is used only when every header field matches the file as it is now;
+// otherwise the file is parsed and the cache rewritten (through a temporary
+// file and a rename).  FAP_MTX_CACHE=0 in the environment turns it off.
+struct CacheHead {
+  char magic[8];
+  int32_t directed, weighted;
+  uint64_t src_size;
+  int64_t src_sec, src_nsec;
+  int32_t n;
+  int64_t header_m, m;
+};
+
+bool cache_enabled() {
+  const char *v = std::getenv("FAP_MTX_CACHE");
+  return !(v && v[0] == '0');
+}
+
+std::string cache_path(const char *path) { return std::string(path) + ".fapcsr"; }
+
+bool source_stamp(const char *path, uint64_t &size, int64_t &sec, int64_t &nsec) {
+  struct stat st;
+  if (stat(path, &st) != 0) return false;
+  size = (uint64_t)st.st_size;
+  sec = (int64_t)st.st_mtim.tv_sec;
+  nsec = (int64_t)st.st_mtim.tv_nsec;
+  return true;
+}
+
+// Opens the cache of `path` and reads its header when it matches the file
+// as it is now; returns the open stream (positioned after the header) or null.
+FILE *open_cache(const char *path, bool directed, bool weighted, CacheHead &h) {
+  if (!cache_enabled()) return nullptr;
+  uint64_t size;
+  int64_t sec, nsec;
+  if (!source_stamp(path, size, sec, nsec)) return nullptr;
+  FILE *f = std::fopen(cache_path(path).c_str(), "rb");
+  if (!f) return nullptr;
+  if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, "FAPCSR01", 8) != 0 ||
+      h.directed != (int32_t)directed || h.weighted != (int32_t)weighted || h.src_size != size ||
+      h.src_sec != sec || h.src_nsec != nsec || h.n < 0 || h.m < 0 || h.m > h.header_m) {
+    std::fclose(f);
+    return nullptr;
+  }
+  return f;
+}
+
+void write_cache(const char *path, bool directed, bool weighted, int32_t n, int64_t header_m,
+                 int64_t m, const int32_t *row_offset, const int32_t *col_val, const float *weight) {
+  if (!cache_enabled()) return;
+  CacheHead h{};
+  std::memcpy(h.magic, "FAPCSR01", 8);
+  h.directed = directed;
+  h.weighted = weighted;
+  if (!source_stamp(path, h.src_size, h.src_sec, h.src_nsec)) return;
+  h.n = n;
+  h.header_m = header_m;
+  h.m = m;
+  const std::string fin = cache_path(path), tmp = fin + ".tmp";
+  FILE *f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return;  // read-only directory: no cache
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+            std::fwrite(row_offset, sizeof(int32_t), (size_t)n + 1, f) == (size_t)n + 1 &&
+            std::fwrite(col_val, sizeof(int32_t), (size_t)m, f) == (size_t)m &&
+            std::fwrite(weight, sizeof(float), (size_t)m, f) == (size_t)m;
+  ok = std::fclose(f) == 0 && ok;
+  if (!ok || std::rename(tmp.c_str(), fin.c_str()) != 0) std::remove(tmp.c_str());
+}
+
+// The body's entries parsed by up to 16 threads, each over a run of whole
+// lines; concatenated in input order.
+struct Entries {
+  std::vector<int32_t> src, dst;
+  std::vector<float> w;
+  int bad = 0;  // 1: vertex id outside 1..n
+};
+
+void parse_lines(const char *p, const char *end, bool directed, bool weighted, int32_t n, Entries &out) {
+  while (p < end) {
+    char *q = nullptr;
+    while (p < end && std::isspace((unsigned char)*p)) p++;
+    if (p >= end) break;
+    const long long a = std::strtoll(p, &q, 10);
+    if (q == p) break;
+    p = q;
+    const long long c2 = std::strtoll(p, &q, 10);
+    if (q == p) break;
+    p = q;
+    double c = 1.0;
+    if (weighted) {
+      c = std::strtod(p, &q);
+      if (q == p) break;
+      p = q;
+    }
+    if (a < 1 || a > n || c2 < 1 || c2 > n) {
+      out.bad = 1;
+      return;
+    }
+    const float tc = weighted ? (float)std::fabs(c) : 1.0f;
+    out.src.push_back((int32_t)(a - 1));
+    out.dst.push_back((int32_t)(c2 - 1));
+    out.w.push_back(tc);
+    if (!directed) {
+      out.src.push_back((int32_t)(c2 - 1));
+      out.dst.push_back((int32_t)(a - 1));
+      out.w.push_back(tc);
+    }
+  }
+}
+
 }  // namespace
 
 int mtx_counts(const char *path, bool directed, int32_t *n, int64_t *m) {
+  CacheHead h;
+  // the cache records the flags it was read with; either reading gives the header counts
+  FILE *cf = open_cache(path, directed, false, h);
+  if (!cf) cf = open_cache(path, directed, true, h);
+  if (cf) {
+    std::fclose(cf);
+    *n = h.n;
+    *m = h.header_m;
+    return FAP_OK;
+  }
   Buf b;
   if (!slurp(path, b)) return set_error(FAP_ERR_IO, std::string("cannot open ") + path);
   skip_comment_lines(b);
@@ -89,36 +218,61 @@ int mtx_counts(const char *path, bool directed, int32_t *n, int64_t *m) {
 
 int mtx_read(const char *path, bool directed, bool weighted, int32_t n, int64_t m,
              int32_t *adj_size, int32_t *row_offset, int32_t *col_val, float *weight) {
+  {
+    CacheHead h;
+    if (FILE *cf = open_cache(path, directed, weighted, h)) {
+      bool ok = h.n == n && h.m <= m &&
+                std::fread(row_offset, sizeof(int32_t), (size_t)n + 1, cf) == (size_t)n + 1 &&
+                std::fread(col_val, sizeof(int32_t), (size_t)h.m, cf) == (size_t)h.m &&
+                std::fread(weight, sizeof(float), (size_t)h.m, cf) == (size_t)h.m;
+      std::fclose(cf);
+      if (ok) {
+        for (int32_t i = 0; i < n; i++) adj_size[i] = row_offset[i + 1] - row_offset[i];
+        return FAP_OK;
+      }  // a damaged cache: parse the file (and rewrite the cache) below
+    }
+  }
   Buf b;
   if (!slurp(path, b)) return set_error(FAP_ERR_IO, std::string("cannot open ") + path);
   skip_comment_lines(b);
   long long nn, t, mm;
   if (!next_ll(b, nn) || !next_ll(b, t) || !next_ll(b, mm))
     return set_error(FAP_ERR_IO, "bad MatrixMarket header");
-  // Entries in input order; each row is emitted newest-first afterwards.
+  // Entries in input order (threads over runs of whole lines, concatenated
+  // in order); each row is emitted newest-first afterwards.
+  const char *body = b.data.data() + b.pos, *body_end = b.data.data() + b.data.size() - 1;
+  const size_t len = (size_t)(body_end - body);
+  const int nt = (int)std::max<size_t>(1, std::min<size_t>({16, std::thread::hardware_concurrency() ? std::thread::hardware_concurrency() : 1, len / (1 << 20)}));
+  std::vector<const char *> cuts(nt + 1, body_end);
+  cuts[0] = body;
+  for (int i = 1; i < nt; i++) {
+    const char *c = body + len * i / nt;
+    while (c < body_end && *c != '\n') c++;
+    cuts[i] = std::max(c, cuts[i - 1]);
+  }
+  std::vector<Entries> parts(nt);
+  {
+    std::vector<std::thread> th;
+    for (int i = 1; i < nt; i++)
+      th.emplace_back(parse_lines, cuts[i], cuts[i + 1], directed, weighted, n, std::ref(parts[i]));
+    parse_lines(cuts[0], cuts[1], directed, weighted, n, parts[0]);
+    for (auto &x : th) x.join();
+  }
+  size_t total = 0;
+  for (const Entries &p : parts) {
+    if (p.bad) return set_error(FAP_ERR_RANGE, "vertex id outside 1..n in MatrixMarket body");
+    total += p.src.size();
+  }
   std::vector<int32_t> src, dst;
   std::vector<float> w;
-  src.reserve((size_t)m);
-  dst.reserve((size_t)m);
-  w.reserve((size_t)m);
-  for (;;) {
-    long long a, c2;
-    double c = 1.0;
-    if (!next_ll(b, a) || !next_ll(b, c2)) break;
-    if (weighted && !next_double(b, c)) break;
-    a--;
-    c2--;
-    if (a < 0 || a >= n || c2 < 0 || c2 >= n)
-      return set_error(FAP_ERR_RANGE, "vertex id outside 1..n in MatrixMarket body");
-    float tc = weighted ? (float)std::fabs(c) : 1.0f;
-    src.push_back((int32_t)a);
-    dst.push_back((int32_t)c2);
-    w.push_back(tc);
-    if (!directed) {
-      src.push_back((int32_t)c2);
-      dst.push_back((int32_t)a);
-      w.push_back(tc);
-    }
+  src.reserve(total);
+  dst.reserve(total);
+  w.reserve(total);
+  for (Entries &p : parts) {
+    src.insert(src.end(), p.src.begin(), p.src.end());
+    dst.insert(dst.end(), p.dst.begin(), p.dst.end());
+    w.insert(w.end(), p.w.begin(), p.w.end());
+    p = Entries();  // release the part's buffers
   }
   if ((int64_t)src.size() > m) return set_error(FAP_ERR_RANGE, "more entries than the header announces");
   std::vector<int64_t> cnt((size_t)n + 1, 0);
@@ -136,6 +290,8 @@ int mtx_read(const char *path, bool directed, bool weighted, int32_t n, int64_t 
     col_val[pos] = dst[e];
     weight[pos] = w[e];
   }
+  write_cache(path, directed, weighted, n, directed ? (int64_t)mm : 2 * (int64_t)mm, (int64_t)src.size(),
+              row_offset, col_val, weight);
   return FAP_OK;
 }
 

@@ -51,6 +51,9 @@ unsigned pack_limit();
 // with no active step, active steps over all tiles]; optionally reset.
 cudaError_t strip_counters(unsigned long long out[3], bool reset);
 int max_packed_k();
+// Add-mins executed by the FW remaining-tile strips on the current device
+// since the last reset; optionally reset.
+cudaError_t fw_strip_counter(unsigned long long *out, bool reset);
 cudaError_t launch_fw_diag(bool f32, bool pred, const FwDiagJob *d_jobs, int njobs,
                            cudaStream_t st);
 // Packed int32 form: closes each job's pivot block and updates its row and

@@ -1116,6 +1116,10 @@ __device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, in
   }
 }
 
+// Work counter of the FW remaining-tile strips (diagnostics): add-mins
+// executed (steps run x the tile's 128 x TN outputs), summed per CTA.
+__device__ unsigned long long g_fw_counters[1];
+
 template <bool PRED, int TN>
 __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     mp_fwstrip_kernel(const MpSegment *__restrict__ segs, int nseg) {
@@ -1173,6 +1177,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
   int32_t *const p_mat = s.Cp;
   const int64_t ldc = s.ldc, ldcp = s.ldcp;
   const int m_rows = s.M, n_cols = s.N;
+  unsigned long long n_work = 0;  // add-mins executed (thread 0)
 
   for (int jt = jt0; jt < jt1; jt++) {
     const int buf = (jt - jt0) & 1;
@@ -1254,6 +1259,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       unsigned long long msk = (unsigned long long)(s_kmask[buf][0] & s_amask[0]) |
                                ((unsigned long long)(s_kmask[buf][1] & s_amask[1]) << 32);
       if (kseg < 64) msk &= (1ull << kseg) - 1ull;
+      n_work += (unsigned long long)(__popcll(msk) == s.K ? kseg : __popcll(msk)) * kTile * TN;
       if (__popcll(msk) == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
         uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
@@ -1328,6 +1334,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     __syncthreads();  // C, B[buf] and the predecessors are free again
   }
   cp_async_wait_0();
+  if (threadIdx.x == 0 && n_work > 0) atomicAdd(&g_fw_counters[0], n_work);
 }
 
 template <typename T, bool PRED>
@@ -1863,6 +1870,13 @@ cudaError_t launch_max_finite(const MatRef *d_mats, int nmats, unsigned *out, cu
 }
 
 unsigned pack_limit() { return kPackH; }
+
+cudaError_t fw_strip_counter(unsigned long long *out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_fw_counters, sizeof(unsigned long long));
+  if (e != cudaSuccess || !reset) return e;
+  const unsigned long long zero = 0;
+  return cudaMemcpyToSymbol(g_fw_counters, &zero, sizeof(zero));
+}
 
 cudaError_t strip_counters(unsigned long long out[3], bool reset) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_strip_counters, sizeof(unsigned long long) * 3);

@@ -170,6 +170,13 @@ class Engine:
         check(lib().fap_minplus_counters(self._h, v, int(bool(reset))), "fap_minplus_counters")
         return dict(zip(["tiles", "empty_tiles", "executed_addmins"], list(v)))
 
+    def fw_counters(self, reset: bool = True):
+        """FW add-mins since the last reset: executed by the remaining-tile
+        strips (device counter) and by the other FW launches (block count)."""
+        v = (C.c_uint64 * 2)()
+        check(lib().fap_fw_counters(self._h, v, int(bool(reset))), "fap_fw_counters")
+        return dict(zip(["strip_addmins", "other_addmins"], list(v)))
+
     def sssp_stats(self):
         """Counters of the last solve's SSSP phase."""
         v = (C.c_uint64 * 5)()

@@ -40,6 +40,9 @@ class Graph:
     lines_dst: np.ndarray
     lines_w: np.ndarray
     integer_weights: bool = True
+    # Planar coordinates of the vertices where the generator has them (n x 2;
+    # None otherwise): the input of geometric partitioning baselines.
+    coords: np.ndarray = None
 
     @property
     def m(self) -> int:
@@ -136,7 +139,9 @@ def grid_graph(rows=128, cols=128, p=0.6, seed=20261204) -> Graph:
     sel = np.nonzero(keep)[0]
     sel = sel[rng.permutation(sel.shape[0])]  # input line order
     w = np.ones(sel.shape[0], dtype=np.float32)
-    return csr_from_lines(rows * cols, eu[sel], ev[sel], w, directed=False, weighted=False)
+    g = csr_from_lines(rows * cols, eu[sel], ev[sel], w, directed=False, weighted=False)
+    g.coords = np.stack(np.divmod(np.arange(rows * cols), cols), 1).astype(np.float64)
+    return g
 
 
 def geometric_knn(n=65536, k=3, wmin=1, wmax=1000, seed=20261205) -> Graph:
@@ -150,7 +155,9 @@ def geometric_knn(n=65536, k=3, wmin=1, wmax=1000, seed=20261205) -> Graph:
     src = np.repeat(np.arange(n), k)
     dst = nn[:, 1:].reshape(-1)
     w = rng.integers(wmin, wmax + 1, size=src.shape[0]).astype(np.float32)
-    return csr_from_lines(n, src, dst, w, directed=True, weighted=True)
+    g = csr_from_lines(n, src, dst, w, directed=True, weighted=True)
+    g.coords = pts
+    return g
 
 
 def road_like(n_target=114599, extra_ratio=0.0442, wmin=0.1, wmax=10.0, seed=20261207) -> Graph:
@@ -176,10 +183,13 @@ def road_like(n_target=114599, extra_ratio=0.0442, wmin=0.1, wmax=10.0, seed=202
     # distribute chain vertices over the base edges
     per_edge = np.bincount(rng.integers(0, bu.shape[0], size=n_chain), minlength=bu.shape[0])
     src, dst = [], []
+    xy = np.zeros((n_target, 2))
+    xy[:n0] = np.stack(np.divmod(np.arange(n0), cols), 1)
     nxt = n0
     for a, b, c in zip(bu.tolist(), bv.tolist(), per_edge.tolist()):
         prev = a
-        for _ in range(c):
+        for i in range(c):  # chain vertices evenly along the junctions' segment
+            xy[nxt] = xy[a] + (xy[b] - xy[a]) * (i + 1) / (c + 1)
             src.append(prev)
             dst.append(nxt)
             prev = nxt
@@ -194,8 +204,11 @@ def road_like(n_target=114599, extra_ratio=0.0442, wmin=0.1, wmax=10.0, seed=202
     order = rng.permutation(src.shape[0])
     src, dst = src[order], dst[order]
     w = rng.uniform(wmin, wmax, size=src.shape[0]).astype(np.float32)
-    return csr_from_lines(n_target, src, dst, w, directed=False, weighted=True,
-                          integer_weights=False)
+    g = csr_from_lines(n_target, src, dst, w, directed=False, weighted=True, integer_weights=False)
+    coords = np.empty_like(xy)
+    coords[perm] = xy
+    g.coords = coords
+    return g
 
 
 def regular_digraph(n, degree=4, wlo=0.5, whi=2.0, rng=None) -> Graph:

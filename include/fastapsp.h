@@ -221,6 +221,12 @@ int fap_precondition(fap_engine *e);
  *                      into the host rows (no device copy of the n x n
  *                      result; also the choice of 0 without room).  Same
  *                      rows either way.
+ *   FAP_OPT_INT32_FORM (int32 engines) 0 (default) = the FW and min-plus run
+ *                      on packed keys (distance << 7 | step, one DPX add-min)
+ *                      when the first run of a plan proves every finite
+ *                      result stays below 2^24 - 1, else on separate values
+ *                      and steps (the wide form); 1 = always the wide form.
+ *                      Same rows either way.
  * Setting an option takes effect from the next solve. */
 #define FAP_OPT_SSSP_FP64 1
 #define FAP_OPT_SSSP_DELTA 2
@@ -229,6 +235,7 @@ int fap_precondition(fap_engine *e);
 #define FAP_OPT_TILE_COLS 5
 #define FAP_OPT_SSSP_METHOD 6
 #define FAP_OPT_HOST_RESULTS 7
+#define FAP_OPT_INT32_FORM 8
 int fap_set_option(fap_engine *e, int32_t option, double value);
 int fap_get_option(const fap_engine *e, int32_t option, double *value);
 
@@ -245,6 +252,14 @@ int fap_last_launches(const fap_engine *e, int64_t *count);
  * the tile's outputs (128 x 64 or 128 x 128), summed over tiles].  reset != 0
  * clears them after reading. */
 int fap_minplus_counters(fap_engine *e, uint64_t *out3, int32_t reset);
+/* Floyd-Warshall work of the solves since the last reset (no reference
+ * counterpart; the executed-work view of the FW roofline): [add-mins the
+ * remaining-tile strips executed on the engine's GPU (steps they ran x tile
+ * outputs; they skip steps whose pivot row or column is unreached over the
+ * tile), add-mins of the other FW launches (the pivot steps' 64 x 64 x 64
+ * block products in the packed int32 form, every block in the other forms,
+ * which skip nothing)].  reset != 0 clears them after reading. */
+int fap_fw_counters(fap_engine *e, uint64_t *out2, int32_t reset);
 
 /* ---- standalone kernels on caller device memory ------------------------- */
 

@@ -8,7 +8,7 @@ reference binary with that partition (solve() for every case, plus
 solveSubGraph() for two parts of the last case).  The fixture stores the input
 lines, the partition, the reference's mapping and its dist/path outputs.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -39,13 +39,21 @@ def cases():
     yield "rand40_k1", graphs.small_random_graph(40, 90, True, True, seed=7), 1
     yield "tiny10_k3", graphs.small_random_graph(10, 12, False, False, seed=8), 3
     yield "grid16_sub", graphs.grid_graph(16, 16, p=0.6, seed=9), 5
+    # integer weights up to 3.5e6 on 300 vertices: (n - 1) * max weight stays
+    # below 2^30 (the int32 engine's limit) while many distances exceed
+    # 2^24 - 1, where the engine must leave its packed keys for the wide form
+    # and where the reference's FP32 arithmetic is no longer exact
+    yield "bigw300_dir_wide", graphs.small_random_graph(300, 650, True, True, seed=10, wmax=3_500_000), 4
 
 
 def main():
+    only = set(sys.argv[1:])  # case names to (re)generate; all when empty
     oracle.build(ref=True)
     with tempfile.TemporaryDirectory() as tmp:
         tmp = Path(tmp)
         for name, g, K in cases():
+            if only and name not in only:
+                continue
             typ = ("weight-" if g.weighted else "unweight-") + ("directed" if g.directed else "undirected")
             (tmp / "graph" / typ).mkdir(parents=True, exist_ok=True)
             graphs.write_mtx(g, str(tmp / "graph" / typ / f"{name}.mtx"))

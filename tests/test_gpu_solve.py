@@ -8,7 +8,9 @@ from helpers import MAXV, check_pred_tight, has_parallel_edges, to_ref_float
 
 pytestmark = pytest.mark.gpu
 
-INT_CASES = [n for n in GOLDEN if not n.endswith("f32")]
+# *_wide fixtures hold distances above 2^24, where the reference's FP32
+# arithmetic is inexact; tests/test_gpu_wide.py checks them
+INT_CASES = [n for n in GOLDEN if not n.endswith("f32") and not n.endswith("wide")]
 F32_CASES = [n for n in GOLDEN if n.endswith("f32")]
 
 
