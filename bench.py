@@ -112,8 +112,7 @@ def workload_config(name, g, K, gid, cut):
             "partition": f"tests/golden/partitions/partition_{wl['part']}.npz (the engine's multilevel partitioner, "
                          "committed; both arms solve the same parts)",
             "l2": "L2 flushed (256 MiB write) before every timed step; outputs "
-                  f"{g.n * g.n * 8 / 1e9:.1f} GB",
-            "parallelism": "replicas (one instance per GPU)"}
+                  f"{g.n * g.n * 8 / 1e9:.1f} GB"}
 
 
 def read_peaks():
@@ -238,14 +237,26 @@ def run_solve(args, name, rank, world, local_rank):
     for o, v in options.items():
         eng.set_option(o, v)
     subs, bdys, addmin_mp, addmin_fw = part_stats(eng, K, n)
-    dist = torch.empty((n, n), dtype=tdt, device="cuda")
-    pred = torch.empty((n, n), dtype=torch.int32, device="cuda")
+    # Under torchrun the parts of the one graph are split over the ranks by
+    # the cost-balanced assignment (no collective touches the rows); with
+    # --shard replicas every rank solves the whole graph instead.
+    share = None
+    if world > 1 and args.shard == "parts":
+        from fastapsp_gb300.sharding import assign_parts
+
+        share = assign_parts(np.r_[0, subs], np.r_[0, bdys], n, g.m, world)[rank]
+    rows = n if share is None else int(sum(subs[q - 1] for q in share))
+    dist = torch.empty((max(rows, 1), n), dtype=tdt, device="cuda")
+    pred = torch.empty((max(rows, 1), n), dtype=torch.int32, device="cuda")
     flush = torch.empty(64 << 20, dtype=torch.int32, device="cuda")  # 256 MiB > L2
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
 
     def step():
-        eng.solve(dist, pred, fap.MODE_BATCHED, stream=sptr)
+        if share is None:
+            eng.solve(dist, pred, fap.MODE_BATCHED, stream=sptr)
+        elif share:
+            eng.solve_parts(share, dist, pred, fap.MODE_BATCHED, stream=sptr)
 
     for _ in range(args.warmup):
         step()
@@ -278,7 +289,9 @@ def run_solve(args, name, rank, world, local_rank):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
-    value = world * float(n) * n / (ms_per_step / 1e3)
+    # whole-job distances per second: every rank's rows (n x n in all when the
+    # parts are shared out, n x n per rank for replicas) over the slowest rank
+    value = (world if share is None else 1) * float(n) * n / (ms_per_step / 1e3)
 
     ph = {k: statistics.mean(p[k] for p in phase) for k in phase[0]}
     sssp_stats = eng.sssp_stats()
@@ -313,7 +326,7 @@ def run_solve(args, name, rank, world, local_rank):
     # plain form (one launch sequence per part, the reference's loop) on the
     # same graph, for batched-vs-plain
     plain_ms = float("nan")
-    if args.plain:
+    if args.plain and world == 1:
         eng.solve(dist, pred, fap.MODE_PLAIN, stream=sptr)
         flush.fill_(1)
         a = torch.cuda.Event(enable_timing=True)
@@ -338,8 +351,8 @@ def run_solve(args, name, rank, world, local_rank):
     host_alloc = None
     if args.e2e_steps > 0:
         npdt = np.float32 if f32 else np.int32
-        dist_h, free_d, host_alloc = pinned_host((n, n), npdt)
-        pred_h, free_p, _ = pinned_host((n, n), np.int32)
+        dist_h, free_d, host_alloc = pinned_host((max(rows, 1), n), npdt)
+        pred_h, free_p, _ = pinned_host((max(rows, 1), n), np.int32)
         for i in range(1 + args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -348,7 +361,10 @@ def run_solve(args, name, rank, world, local_rank):
             for o, v in {**options, **tuned}.items():
                 e.set_option(o, v)
             tc = time.perf_counter()
-            e.solve(dist_h, pred_h, fap.MODE_BATCHED)
+            if share is None:
+                e.solve(dist_h, pred_h, fap.MODE_BATCHED)
+            elif share:
+                e.solve_parts(share, dist_h, pred_h, fap.MODE_BATCHED)
             ts = time.perf_counter()
             e.close()
             t1 = time.perf_counter()
@@ -360,20 +376,23 @@ def run_solve(args, name, rank, world, local_rank):
         del dist_h, pred_h
     e2e_ms_step = statistics.mean(e2e_ms) if e2e_ms else float("nan")
     h2d = int(g.row_offset.nbytes + g.col_val.nbytes + g.weight.nbytes + gid.nbytes)
-    d2h = int(n) * n * 8
+    d2h = int(rows) * n * 8
 
     traffic_scale = MP_TRAFFIC_PER_BYTE.get(name)
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if f32 else "int32", "data": "synthetic",
+        "scaling": "weak" if share is None else "strong", "vs_baseline": None,
+        "dtype": "f32" if f32 else "int32", "data": "synthetic",
+        "parallelism": (f"parts of the one graph shared out over {world} GPUs (cost-balanced, no collective on "
+                        f"the rows)" if share is not None else f"replicas x{world}"),
         "config": workload_config(name, g, K, gid, cut),
         "mode": "batched (one launch per phase, CUDA graph)",
         "arithmetic": ("SSSP exact (FP64 option), rounded once to FP32; FW and min-plus in FP32" if f32 and
                        wl["fp64_sssp"] else "f32 (the reference's)" if f32 else "int32 (exact)"),
         "tuning": {"sssp_delta": tuned[fap._lib.OPT_SSSP_DELTA],
                    "sssp_lanes": int(tuned[fap._lib.OPT_SSSP_LANES])},
-        "e2e": {"value": world * float(n) * n / (e2e_ms_step / 1e3), "unit": UNIT,
+        "e2e": {"value": (world if share is None else 1) * float(n) * n / (e2e_ms_step / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms_step,
                 "create_solve_destroy_ms": [statistics.mean(x) for x in zip(*e2e_parts)] if e2e_parts else None,
@@ -643,6 +662,9 @@ def main():
                     help="host work of the cpu_baseline sample (whole parts until this is reached)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
+    ap.add_argument("--shard", choices=["parts", "replicas"], default="parts",
+                    help="under torchrun: share the graph's parts out over the ranks (default) or solve "
+                         "the whole graph on every rank")
     ap.add_argument("--no-c3", dest="with_c3", action="store_false",
                     help="leave out the dense batched FW of 512 instances from the solve line")
     ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c4",

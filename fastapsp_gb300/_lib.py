@@ -61,6 +61,7 @@ SIGNATURES = {
     "fap_part_info": (C.c_int, [_p, _i32, _pi32, _pi32, _pi32]),
     "fap_solve_part": (C.c_int, [_p, _i32, _p, _p, _p]),
     "fap_solve": (C.c_int, [_p, _p, _p, _i32, _p]),
+    "fap_solve_parts": (C.c_int, [_p, _p, _i32, _p, _p, _i32, _p]),
     "fap_solve_all": (C.c_int, [_p, _p, _p, _p]),
     "fap_solve_batched": (C.c_int, [_p, _p, _p, _p]),
     "fap_set_partition": (C.c_int, [_p, _p]),
@@ -69,6 +70,7 @@ SIGNATURES = {
     "fap_last_launches": (C.c_int, [_p, C.POINTER(C.c_int64)]),
     "fap_minplus_counters": (C.c_int, [_p, C.POINTER(C.c_uint64), _i32]),
     "fap_fw_counters": (C.c_int, [_p, C.POINTER(C.c_uint64), _i32]),
+    "fap_query": (C.c_int, [_p, _p, _p, _i32, _p, _p, _p, _p, _p, _i32, _p]),
     "fap_minplus": (C.c_int, [_p, _i32, _i32, _i32, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i64,
                               _p, _i64, _p]),
     "fap_floyd_batched": (C.c_int, [_p, _i32, _i32, _p, _p, _p, _p, _p]),

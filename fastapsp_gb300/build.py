@@ -21,8 +21,8 @@ LIB = PKG / "libfastapsp.so"
 EXAMPLE = PKG / "fap_single_node"
 INCLUDE = PKG.parent / "include"
 
-CUDA_SOURCES = ["minplus.cu", "sssp.cu", "bgraph.cu", "transform.cu", "adjoint.cu", "probe.cu",
-                "engine.cu", "noalloc.cu"]
+CUDA_SOURCES = ["minplus.cu", "sssp.cu", "bgraph.cu", "transform.cu", "query.cu", "adjoint.cu",
+                "probe.cu", "engine.cu", "noalloc.cu"]
 CXX_SOURCES = ["host_prep.cpp", "fap_graph.cpp", "fap_more_task.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1810,6 +1810,22 @@ int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode, void *stre
   return solve_common(e, parts, e->n, dist, pred, mode, stream);
 }
 
+int fap_solve_parts(fap_engine *e, const int32_t *parts, int32_t nparts, void *dist, int32_t *pred,
+                    int32_t mode, void *stream) {
+  if (!e || !dist || !parts || nparts < 1) return set_error(FAP_ERR_INVALID, "null argument");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  if (mode != FAP_MODE_PLAIN && mode != FAP_MODE_BATCHED) return set_error(FAP_ERR_INVALID, "unknown mode");
+  std::vector<int32_t> list(parts, parts + nparts);
+  std::vector<char> seen(e->K + 1, 0);
+  int64_t rows = 0;
+  for (int32_t p : list) {
+    if (p < 1 || p > e->K) return set_error(FAP_ERR_INVALID, "part id outside 1..K");
+    if (seen[p]++) return set_error(FAP_ERR_INVALID, "part listed twice");
+    rows += e->ver_num[p];
+  }
+  return solve_common(e, list, rows, dist, pred, mode, stream);
+}
+
 int fap_solve_all(fap_engine *e, void *dist, int32_t *pred, void *stream) {
   return fap_solve(e, dist, pred, FAP_MODE_PLAIN, stream);
 }
@@ -1881,6 +1897,41 @@ int fap_minplus_counters(fap_engine *e, uint64_t *out3, int32_t reset) {
   FAP_CUDA(fapk::strip_counters(v, reset != 0));
   for (int i = 0; i < 3; i++) out3[i] = v[i];
   return FAP_OK;
+}
+
+int fap_query(fap_engine *e, const void *dist, const int32_t *pred, int32_t nq, const int32_t *src,
+              const int32_t *dst, void *out_dist, int32_t *out_len, int32_t *out_path, int32_t max_len,
+              void *stream) {
+  if (!e || nq < 0) return set_error(FAP_ERR_INVALID, "fap_query: bad arguments");
+  if (!e->has_graph) return set_error(FAP_ERR_STATE, "handle has no graph");
+  if (nq == 0) return FAP_OK;
+  if (!dist || !pred || !src || !dst || !out_dist || !out_len || (out_path && max_len < 1))
+    return set_error(FAP_ERR_INVALID, "fap_query: null buffer");
+  std::lock_guard<std::mutex> lk(e->mu);
+  DeviceGuard g(e->device);
+  fapi::clear_error();
+  const void *bufs[] = {dist, pred, src, dst, out_dist, out_len};
+  for (const void *b : bufs)
+    if (!is_device_ptr(b)) return set_error(FAP_ERR_INVALID, "fap_query: buffers must be device memory");
+  if (out_path && !is_device_ptr(out_path))
+    return set_error(FAP_ERR_INVALID, "fap_query: out_path must be device memory");
+  cudaStream_t st = pick_stream(e, stream);
+  fapk::QueryArgs a{};
+  a.n = e->n;
+  a.dist = dist;
+  a.pred = pred;
+  a.ed2st = e->d_ed2st;
+  a.nq = nq;
+  a.src = src;
+  a.dst = dst;
+  a.out_dist = out_dist;
+  a.out_len = out_len;
+  a.out_path = out_path;
+  a.max_len = max_len;
+  a.status = e->d_status;
+  FAP_CUDA(fapk::launch_query(e->f32(), a, st));
+  FAP_CUDA(cudaStreamSynchronize(st));
+  return check_status(e);
 }
 
 int fap_fw_counters(fap_engine *e, uint64_t *out2, int32_t reset) {

@@ -152,6 +152,22 @@ cudaError_t launch_bg_local(bool wide, const BgArgs &a, int njobs, int max_sub, 
 cudaError_t launch_bg_boundary(bool wide, const BgArgs &a, int njobs, cudaStream_t st);
 cudaError_t launch_bg_rows(bool wide, int lanes, const BgArgs &a, const BgRowArgs &r, cudaStream_t st);
 
+// query.cu -- point-to-point queries on solve() rows in device memory
+struct QueryArgs {
+  int32_t n;
+  const void *dist;        // n x n solve() rows (row = sorted position)
+  const int32_t *pred;
+  const int32_t *ed2st;    // vertex -> row
+  int32_t nq;
+  const int32_t *src, *dst;
+  void *out_dist;          // nq entries of the distance type
+  int32_t *out_len;        // vertices on each path (0: unreached)
+  int32_t *out_path;       // nq x max_len, may be null
+  int32_t max_len;
+  unsigned *status;
+};
+cudaError_t launch_query(bool f32, const QueryArgs &a, cudaStream_t st);
+
 // transform.cu
 struct PartDesc {
   int32_t sub, bdy, start;  // part size, boundary count, first sorted position

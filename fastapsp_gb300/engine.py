@@ -138,6 +138,12 @@ class Engine:
     def solve(self, dist, pred=None, mode=MODE_BATCHED, stream=None):
         check(lib().fap_solve(self._h, ptr(dist), ptr(pred), int(mode), stream), "fap_solve")
 
+    def solve_parts(self, parts, dist, pred=None, mode=MODE_BATCHED, stream=None):
+        """Rows of the listed parts, one part after another (fap_solve_parts)."""
+        pl = _i32(parts)
+        check(lib().fap_solve_parts(self._h, ptr(pl), int(pl.shape[0]), ptr(dist), ptr(pred), int(mode), stream),
+              "fap_solve_parts")
+
     def solve_part(self, part: int, dist, pred=None, stream=None):
         check(lib().fap_solve_part(self._h, int(part), ptr(dist), ptr(pred), stream), "fap_solve_part")
 
@@ -169,6 +175,13 @@ class Engine:
         v = (C.c_uint64 * 3)()
         check(lib().fap_minplus_counters(self._h, v, int(bool(reset))), "fap_minplus_counters")
         return dict(zip(["tiles", "empty_tiles", "executed_addmins"], list(v)))
+
+    def query(self, dist, pred, src, dst, out_dist, out_len, out_path=None, max_len=0, stream=None):
+        """Point-to-point distances and paths from device-resident solve()
+        rows (fap_query); every argument is a device buffer."""
+        n = int(src.numel()) if hasattr(src, "numel") else len(src)
+        check(lib().fap_query(self._h, ptr(dist), ptr(pred), n, ptr(src), ptr(dst), ptr(out_dist),
+                              ptr(out_len), ptr(out_path), int(max_len), stream), "fap_query")
 
     def fw_counters(self, reset: bool = True):
         """FW add-mins since the last reset: executed by the remaining-tile
@@ -404,6 +417,41 @@ class FapGraph:
     def getSubGraphPath(self, sub_graph_id):
         assert self.current_subgraph_id == sub_graph_id
         return self.subgraph_path
+
+    def _row_of(self, s):
+        """(distance row, predecessor row) of vertex s from the last solve()
+        or, after solveSubGraph, from the current part."""
+        if self.dist is not None and not self.is_split:
+            r = int(self.ed2st[s])
+            return self.dist[r], self.path[r]
+        off = int(self.C_BlockVer_offset[self.current_subgraph_id])
+        r = int(self.ed2st[s]) - off
+        if not 0 <= r < self.subgraph_dist.shape[0]:
+            raise ValueError("vertex not in the current subgraph")
+        return self.subgraph_dist[r], self.subgraph_path[r]
+
+    def getDistanceP2P(self, source, target):
+        """Distance from source to target (1e8 when unreached); declared by
+        the reference without a body (fap/fap.cpp:674-680)."""
+        if not (0 <= source < self.num_vertexs and 0 <= target < self.num_vertexs):
+            raise IndexError("vertex id")
+        return float(self._row_of(source)[0][target])
+
+    def getPathP2P(self, source, target):
+        """Vertices from source to target along the predecessors ([] when
+        unreached)."""
+        if not (0 <= source < self.num_vertexs and 0 <= target < self.num_vertexs):
+            raise IndexError("vertex id")
+        prow = self._row_of(source)[1]
+        out, v = [], int(target)
+        for _ in range(self.num_vertexs + 1):
+            if v < 0:
+                return []
+            out.append(v)
+            if v == source:
+                return out[::-1]
+            v = int(prow[v])
+        return []
 
     def getTimeSSSP(self):
         return self.times["sssp"]

@@ -150,6 +150,17 @@ int fap_solve_part(fap_engine *e, int32_t part, void *dist, int32_t *pred,
 int fap_solve(fap_engine *e, void *dist, int32_t *pred, int32_t mode,
               void *stream);
 
+/* Several parts in one call (no single reference counterpart: the
+ * reference's MPI task layer runs solveSubGraph over each process's parts,
+ * fap/fap_more_task_mpi.cpp:34-91): the rows of parts[0..nparts) go to
+ * dist/pred one part after another in the order listed, each part's rows in
+ * mapping order (sub_i x n each); mode as fap_solve (FAP_MODE_BATCHED: one
+ * launch per phase over all listed parts).  This is what a process of a
+ * part-sharded multi-GPU run calls with its share of the parts.  Parts must
+ * be distinct, 1..K. */
+int fap_solve_parts(fap_engine *e, const int32_t *parts, int32_t nparts,
+                    void *dist, int32_t *pred, int32_t mode, void *stream);
+
 /* fap_solve in each mode by name: solve() part by part
  * (fap/fap.cpp:507-518), and the batched form. */
 int fap_solve_all(fap_engine *e, void *dist, int32_t *pred, void *stream);
@@ -348,6 +359,23 @@ int fap_sssp_noalloc(int32_t dtype, int32_t n, int64_t m,
                      const int32_t *in_col_val, const void *in_weight,
                      const int32_t *sources, int32_t num_sources, void *dist,
                      int32_t *pred, int64_t ld, void *stream);
+
+/* Point-to-point queries on the rows of a full fap_solve kept in device
+ * memory (no reference counterpart: the reference declares getDistanceP2P /
+ * getPathP2P, fap/fap.h:144-145, without bodies, fap/fap.cpp:674-680, and
+ * keeps its results in host vectors).  dist / pred: the n x n solve() rows
+ * on the engine's GPU (row r = vertex mapping[r], columns = vertex ids);
+ * src[nq] / dst[nq]: vertex ids; all buffers device memory.  For query q:
+ * out_dist[q] = the distance (int32 or float like dist; the unreached
+ * sentinel when there is no path), out_len[q] = vertices on the path
+ * src..dst (1 when src == dst, 0 when unreached), and, when out_path is not
+ * NULL, that path in out_path[q * max_len ...] when it has at most max_len
+ * vertices (a longer path reports its length and leaves its slots as they
+ * were).  Ids outside 0..n-1, or predecessors that do not lead back to src
+ * within n steps, give FAP_ERR_INVALID.  Synchronizes `stream`. */
+int fap_query(fap_engine *e, const void *dist, const int32_t *pred, int32_t nq,
+              const int32_t *src, const int32_t *dst, void *out_dist,
+              int32_t *out_len, int32_t *out_path, int32_t max_len, void *stream);
 
 /* ---- diagnostics -------------------------------------------------------- */
 
