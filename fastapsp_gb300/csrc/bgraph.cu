@@ -31,8 +31,9 @@
 //
 // Step 3 writes the same vertex-major per-batch tables as the whole-graph
 // search (sssp.cu), and the same output pass turns them into rows:
-// predecessors by the Dijkstra tie rule from the in-edges, rounding (FP32
-// from the fixed point through FP64, which is exact here: one rounding),
+// predecessors by the Dijkstra tie rule from the in-edges (for FP32 graphs
+// with integer comparisons in the fixed-point units), rounding (FP32 from the
+// fixed point: an exact product by 2^-shift in FP64, then one rounding),
 // transposes and coalesced row stores.
 
 #include <cuda_runtime.h>
@@ -80,30 +81,67 @@ __host__ __device__ inline size_t bg_smem(int N) {
 // shared memory.  `relax(u, lane, du, push)` relaxes node u's out-edges for
 // one lane (du = that lane's distance of u) and calls push(v, improved) once
 // per edge in lockstep across the group's lanes.  The sources' own entries
-// were set to 0 and listed by the caller.  Returns false at the round cap.
+// were set to 0 and listed by the caller.
+//
+// With delta > 0 the frontier is worked in distance order, as in
+// delta-stepping: a node whose smallest distance over the lanes is above a
+// threshold stays in the frontier unrelaxed, and when a round has relaxed
+// nothing the threshold moves to the smallest deferred distance + delta.
+// Nodes are then relaxed about once each instead of being re-relaxed every
+// time a lane improves them (on the boundary graph of the 114,599-vertex
+// road-like graph each node was relaxed about ten times).  The order of the
+// relaxations never changes the fixpoint the distances converge to.
+// Returns false at the round cap.
 template <typename V, typename Relax>
-__device__ bool bg_bellman_ford(V *d, int *list0, unsigned *bits0, int N, int *s_cnt, Relax relax,
+__device__ bool bg_bellman_ford(V *d, int *list0, unsigned *bits0, int N, int *s_cnt, V delta, Relax relax,
                                 unsigned long long &rounds, unsigned long long &visited) {
+  __shared__ int s_done[2];                  // nodes relaxed in the round (by round parity)
+  __shared__ unsigned long long s_defer[2];  // smallest deferred distance (by round parity)
   const int words = (N + 31) / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = lane / kBgLanes, gl = lane % kBgLanes;
+  if (threadIdx.x < 2) {
+    s_done[threadIdx.x] = 0;
+    s_defer[threadIdx.x] = ~0ull;
+  }
+  __syncthreads();
+  V thr = delta;
   int cur = 0;
   for (int r = 0;; r++) {
     const int f = s_cnt[cur];
     if (f == 0) return true;
-    if (r > N + 1) return false;  // a shortest path has at most N - 1 edges
+    // a shortest path has at most N - 1 edges; rounds that only defer
+    // alternate with rounds that relax
+    if (r > 4 * N + 16) return false;
     rounds++;
-    visited += (unsigned long long)f;
+    const int par = r & 1;
     const int nxt = cur ^ 1;
     const int *lcur = list0 + cur * N;
     int *lnxt = list0 + nxt * N;
     unsigned *bcur = bits0 + cur * words, *bnxt = bits0 + nxt * words;
     for (int base = warp * kBgGroups; base < f; base += kBgWarps * kBgGroups) {
       const int idx = base + grp;
-      const int u = idx < f ? lcur[idx] : -1;
-      if (u >= 0 && gl == 0) atomicAnd(&bcur[u >> 5], ~(1u << (u & 31)));
-      const V du = u >= 0 ? d[(size_t)u * kBgLanes + gl] : bg_inf<V>();
-      relax(u, gl, du, [&](int v, bool improved) {
+      int u = idx < f ? lcur[idx] : -1;
+      V du = u >= 0 ? d[(size_t)u * kBgLanes + gl] : bg_inf<V>();
+      V key = du;
+#pragma unroll
+      for (int o = 1; o < kBgLanes; o <<= 1) {
+        const V other = __shfl_xor_sync(0xffffffffu, key, o);
+        key = other < key ? other : key;
+      }
+      const bool defer = delta > 0 && u >= 0 && key > thr;
+      if (u >= 0 && gl == 0) {
+        atomicAnd(&bcur[u >> 5], ~(1u << (u & 31)));
+        if (defer) {
+          if (bg_set_bit(bnxt, u)) lnxt[atomicAdd(&s_cnt[nxt], 1)] = u;
+          atomicMin(&s_defer[par], (unsigned long long)key);
+        } else {
+          atomicAdd(&s_done[par], 1);
+        }
+      }
+      if (defer) u = -1;
+      if (u >= 0) visited++;
+      relax(u, gl, u >= 0 ? du : bg_inf<V>(), [&](int v, bool improved) {
         // one lane of the group files v when any lane improved it
         const unsigned bal = __ballot_sync(0xffffffffu, improved);
         const unsigned gmask = ((1u << kBgLanes) - 1u) << (grp * kBgLanes);
@@ -111,7 +149,12 @@ __device__ bool bg_bellman_ford(V *d, int *list0, unsigned *bits0, int N, int *s
       });
     }
     __syncthreads();
-    if (threadIdx.x == 0) s_cnt[cur] = 0;
+    if (delta > 0 && s_done[par] == 0) thr = (V)s_defer[par] + delta;  // nothing was below it
+    if (threadIdx.x == 0) {
+      s_cnt[cur] = 0;
+      s_done[par ^ 1] = 0;  // last read in the previous round
+      s_defer[par ^ 1] = ~0ull;
+    }
     cur = nxt;
     __syncthreads();
   }
@@ -151,7 +194,7 @@ __global__ void __launch_bounds__(kBgThreads) bg_local_kernel(BgArgs a) {
   const int lane = threadIdx.x & 31;
   unsigned long long rounds = 0, visited = 0;
   const bool ok = bg_bellman_ford<V>(
-      d, list0, bits0, N, s_cnt,
+      d, list0, bits0, N, s_cnt, (V)a.delta_local,
       [&](int u, int gl, V du, auto push) {
         int e0 = 0, deg = 0;
         if (u >= 0) {
@@ -217,7 +260,7 @@ __global__ void __launch_bounds__(kBgThreads) bg_boundary_kernel(BgArgs a) {
   const V *cw = static_cast<const V *>(a.cw);
   unsigned long long rounds = 0, visited = 0;
   const bool ok = bg_bellman_ford<V>(
-      d, list0, bits0, N, s_cnt,
+      d, list0, bits0, N, s_cnt, (V)a.delta_boundary,
       [&](int u, int gl, V du, auto push) {
         // the node's part-mates (row of its part's local rows), then its cut edges
         int nb = 0, boff = 0, e0 = 0, ncut = 0;
@@ -277,7 +320,7 @@ __device__ __forceinline__ V bg_addmin(V x, V y, V acc) {
 // Step 3: rows of one SSSP batch (LANES sources) over the vertices of one
 // part, written into the batch's vertex-major table (slot = batch index):
 // D[s][v] = min over the part's boundary b of D_S[s][b] + L_q[b][v].
-// OUT64: table of FP64 values (fixed point x scale, exact), else uint32.
+// OUT64: table of 64-bit fixed-point values, else uint32.
 template <typename V, int LANES, bool OUT64>
 __global__ void __launch_bounds__(kRowThreads) bg_rows_kernel(BgArgs a, BgRowArgs r) {
   constexpr int kRowTJ = row_tj<V>();
@@ -330,9 +373,8 @@ __global__ void __launch_bounds__(kRowThreads) bg_rows_kernel(BgArgs a, BgRowArg
       if (j0 + jj >= q.sub) continue;
       const int v = r.st2ed[q.start + j0 + jj];
       K out;
-      if constexpr (OUT64) {
-        const double x = acc[o] >= bg_inf<V>() || l >= cnt ? 1e8 : (double)acc[o] * r.scale;
-        out = (K)__double_as_longlong(x);
+      if constexpr (OUT64) {  // fixed point as it is (the output pass rounds it)
+        out = (l >= cnt || acc[o] >= r.fix_inf) ? (K)r.fix_inf : (K)acc[o];
       } else {
         out = (l >= cnt || acc[o] >= bg_inf<V>()) ? (K)bg_inf<V>() : (K)acc[o];
       }
@@ -397,7 +439,7 @@ cudaError_t launch_bg_boundary(bool wide, const BgArgs &a, int njobs, cudaStream
 
 cudaError_t launch_bg_rows(bool wide, int lanes, const BgArgs &a, const BgRowArgs &r, cudaStream_t st) {
   if (r.nbatches <= 0 || a.nparts <= 0) return cudaSuccess;
-  if (wide) {  // FP32 graphs in fixed point: FP64 tables (the FP64 search's layout)
+  if (wide) {  // FP32 graphs in fixed point: 8-byte tables (the FP64 search's layout)
     if (lanes == 16) return launch_rows_t<unsigned long long, 16, true>(a, r, st);
     if (lanes == 32) return launch_rows_t<unsigned long long, 32, true>(a, r, st);
     return cudaErrorInvalidValue;

@@ -89,6 +89,11 @@ struct SsspArgs {
   unsigned long long *stats;  // may be null: [near steps, far splits, frontier
                               // vertices relaxed, far entries scanned, batches]
   int32_t defer_output;       // set by launch_sssp: output pass in its own launch
+  // launch_sssp_output on tables of exact 64-bit fixed point (FP32 graphs):
+  int32_t fix;                        // 1: tables hold fixed-point values, not FP64
+  const unsigned long long *iwfix;    // in-edge weights in the same units
+  unsigned long long fix_inf;         // values at or above are unreached
+  double fix_scale;                   // 2^-shift: fixed point -> distance
 };
 // delta value that puts every vertex in the near frontier (plain frontier BF)
 constexpr double kSsspNoDelta = 2147483647.0;
@@ -135,6 +140,9 @@ struct BgArgs {
   void *DS;                    // [B][B] boundary-graph distances, row = source boundary index
   unsigned *status;
   unsigned long long *stats;   // may be null: [rounds, -, nodes visited, -, -]
+  // threshold steps of the distance-ordered frontier (0: plain Bellman-Ford),
+  // in the weights' units, for steps 1 and 2
+  unsigned long long delta_local, delta_boundary;
 };
 struct BgRowArgs {
   const SsspBatch *batches;
@@ -142,7 +150,7 @@ struct BgRowArgs {
   const int32_t *st2ed;
   void *scratch;               // batch b's table at scratch + b * slot_bytes
   size_t slot_bytes;
-  double scale;                // 2^-shift (fixed point -> FP64)
+  unsigned long long fix_inf;  // wide tables: entries at or above are unreached (written as fix_inf)
 };
 constexpr size_t kBgSmemMax = 226 * 1024;  // dynamic; the 227 KB per-block limit also holds the static part
 size_t bg_smem_bytes(bool wide, int nodes);  // shared memory of steps 1 and 2 over `nodes` nodes

@@ -96,26 +96,36 @@ struct Acc<float, true> {  // FP32 weights, FP64 search
   static __device__ __forceinline__ V from_double(double x) { return x; }
 };
 
+// FP32 graphs whose tables hold exact 64-bit fixed-point distances (the
+// boundary-graph method, bgraph.cu): integer comparisons against the in-edge
+// weights in the same units, one rounding to FP32 at the end.
+struct AccFix {
+  using V = unsigned long long;
+  using K = unsigned long long;
+  static __device__ __forceinline__ V val(K k) { return k; }
+  static __device__ __forceinline__ K inf() { return ~0ull; }  // the real bound is SsspArgs::fix_inf
+};
+
 // Predecessors and transposed output of one 32-vertex block of batch b (the
 // calling warp's; the warp synchronizes only with itself).  A lane group
 // takes two vertices at a time and scans their in-edge lists side by side
 // (edge j of both per iteration), so their loads overlap; the block then
 // goes through the warp's shared-memory tile so that every source row is
 // written with coalesced stores.
-template <typename T, bool PRED, int LANES, bool ACC64>
-__device__ __forceinline__ void sssp_out_block(const SsspArgs &a,
-                                               const typename Acc<T, ACC64>::K *dvm, int b,
-                                               int cnt, int my_src, int v0, OutTile<LANES> &tile,
-                                               unsigned &local_max) {
-  using A = Acc<T, ACC64>;
+template <typename T, bool PRED, int LANES, bool ACC64, bool FIX = false>
+__device__ __forceinline__ void sssp_out_block(
+    const SsspArgs &a, const typename std::conditional<FIX, AccFix, Acc<T, ACC64>>::type::K *dvm, int b,
+    int cnt, int my_src, int v0, OutTile<LANES> &tile, unsigned &local_max) {
+  using A = typename std::conditional<FIX, AccFix, Acc<T, ACC64>>::type;
   using V = typename A::V;
   using K = typename A::K;
+  using W = typename std::conditional<FIX, unsigned long long, unsigned>::type;
   constexpr int VPW = 32 / LANES;
   const int lane = threadIdx.x & 31;
   const int sub = lane / LANES, sl = lane % LANES;
   const int32_t n = a.n;
   const unsigned *iwb = static_cast<const unsigned *>(a.iw);
-  const K INF = A::inf();
+  const K INF = FIX ? (K)a.fix_inf : A::inf();
   for (int vb = 0; vb < 32; vb += 2 * VPW) {
     int vv[2], e0[2], deg[2], bu[2];
     K dk[2], bdu[2];
@@ -139,18 +149,26 @@ __device__ __forceinline__ void sssp_out_block(const SsspArgs &a,
       if (!__any_sync(0xffffffffu, dk[0] < INF || dk[1] < INF)) dmax = 0;
       for (int j = 0; j < dmax; j++) {
         int u[2];
-        unsigned wq[2];
+        W wq[2];
         K duk[2];
 #pragma unroll
         for (int i = 0; i < 2; i++) {
           const bool has = j < deg[i];
           u[i] = has ? a.icol[e0[i] + j] : 0;
-          wq[i] = has ? iwb[e0[i] + j] : 0u;
+          if constexpr (FIX)
+            wq[i] = has ? a.iwfix[e0[i] + j] : 0ull;
+          else
+            wq[i] = has ? iwb[e0[i] + j] : 0u;
           duk[i] = (has && dk[i] < INF) ? __ldcg(&dvm[(size_t)u[i] * LANES + sl]) : INF;
         }
 #pragma unroll
         for (int i = 0; i < 2; i++) {
-          const bool better = duk[i] < INF && A::val(duk[i]) + A::weight(wq[i]) == dvv[i] &&
+          bool tight;
+          if constexpr (FIX)
+            tight = duk[i] + wq[i] == dvv[i];
+          else
+            tight = A::val(duk[i]) + A::weight(wq[i]) == dvv[i];
+          const bool better = duk[i] < INF && tight &&
                               (duk[i] < bdu[i] || (duk[i] == bdu[i] && u[i] < bu[i]));
           bdu[i] = better ? duk[i] : bdu[i];
           bu[i] = better ? u[i] : bu[i];
@@ -162,7 +180,10 @@ __device__ __forceinline__ void sssp_out_block(const SsspArgs &a,
       unsigned dv_out = Dist<T>::bits(Dist<T>::inf());
       int32_t p = -1;
       if (dk[i] < INF) {
-        dv_out = A::out(dk[i]);
+        if constexpr (FIX)
+          dv_out = __float_as_uint((float)((double)dk[i] * a.fix_scale));  // exact product, one rounding
+        else
+          dv_out = A::out(dk[i]);
         if (!std::is_same<T, float>::value) local_max = max(local_max, dv_out);
         if (PRED) p = vv[i] == my_src ? vv[i] : bu[i];
       }
@@ -185,23 +206,23 @@ __device__ __forceinline__ void sssp_out_block(const SsspArgs &a,
 // Output pass of every batch at once, after a search launch that deferred it
 // (one batch per search CTA, so batch b's distance table is slot b): block
 // (x, b) has its warps take 32-vertex blocks x * warps + w of batch b.
-template <typename T, bool PRED, int LANES, bool ACC64>
+template <typename T, bool PRED, int LANES, bool ACC64, bool FIX = false>
 __global__ void __launch_bounds__(kOutThreads)
     sssp_output_kernel(SsspArgs a) {
-  using A = Acc<T, ACC64>;
+  using A = typename std::conditional<FIX, AccFix, Acc<T, ACC64>>::type;
   using K = typename A::K;
   extern __shared__ __align__(16) unsigned char out_smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   OutTile<LANES> &tile = reinterpret_cast<OutTile<LANES> *>(out_smem_raw)[warp];
   const int b = blockIdx.y;
   const K *dvm = reinterpret_cast<const K *>(static_cast<const unsigned char *>(a.scratch) +
-                                             (size_t)b * slot_bytes(a.n, ACC64 && LANES == 32));
+                                             (size_t)b * slot_bytes(a.n, (ACC64 || FIX) && LANES == 32));
   const int cnt = a.batches[b].count;
   const int sl = lane % LANES;
   const int my_src = sl < cnt ? a.batches[b].src[sl] : -1;
   unsigned local_max = 0;
   const int v0 = (blockIdx.x * (kOutThreads / 32) + warp) * 32;
-  if (v0 < a.n) sssp_out_block<T, PRED, LANES, ACC64>(a, dvm, b, cnt, my_src, v0, tile, local_max);
+  if (v0 < a.n) sssp_out_block<T, PRED, LANES, ACC64, FIX>(a, dvm, b, cnt, my_src, v0, tile, local_max);
   if (a.maxd != nullptr) {
     local_max = __reduce_max_sync(0xffffffffu, local_max);
     if (lane == 0 && local_max) atomicMax(a.maxd, local_max);
@@ -499,16 +520,22 @@ cudaError_t launch_one(const SsspArgs &a0, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <typename T, bool PRED, int LANES, bool ACC64>
+template <typename T, bool PRED, int LANES, bool ACC64, bool FIX = false>
 cudaError_t launch_output(const SsspArgs &a, cudaStream_t st) {
   const dim3 grid((unsigned)((a.n + kOutThreads - 1) / kOutThreads), (unsigned)a.nbatches);
   ++launch_count();
-  sssp_output_kernel<T, PRED, LANES, ACC64><<<grid, kOutThreads, out_kernel_smem<LANES>(), st>>>(a);
+  sssp_output_kernel<T, PRED, LANES, ACC64, FIX><<<grid, kOutThreads, out_kernel_smem<LANES>(), st>>>(a);
   return cudaGetLastError();
 }
 
 template <typename T, bool PRED>
 cudaError_t launch_output_t(const SsspArgs &a, cudaStream_t st) {
+  if (a.fix) {
+    if constexpr (std::is_same<T, float>::value)
+      return a.lanes == 16 ? launch_output<float, PRED, 16, false, true>(a, st)
+                           : launch_output<float, PRED, 32, false, true>(a, st);
+    return cudaErrorInvalidValue;
+  }
   if (a.acc64) {
     if constexpr (std::is_same<T, float>::value)
       return a.lanes == 16 ? launch_output<float, PRED, 16, true>(a, st) : launch_output<float, PRED, 32, true>(a, st);
@@ -568,6 +595,16 @@ cudaError_t init_sssp_kernels() {
   FAP_SSSP_ATTR(float, true, 32, true)
   FAP_SSSP_ATTR(float, false, 32, true)
 #undef FAP_SSSP_ATTR
+#define FAP_OUT_FIX_ATTR(P, L)                                                                     \
+  if ((e = cudaFuncSetAttribute(sssp_output_kernel<float, P, L, false, true>,                      \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,                       \
+                                (int)out_kernel_smem<L>())) != cudaSuccess)                        \
+    return e;
+  FAP_OUT_FIX_ATTR(true, 16)
+  FAP_OUT_FIX_ATTR(false, 16)
+  FAP_OUT_FIX_ATTR(true, 32)
+  FAP_OUT_FIX_ATTR(false, 32)
+#undef FAP_OUT_FIX_ATTR
   return cudaSuccess;
 }
 
@@ -584,7 +621,8 @@ cudaError_t launch_sssp(bool f32, const SsspArgs &a, cudaStream_t st) {
 cudaError_t launch_sssp_output(bool f32, const SsspArgs &a, cudaStream_t st) {
   if (a.nbatches <= 0) return cudaSuccess;
   if (a.lanes != 8 && a.lanes != 16 && a.lanes != 32) return cudaErrorInvalidValue;
-  if (a.acc64 && (!f32 || a.lanes == 8)) return cudaErrorInvalidValue;
+  if ((a.acc64 || a.fix) && (!f32 || a.lanes == 8)) return cudaErrorInvalidValue;
+  if (a.fix && a.iwfix == nullptr && a.pred != nullptr) return cudaErrorInvalidValue;
   if (a.slots < a.nbatches) return cudaErrorInvalidValue;
   const bool pred = a.pred != nullptr;
   if (f32) return pred ? launch_output_t<float, true>(a, st) : launch_output_t<float, false>(a, st);
