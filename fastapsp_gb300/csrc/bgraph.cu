@@ -53,11 +53,9 @@ constexpr int kBgThreads = 512;
 constexpr int kBgWarps = kBgThreads / 32;
 constexpr int kBgLanes = 8;          // sources per CTA in steps 1 and 2
 constexpr int kBgGroups = 32 / kBgLanes;  // frontier nodes a warp relaxes at once
+constexpr int kBgEdges = 8;               // edges of a node whose loads are in flight together
 constexpr int kRowThreads = 256;     // step 3
-constexpr int kRowTA = 64;           // boundary vertices per step-3 chunk
-// vertices of a part per step-3 tile (static shared memory stays below 48 KB)
-template <typename V>
-__host__ __device__ constexpr int row_tj() { return sizeof(V) == 8 ? 32 : 64; }
+constexpr int kRowTA = 32;           // boundary vertices per step-3 chunk
 
 template <typename V>
 __host__ __device__ constexpr V bg_inf() {
@@ -204,14 +202,23 @@ __global__ void __launch_bounds__(kBgThreads) bg_local_kernel(BgArgs a) {
         int dmax = deg;
 #pragma unroll
         for (int o = kBgLanes; o < 32; o <<= 1) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-        for (int t = 0; t < dmax; t++) {
-          bool imp = false;
-          int v = 0;
-          if (t < deg) {
-            v = a.lcol[e0 + t];
-            if (du < bg_inf<V>()) imp = bg_try(&d[(size_t)v * kBgLanes + gl], (V)(du + lw[e0 + t]));
+        // kBgEdges edges at a time: their loads issue together
+        for (int t0 = 0; t0 < dmax; t0 += kBgEdges) {
+          int v[kBgEdges];
+          V w[kBgEdges];
+#pragma unroll
+          for (int q = 0; q < kBgEdges; q++) {
+            const bool in = t0 + q < deg;
+            v[q] = in ? a.lcol[e0 + t0 + q] : 0;
+            w[q] = in ? lw[e0 + t0 + q] : bg_inf<V>();
           }
-          push(v, imp);
+#pragma unroll
+          for (int q = 0; q < kBgEdges; q++) {
+            if (t0 + q >= dmax) break;  // uniform over the warp
+            bool imp = false;
+            if (t0 + q < deg && du < bg_inf<V>()) imp = bg_try(&d[(size_t)v[q] * kBgLanes + gl], (V)(du + w[q]));
+            push(v[q], imp);
+          }
         }
         (void)lane;
       },
@@ -278,21 +285,31 @@ __global__ void __launch_bounds__(kBgThreads) bg_boundary_kernel(BgArgs a) {
 #pragma unroll
         for (int o = kBgLanes; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
         const bool live = du < bg_inf<V>();
-        for (int t = 0; t < tmax; t++) {
-          bool imp = false;
-          int v = 0;
-          if (t < tot) {
-            V w;
+        // kBgEdges edges at a time: their loads issue together
+        for (int t0 = 0; t0 < tmax; t0 += kBgEdges) {
+          int v[kBgEdges];
+          V w[kBgEdges];
+#pragma unroll
+          for (int q = 0; q < kBgEdges; q++) {
+            const int t = t0 + q;
+            v[q] = 0;
+            w[q] = bg_inf<V>();
             if (t < nb) {
-              v = boff + t;
-              w = Lrow[t];
-            } else {
-              v = a.ccol[e0 + t - nb];
-              w = cw[e0 + t - nb];
+              v[q] = boff + t;
+              w[q] = Lrow[t];
+            } else if (t < tot) {
+              v[q] = a.ccol[e0 + t - nb];
+              w[q] = cw[e0 + t - nb];
             }
-            if (live && v != u && w < bg_inf<V>()) imp = bg_try(&d[(size_t)v * kBgLanes + gl], (V)(du + w));
           }
-          push(v, imp);
+#pragma unroll
+          for (int q = 0; q < kBgEdges; q++) {
+            if (t0 + q >= tmax) break;  // uniform over the warp
+            bool imp = false;
+            if (live && t0 + q < tot && v[q] != u && w[q] < bg_inf<V>())
+              imp = bg_try(&d[(size_t)v[q] * kBgLanes + gl], (V)(du + w[q]));
+            push(v[q], imp);
+          }
         }
       },
       rounds, visited);
@@ -320,12 +337,25 @@ __device__ __forceinline__ V bg_addmin(V x, V y, V acc) {
 // Step 3: rows of one SSSP batch (LANES sources) over the vertices of one
 // part, written into the batch's vertex-major table (slot = batch index):
 // D[s][v] = min over the part's boundary b of D_S[s][b] + L_q[b][v].
+// A thread owns 4 sources x 4 vertices (16 outputs from 8 shared loads per
+// boundary vertex); a pass covers row_pass<LANES>() vertices; the boundary
+// goes through in chunks of kRowTA.
 // OUT64: table of 64-bit fixed-point values, else uint32.
+template <int LANES>
+__host__ __device__ constexpr int row_pass() { return (kRowThreads / (LANES / 4)) * 4; }
+
+template <typename V, int LANES>
+__host__ __device__ constexpr size_t row_smem() {
+  return (size_t)kRowTA * (LANES + row_pass<LANES>()) * sizeof(V);
+}
+
 template <typename V, int LANES, bool OUT64>
 __global__ void __launch_bounds__(kRowThreads) bg_rows_kernel(BgArgs a, BgRowArgs r) {
-  constexpr int kRowTJ = row_tj<V>();
-  __shared__ V s_ds[LANES][kRowTA + 1];  // padded: lanes read different rows
-  __shared__ V s_l[kRowTA][kRowTJ];
+  constexpr int LG = LANES / 4;          // lane quads
+  constexpr int TJ = row_pass<LANES>();  // vertices per pass
+  extern __shared__ __align__(16) unsigned char row_smem_raw[];
+  V *s_ds = reinterpret_cast<V *>(row_smem_raw);  // [kRowTA][LANES]
+  V *s_l = s_ds + kRowTA * LANES;                 // [kRowTA][TJ]
   const int b = blockIdx.x;
   const BgPart q = a.parts[blockIdx.y];
   const int cnt = r.batches[b].count;
@@ -334,51 +364,57 @@ __global__ void __launch_bounds__(kRowThreads) bg_rows_kernel(BgArgs a, BgRowArg
   const V *L = static_cast<const V *>(a.L) + q.loff;
   using K = typename std::conditional<OUT64, unsigned long long, unsigned>::type;
   K *dvm = reinterpret_cast<K *>(static_cast<unsigned char *>(r.scratch) + (size_t)b * r.slot_bytes);
-  constexpr int OUTS = kRowTJ * LANES / kRowThreads;  // outputs per thread per tile
-  static_assert(OUTS >= 1 && (kRowTJ * LANES) % kRowThreads == 0, "tile shape");
-  for (int j0 = 0; j0 < q.sub; j0 += kRowTJ) {
-    V acc[OUTS];
+  const int lq = threadIdx.x % LG, vq = threadIdx.x / LG;  // this thread's lanes 4lq.., vertices 4vq..
+  for (int j0 = 0; j0 < q.sub; j0 += TJ) {
+    V acc[4][4];
 #pragma unroll
-    for (int o = 0; o < OUTS; o++) acc[o] = (V)(2 * (unsigned long long)bg_inf<V>());
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc[i][c] = (V)(2 * (unsigned long long)bg_inf<V>());
     for (int a0 = 0; a0 < q.bdy; a0 += kRowTA) {
       const int na = min(kRowTA, q.bdy - a0);
       __syncthreads();
-      for (int i = threadIdx.x; i < LANES * kRowTA; i += kRowThreads) {
-        const int l = i / kRowTA, t = i - l * kRowTA;
+      for (int i = threadIdx.x; i < kRowTA * LANES; i += kRowThreads) {
+        const int t = i / LANES, l = i - t * LANES;
         V x = bg_inf<V>();
         if (l < cnt && t < na) {
           const int s = srcs[l];  // -1 (not a boundary vertex) was flagged by step 2
           if (s >= 0 && s < a.B) x = DS[(size_t)s * a.B + q.boff + a0 + t];
         }
-        s_ds[l][t] = x;
+        s_ds[i] = x;
       }
-      for (int i = threadIdx.x; i < kRowTA * kRowTJ; i += kRowThreads) {
-        const int t = i / kRowTJ, jj = i - t * kRowTJ;
-        s_l[t][jj] = (t < na && j0 + jj < q.sub) ? L[(size_t)(a0 + t) * q.sub + j0 + jj] : bg_inf<V>();
+      for (int i = threadIdx.x; i < kRowTA * TJ; i += kRowThreads) {
+        const int t = i / TJ, jj = i - t * TJ;
+        s_l[i] = (t < na && j0 + jj < q.sub) ? L[(size_t)(a0 + t) * q.sub + j0 + jj] : bg_inf<V>();
       }
       __syncthreads();
+      for (int t = 0; t < na; t++) {
+        V x[4], y[4];
 #pragma unroll
-      for (int o = 0; o < OUTS; o++) {
-        const int idx = threadIdx.x + o * kRowThreads;
-        const int jj = idx / LANES, l = idx % LANES;
-        V x = acc[o];
-        for (int t = 0; t < na; t++) x = bg_addmin(s_ds[l][t], s_l[t][jj], x);
-        acc[o] = x;
+        for (int i = 0; i < 4; i++) x[i] = s_ds[t * LANES + lq * 4 + i];
+#pragma unroll
+        for (int c = 0; c < 4; c++) y[c] = s_l[t * TJ + vq * 4 + c];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+          for (int c = 0; c < 4; c++) acc[i][c] = bg_addmin(x[i], y[c], acc[i][c]);
       }
     }
 #pragma unroll
-    for (int o = 0; o < OUTS; o++) {
-      const int idx = threadIdx.x + o * kRowThreads;
-      const int jj = idx / LANES, l = idx % LANES;
+    for (int c = 0; c < 4; c++) {
+      const int jj = vq * 4 + c;
       if (j0 + jj >= q.sub) continue;
       const int v = r.st2ed[q.start + j0 + jj];
-      K out;
-      if constexpr (OUT64) {  // fixed point as it is (the output pass rounds it)
-        out = (l >= cnt || acc[o] >= r.fix_inf) ? (K)r.fix_inf : (K)acc[o];
-      } else {
-        out = (l >= cnt || acc[o] >= bg_inf<V>()) ? (K)bg_inf<V>() : (K)acc[o];
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int l = lq * 4 + i;
+        K out;
+        if constexpr (OUT64)  // fixed point as it is (the output pass rounds it)
+          out = (l >= cnt || acc[i][c] >= r.fix_inf) ? (K)r.fix_inf : (K)acc[i][c];
+        else
+          out = (l >= cnt || acc[i][c] >= bg_inf<V>()) ? (K)bg_inf<V>() : (K)acc[i][c];
+        dvm[(size_t)v * LANES + l] = out;
       }
-      dvm[(size_t)v * LANES + l] = out;
     }
   }
 }
@@ -396,8 +432,14 @@ template <typename V, int LANES, bool OUT64>
 cudaError_t launch_rows_t(const BgArgs &a, const BgRowArgs &r, cudaStream_t st) {
   const dim3 grid((unsigned)r.nbatches, (unsigned)a.nparts);
   ++launch_count();
-  bg_rows_kernel<V, LANES, OUT64><<<grid, kRowThreads, 0, st>>>(a, r);
+  bg_rows_kernel<V, LANES, OUT64><<<grid, kRowThreads, row_smem<V, LANES>(), st>>>(a, r);
   return cudaGetLastError();
+}
+
+template <typename V, int LANES, bool OUT64>
+cudaError_t set_rows_attr() {
+  return cudaFuncSetAttribute(bg_rows_kernel<V, LANES, OUT64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)row_smem<V, LANES>());
 }
 
 }  // namespace
@@ -408,9 +450,15 @@ size_t bg_smem_bytes(bool wide, int nodes) {
 int bg_lanes() { return kBgLanes; }
 
 cudaError_t init_bg_kernels() {
-  cudaError_t e = set_bg_attrs<uint32_t>();
-  if (e != cudaSuccess) return e;
-  return set_bg_attrs<unsigned long long>();
+  cudaError_t e;
+  if ((e = set_bg_attrs<uint32_t>()) != cudaSuccess || (e = set_bg_attrs<unsigned long long>()) != cudaSuccess ||
+      (e = set_rows_attr<unsigned long long, 16, true>()) != cudaSuccess ||
+      (e = set_rows_attr<unsigned long long, 32, true>()) != cudaSuccess ||
+      (e = set_rows_attr<uint32_t, 8, false>()) != cudaSuccess ||
+      (e = set_rows_attr<uint32_t, 16, false>()) != cudaSuccess ||
+      (e = set_rows_attr<uint32_t, 32, false>()) != cudaSuccess)
+    return e;
+  return cudaSuccess;
 }
 
 cudaError_t launch_bg_local(bool wide, const BgArgs &a, int njobs, int max_sub, cudaStream_t st) {
