@@ -139,6 +139,10 @@ struct Plan {
     // row and column r + 1 (which pivot step r + 1 updates itself), strip form
     std::vector<const MpSegment *> rest2;
     std::vector<int> rest2_nseg, rest2_strips;
+    // FP32 form: round r's remaining tiles (all but block row and column r),
+    // strip form
+    std::vector<const MpSegment *> rests;
+    std::vector<int> rests_nseg, rests_strips;
     // boundary rows in their own buffer (host results): per part {element
     // offset in the results, element offset in the buffer, elements}, copied
     // out as soon as the SSSP has written them
@@ -611,7 +615,7 @@ int build_plan(fap_engine *e, Plan &pl) {
   TableBuilder tb;
   struct GroupOffs {
     size_t batches, batches_alt, pdesc, row_begin, dec_begin, mp, bjobs, bsrc;
-    std::vector<size_t> diag, panel, rest, rest2;
+    std::vector<size_t> diag, panel, rest, rest2, rests;
   };
   std::vector<GroupOffs> goffs(groups.size());
   pl.groups.assign(groups.size(), Plan::Group{});
@@ -744,14 +748,17 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.rest_tiles.assign(maxnb, 0);
     G.rest2_nseg.assign(maxnb, 0);
     G.rest2_strips.assign(maxnb, 0);
+    G.rests_nseg.assign(maxnb, 0);
+    G.rests_strips.assign(maxnb, 0);
+    O.rests.assign(maxnb, 0);
     O.diag.assign(maxnb, 0);
     O.panel.assign(maxnb, 0);
     O.rest.assign(maxnb, 0);
     O.rest2.assign(maxnb, 0);
     for (int r = 0; r < maxnb; r++) {
       std::vector<FwDiagJob> dj;
-      std::vector<MpSegment> ps, rs, r2s;
-      int pt = 0, rt = 0, r2strips = 0;
+      std::vector<MpSegment> ps, rs, r2s, rss;
+      int pt = 0, rt = 0, r2strips = 0, rsstrips = 0;
       for (const PartDesc &d : pdesc) {
         int nb = d.ld / B;
         if (r >= nb) continue;
@@ -768,7 +775,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         {  // 64^3 block products: pivot step (lookahead update, closure, panels); tile form (all blocks)
           const unsigned long long blk = (unsigned long long)B * B * B;
           pl.fw_pivot_work += blk * ((r > 0 ? 2ull * (nb - 2) + 1 : 0ull) + 1ull + 2ull * (nb - 1));
-          pl.fw_tile_work += blk * (unsigned long long)nb * nb;
+          pl.fw_tile_work += blk * (e->f32() ? 2ull * nb - 1 : (unsigned long long)nb * nb);
         }
         if (nb > 1) {
           MpSegment rp, cp, rest;
@@ -790,6 +797,13 @@ int build_plan(fap_engine *e, Plan &pl) {
             r2strips += s2;
             r2s.push_back(rest2);
           }
+          MpSegment rests = rest;
+          const int s3 = fw_strips_of(rest, rest.tiles_x);
+          if (s3 > 0) {
+            rests.strip_begin = rsstrips;
+            rsstrips += s3;
+            rss.push_back(rests);
+          }
         }
       }
       G.diag_cnt[r] = (int)dj.size();
@@ -803,6 +817,9 @@ int build_plan(fap_engine *e, Plan &pl) {
       G.rest2_nseg[r] = (int)r2s.size();
       G.rest2_strips[r] = r2strips;
       O.rest2[r] = tb.add(r2s.data(), r2s.size());
+      G.rests_nseg[r] = (int)rss.size();
+      G.rests_strips[r] = rsstrips;
+      O.rests[r] = tb.add(rss.data(), rss.size());
     }
   }
   int st = pl.tables.ensure(std::max<size_t>(tb.bytes.size(), 64));
@@ -827,11 +844,13 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.panel.resize(R);
     G.rest.resize(R);
     G.rest2.resize(R);
+    G.rests.resize(R);
     for (size_t r = 0; r < R; r++) {
       G.diag[r] = reinterpret_cast<const FwDiagJob *>(base + O.diag[r]);
       G.panel[r] = reinterpret_cast<const MpSegment *>(base + O.panel[r]);
       G.rest[r] = reinterpret_cast<const MpSegment *>(base + O.rest[r]);
       G.rest2[r] = reinterpret_cast<const MpSegment *>(base + O.rest2[r]);
+      G.rests[r] = reinterpret_cast<const MpSegment *>(base + O.rests[r]);
     }
   }
   return FAP_OK;
@@ -980,7 +999,10 @@ struct Issuer {
       } else {
         FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
         FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
-        FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
+        if (f32)  // FP32: remaining tiles in the strip form
+          FAP_CUDA(fapk::launch_fw_strips(pred, G.rests[r], G.rests_nseg[r], G.rests_strips[r], st, true));
+        else
+          FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
       }
     }
     if (packed && rounds > 0) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (rounds - 1) % 2], 0));  // join
@@ -2067,12 +2089,13 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
   TableBuilder tb;
-  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb);
-  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), nr2(maxnb), sr2(maxnb);
+  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb), ors(maxnb);
+  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), nr2(maxnb), sr2(maxnb), nrs(maxnb),
+      srs(maxnb);
   for (int r = 0; r < maxnb; r++) {
     std::vector<FwDiagJob> dj;
-    std::vector<MpSegment> ps, rs, r2s;
-    int pt = 0, rt = 0, r2strips = 0;
+    std::vector<MpSegment> ps, rs, r2s, rss;
+    int pt = 0, rt = 0, r2strips = 0, rsstrips = 0;
     for (int32_t b = 0; b < count; b++) {
       int nb = (sizes[b] + Bk - 1) / Bk;
       if (r >= nb) continue;
@@ -2105,11 +2128,21 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
           r2strips += s2;
           r2s.push_back(rest2);
         }
+        MpSegment rests = rest;  // FP32: all remaining tiles, strip form
+        const int s3 = fw_strips_of(rest, rest.tiles_x);
+        if (s3 > 0) {
+          rests.strip_begin = rsstrips;
+          rsstrips += s3;
+          rss.push_back(rests);
+        }
       }
     }
     nr2[r] = (int)r2s.size();
     sr2[r] = r2strips;
     or2[r] = tb.add(r2s.data(), r2s.size());
+    nrs[r] = (int)rss.size();
+    srs[r] = rsstrips;
+    ors[r] = tb.add(rss.data(), rss.size());
     nd[r] = (int)dj.size();
     od[r] = tb.add(dj.data(), dj.size());
     np[r] = (int)ps.size();
@@ -2156,8 +2189,12 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
     } else {
       FAP_CUDA(fapk::launch_fw_diag(f32, pred, djobs, nd[r], st));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], packed, st));
-      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]),
-                                          nr[r], tr[r], packed, st));
+      if (f32)
+        FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ors[r]), nrs[r],
+                                        srs[r], st, true));
+      else
+        FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]),
+                                            nr[r], tr[r], packed, st));
     }
   }
   if (packed) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (maxnb - 1) % 2], 0));  // join

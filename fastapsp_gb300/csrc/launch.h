@@ -32,11 +32,11 @@ cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, 
                                   int max_k, cudaStream_t st, bool f32 = false, int tile_cols = 0);
 int minplus_strip_class_cols(int c);
 int minplus_strip_tiles();
-// Strip form of the FW remaining-tile phase (packed int32, init_from_c = 1,
-// K <= 64): CTAs numbered by MpSegment::strip_begin, tiles_y x
-// ceil(tiles_x / fw_strip_tiles()) strips per segment.
+// Strip form of the FW remaining-tile phase (packed int32, or FP32 with
+// f32; init_from_c = 1, K <= 64): CTAs numbered by MpSegment::strip_begin,
+// tiles_y x ceil(tiles_x / fw_strip_tiles()) strips per segment.
 cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                             cudaStream_t st);
+                             cudaStream_t st, bool f32 = false);
 int fw_strip_tiles();
 int minplus_strip_max_k();   // largest K of the strip form
 // Segments go to the strip form in classes of K (one launch per class, each

@@ -1120,9 +1120,17 @@ __device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, in
 // executed (steps run x the tile's 128 x TN outputs), summed per CTA.
 __device__ unsigned long long g_fw_counters[1];
 
-template <bool PRED, int TN>
+// F32: FP32 distances (value bits, "unreached" = the bits of 1e8): the
+// product keeps each output's value bits and the step (k + 1) of its last
+// strict improvement in two registers (the active steps, in order); the
+// epilogue stores the product where it is strictly below the current value,
+// with the predecessor of that step -- the same result as updating the
+// current value step by step.  TN = 64.  (Two steps per pass, as in the
+// strip min-plus, measured the same here and spills more.)
+template <bool PRED, int TN, bool F32 = false>
 __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     mp_fwstrip_kernel(const MpSegment *__restrict__ segs, int nseg) {
+  static_assert(!F32 || TN == 64, "the FP32 form uses 64-column tiles");
   constexpr int CH = TN / 64;   // 64-column blocks of a tile
   constexpr int TPR = TN / 4;   // threads per row in the row-wise copies
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1152,7 +1160,8 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     return make_int2(b0 >= 0 ? b0 * kBlk : -1, b1 >= 0 ? b1 * kBlk : -1);
   };
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-  const unsigned INF = Dist<uint32_t>::inf();
+  const unsigned INF = F32 ? __float_as_uint(Dist<float>::inf()) : Dist<uint32_t>::inf();
+  const unsigned FIN = F32 ? INF : kPackH;  // entries below are finite
   const int kseg = (s.K + 3) & ~3;
   const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
   const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
@@ -1190,9 +1199,9 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     if (jt == jt0)  // A keys; a warp converts 32 entries of one step k and marks finite ones
       for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads) {
         const unsigned v = (&sm.A[0][0])[idx];
-        (&sm.A[0][0])[idx] = min(v, kPackH) << kIdxBits;
+        if (!F32) (&sm.A[0][0])[idx] = min(v, kPackH) << kIdxBits;
         const int kk = idx >> 7;
-        if (__any_sync(0xffffffffu, v < kPackH) && (threadIdx.x & 31) == 0)
+        if (__any_sync(0xffffffffu, v < FIN) && (threadIdx.x & 31) == 0)
           atomicOr(&s_amask[kk >> 5], 1u << (kk & 31));
       }
     {  // B keys; TPR lanes convert a whole row and its first lane marks it when finite
@@ -1202,12 +1211,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
         uint4 *p = reinterpret_cast<uint4 *>(&sm.B[buf][kk][j]);
         const unsigned idx = (unsigned)kk + 1u;
         uint4 v = *p;
-        const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < kPackH;
-        v.x = (min(v.x, kPackH) << kIdxBits) | idx;
-        v.y = (min(v.y, kPackH) << kIdxBits) | idx;
-        v.z = (min(v.z, kPackH) << kIdxBits) | idx;
-        v.w = (min(v.w, kPackH) << kIdxBits) | idx;
-        *p = v;
+        const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < FIN;
+        if (!F32) {
+          v.x = (min(v.x, kPackH) << kIdxBits) | idx;
+          v.y = (min(v.y, kPackH) << kIdxBits) | idx;
+          v.z = (min(v.z, kPackH) << kIdxBits) | idx;
+          v.w = (min(v.w, kPackH) << kIdxBits) | idx;
+          *p = v;
+        }
         const unsigned bal = __ballot_sync(0xffffffffu, fin);  // every lane runs the same trips
         const unsigned grp = TPR == 32 ? 0xffffffffu : ((1u << (TPR & 31)) - 1u);
         if (lane % TPR == 0 && ((bal >> lane) & grp) != 0u)
@@ -1244,10 +1255,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     }
 
     unsigned acc[8][4 * CH];
+    int arg[8][4 * CH];  // F32: step (k + 1) of the last strict improvement, 0: none
 #pragma unroll
     for (int r = 0; r < 8; r++)
 #pragma unroll
-      for (int c = 0; c < 4 * CH; c++) acc[r][c] = kPackH << kIdxBits;
+      for (int c = 0; c < 4 * CH; c++) {
+        acc[r][c] = F32 ? INF : kPackH << kIdxBits;
+        arg[r][c] = 0;
+      }
     // Only steps k whose B row (pivot row k over this tile's columns) and A
     // column (over this strip's rows) have a finite entry can improve an
     // output: all k (unrolled) when every row
@@ -1260,7 +1275,21 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
                                ((unsigned long long)(s_kmask[buf][1] & s_amask[1]) << 32);
       if (kseg < 64) msk &= (1ull << kseg) - 1ull;
       n_work += (unsigned long long)(__popcll(msk) == s.K ? kseg : __popcll(msk)) * kTile * TN;
-      if (__popcll(msk) == s.K && s.K > 0) {
+      if (F32 && msk) {
+        while (msk) {
+          const int kk = __ffsll(msk) - 1;
+          msk &= msk - 1ull;
+          const uint4 na0 = *reinterpret_cast<const uint4 *>(acol + kk * kTile);
+          const uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kk * kTile + kBlk);
+          const uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * TN);
+          const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
+          const unsigned b[4] = {nb0.x, nb0.y, nb0.z, nb0.w};
+#pragma unroll
+          for (int r = 0; r < 8; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) strip_addmin<true>(acc[r][c], arg[r][c], a[r], b[c], kk + 1);
+        }
+      } else if (__popcll(msk) == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
         uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
         uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
@@ -1323,11 +1352,17 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
         for (int q = 0; q < 4; q++) {
           const int col = cbh + tx * 4 + q;
           const unsigned cq = q == 0 ? cv.x : q == 1 ? cv.y : q == 2 ? cv.z : cv.w;
-          const unsigned key = min(min(cq, kPackH) << kIdxBits, acc[r][h * 4 + q]);
-          const unsigned idx = key & kIdxMask;
-          if (idx == 0 || col >= n_cols) continue;
-          c_mat[(int64_t)row * ldc + col] = key >> kIdxBits;
-          if (PRED) p_mat[(int64_t)row * ldcp + col] = sm.Bp[idx - 1][sc0 + q];
+          if constexpr (F32) {  // strict improvements only: ties keep the current value
+            if (!(acc[r][h * 4 + q] < cq) || col >= n_cols) continue;
+            c_mat[(int64_t)row * ldc + col] = acc[r][h * 4 + q];
+            if (PRED) p_mat[(int64_t)row * ldcp + col] = sm.Bp[arg[r][h * 4 + q] - 1][sc0 + q];
+          } else {
+            const unsigned key = min(min(cq, kPackH) << kIdxBits, acc[r][h * 4 + q]);
+            const unsigned idx = key & kIdxMask;
+            if (idx == 0 || col >= n_cols) continue;
+            c_mat[(int64_t)row * ldc + col] = key >> kIdxBits;
+            if (PRED) p_mat[(int64_t)row * ldcp + col] = sm.Bp[idx - 1][sc0 + q];
+          }
         }
       }
     }
@@ -1799,11 +1834,11 @@ cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks
   return cudaGetLastError();
 }
 
-template <bool PRED>
+template <bool PRED, bool F32>
 cudaError_t launch_fwstrip_t(const MpSegment *d_segs, int nseg, int strips, cudaStream_t st) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
   ++launch_count();
-  mp_fwstrip_kernel<PRED, kFwStripTN>
+  mp_fwstrip_kernel<PRED, kFwStripTN, F32>
       <<<strips, kThreads, sizeof(FwStripSmem<kFwStripTN>), st>>>(d_segs, nseg);
   return cudaGetLastError();
 }
@@ -1852,9 +1887,12 @@ cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, 
 int minplus_strip_tiles() { return kStripTiles; }
 
 cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                             cudaStream_t st) {
-  return pred ? launch_fwstrip_t<true>(d_segs, nseg, strips, st)
-              : launch_fwstrip_t<false>(d_segs, nseg, strips, st);
+                             cudaStream_t st, bool f32) {
+  if (f32)
+    return pred ? launch_fwstrip_t<true, true>(d_segs, nseg, strips, st)
+                : launch_fwstrip_t<false, true>(d_segs, nseg, strips, st);
+  return pred ? launch_fwstrip_t<true, false>(d_segs, nseg, strips, st)
+              : launch_fwstrip_t<false, false>(d_segs, nseg, strips, st);
 }
 int fw_strip_tiles() { return kFwStripTiles; }
 int minplus_strip_max_k() { return kStripMaxK; }
@@ -1945,13 +1983,17 @@ cudaError_t init_minplus_kernels() {
   if ((e = cudaFuncSetAttribute(fw_pivot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(PivotSmem))) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(mp_fwstrip_kernel<true, kFwStripTN>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sizeof(FwStripSmem<kFwStripTN>))) != cudaSuccess)
+#define FAP_FWSTRIP_ATTR(P, F)                                                           \
+  if ((e = cudaFuncSetAttribute(mp_fwstrip_kernel<P, kFwStripTN, F>,                     \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,             \
+                                (int)sizeof(FwStripSmem<kFwStripTN>))) != cudaSuccess)   \
     return e;
-  return cudaFuncSetAttribute(mp_fwstrip_kernel<false, kFwStripTN>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sizeof(FwStripSmem<kFwStripTN>));
+  FAP_FWSTRIP_ATTR(true, false)
+  FAP_FWSTRIP_ATTR(false, false)
+  FAP_FWSTRIP_ATTR(true, true)
+  FAP_FWSTRIP_ATTR(false, true)
+#undef FAP_FWSTRIP_ATTR
+  return cudaSuccess;
 }
 
 int minplus_tile_rows() { return kTile; }
