@@ -263,7 +263,8 @@ def run_solve(args, name, rank, world, local_rank):
     torch.cuda.synchronize()
     # the first solve tuned the SSSP; later engines on the same graph (the
     # e2e loop) take the tuned values instead of tuning again
-    tuned = {o: eng.get_option(o) for o in (fap._lib.OPT_SSSP_DELTA, fap._lib.OPT_SSSP_LANES)}
+    tuned = {o: eng.get_option(o) for o in (fap._lib.OPT_SSSP_METHOD, fap._lib.OPT_SSSP_DELTA,
+                                             fap._lib.OPT_SSSP_LANES)}
     step_ms, phase = [], []
     if world > 1:
         torch.distributed.barrier()
@@ -390,7 +391,9 @@ def run_solve(args, name, rank, world, local_rank):
         "mode": "batched (one launch per phase, CUDA graph)",
         "arithmetic": ("SSSP exact (FP64 option), rounded once to FP32; FW and min-plus in FP32" if f32 and
                        wl["fp64_sssp"] else "f32 (the reference's)" if f32 else "int32 (exact)"),
-        "tuning": {"sssp_delta": tuned[fap._lib.OPT_SSSP_DELTA],
+        "tuning": {"sssp_method": {1: "whole-graph search", 2: "boundary graph"}.get(
+                       int(tuned[fap._lib.OPT_SSSP_METHOD]), "not tuned"),
+                   "sssp_delta": tuned[fap._lib.OPT_SSSP_DELTA],
                    "sssp_lanes": int(tuned[fap._lib.OPT_SSSP_LANES])},
         "e2e": {"value": (world if share is None else 1) * float(n) * n / (e2e_ms_step / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

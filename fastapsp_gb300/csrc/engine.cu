@@ -170,6 +170,7 @@ struct Plan {
   int sssp_lanes = 32;  // sources per SSSP batch
   int sssp_lanes_alt = 0;  // the other width the autotuner tries (0: none)
   int bsssp = 0;        // boundary SSSP through the boundary graph (bgraph.cu) instead of the search
+  bool method_trial = false;  // first run times both SSSP methods (automatic choice)
   // FW add-mins of one run outside the remaining-tile strips: the pivot
   // steps' 64^3 block products (packed form), or every block (tile form)
   unsigned long long fw_pivot_work = 0, fw_tile_work = 0;
@@ -218,7 +219,8 @@ struct fap_engine {
   int tile_cols = 0;       // min-plus strip tile columns: 64, 128, 0 = per class
   int host_results = 0;    // FAP_OPT_HOST_RESULTS: 0 staged when the device has room, 1 direct
   int int32_form = 0;      // FAP_OPT_INT32_FORM: 0 packed keys when provably exact, 1 always wide
-  int sssp_method = 0;     // FAP_OPT_SSSP_METHOD: 0 boundary graph where exact and it fits, 1 search
+  int sssp_method = 0;     // FAP_OPT_SSSP_METHOD: 0 auto, 1 whole-graph search, 2 boundary graph where exact
+  int sssp_method_tuned = 0;  // auto: what the first run's trial chose (1 search, 2 boundary graph)
   int fix_shift = -1;      // FP32 graphs: every weight is a multiple of 2^-fix_shift and every path
                            // length below 2^52 of those units (-1: no such shift)
   // boundary graph (bgraph.cu), built for the current partition on first use
@@ -1166,6 +1168,54 @@ int autotune_sssp(fap_engine *e, Plan &pl, cudaStream_t st) {
   return FAP_OK;
 }
 
+// Automatic SSSP method: on the first run of a plan that can use the
+// boundary graph, times the plan's SSSP phase (every group) through the
+// boundary graph (a warm-up run, then the better of two) and as the
+// whole-graph search at the current near-far step (once: it only has to lose
+// clearly or win), keeps the faster for this plan and the engine's later
+// plans, and reports it through fap_get_option.  Both methods give the same
+// rows, so the trial runs rewrite the same boundary rows.
+int trial_sssp_method(fap_engine *e, Plan &pl, cudaStream_t st) {
+  cudaEvent_t a, b;
+  FAP_CUDA(cudaEventCreate(&a));
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return set_error(FAP_ERR_CUDA, "method trial: event failed");
+  }
+  auto time_phase = [&](float &ms) {
+    Issuer is{e, pl, st, false};
+    if (cudaEventRecord(a, st) != cudaSuccess) return set_error(FAP_ERR_CUDA, "method trial: event failed");
+    for (size_t g = 0; g < pl.groups.size(); g++) {
+      int r = is.sssp(g);
+      if (r != FAP_OK) return r;
+    }
+    if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+      return set_error(FAP_ERR_CUDA, "method trial: event failed");
+    return FAP_OK;
+  };
+  int rc = FAP_OK;
+  float tb = 1e30f, ts = 1e30f;
+  pl.bsssp = 1;
+  for (int rep = 0; rep < 3 && rc == FAP_OK; rep++) {
+    float ms = 0;
+    if ((rc = time_phase(ms)) == FAP_OK && rep > 0) tb = std::min(tb, ms);
+  }
+  if (rc == FAP_OK) {
+    pl.bsssp = 0;
+    rc = time_phase(ts);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  pl.bsssp = ts < tb ? 0 : 1;
+  pl.method_trial = false;
+  if (rc != FAP_OK) return rc;
+  if ((rc = check_status(e)) != FAP_OK) return rc;
+  e->sssp_method_tuned = pl.bsssp ? 2 : 1;
+  pl.sig = buffer_signature(e);
+  return FAP_OK;
+}
+
 // Tile autotuner of the packed min-plus (strip form): on a plan's first run,
 // once the product's inputs are in place (closed FW matrices, boundary
 // rows), times every strip class launch of every group with 128 x 64 and
@@ -1316,14 +1366,17 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   // (int32 graphs; FP32 graphs with the FP64 option and a fixed-point
   // shift), its shared-memory tables fit and every batch of a group gets a
   // table slot of its own; otherwise the whole-graph search.
-  bool bs = false;
-  if (e->sssp_method == 0 && (!e->f32() || acc64)) {
+  bool bs = false, trial = false;
+  if (e->sssp_method != 1 && e->sssp_method_tuned != 1 && (!e->f32() || acc64)) {
     if ((rc = prepare_bgraph(e)) != FAP_OK) return rc;
     if (e->bg_ok) {
       int64_t nb = 0;
       for (int p : parts) nb += (e->bdy_num[p] + lanes - 1) / lanes;
       bs = nb <= max_sssp_slots(e, acc64 && lanes == 32);
     }
+    // automatic: the first run times both methods (the search wins where few
+    // vertices are reachable from the boundary, as on sparse directed graphs)
+    trial = bs && e->sssp_method == 0 && e->sssp_method_tuned == 0 && e->autotune;
   }
   // The SSSP autotuner also tries a second batch width (8 -> 16, 16 -> 32,
   // 32 -> 16; not for the FP64 search, whose 32-source slots have another
@@ -1357,11 +1410,13 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     np->sssp_lanes = lanes;
     np->sssp_lanes_alt = tune_lanes ? alt_lanes : 0;
     np->bsssp = bs ? 1 : 0;
+    np->method_trial = trial;
     if ((rc = build_plan(e, *np)) != FAP_OK) return rc;
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
   }
   if (pl->pack < 0) {
+    if (pl->method_trial && (rc = trial_sssp_method(e, *pl, st)) != FAP_OK) return rc;
     if (e->autotune && e->sssp_delta <= 0 && !pl->bsssp && (rc = autotune_sssp(e, *pl, st)) != FAP_OK)
       return rc;
     if ((rc = first_run(e, *pl, st)) != FAP_OK) return rc;
@@ -2335,8 +2390,10 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
       e->tile_cols = (int)value;
       return FAP_OK;
     case FAP_OPT_SSSP_METHOD:
-      if (value != 0.0 && value != 1.0) return set_error(FAP_ERR_INVALID, "SSSP method must be 0 or 1");
+      if (value != 0.0 && value != 1.0 && value != 2.0)
+        return set_error(FAP_ERR_INVALID, "SSSP method must be 0, 1 or 2");
       e->sssp_method = (int)value;
+      e->sssp_method_tuned = 0;
       return FAP_OK;
     case FAP_OPT_HOST_RESULTS:
       if (value != 0.0 && value != 1.0) return set_error(FAP_ERR_INVALID, "host results must be 0 or 1");
@@ -2359,7 +2416,7 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_AUTOTUNE: *value = e->autotune; return FAP_OK;
     case FAP_OPT_SSSP_LANES: *value = e->sssp_lanes ? e->sssp_lanes : e->sssp_lanes_tuned; return FAP_OK;
     case FAP_OPT_TILE_COLS: *value = e->tile_cols; return FAP_OK;
-    case FAP_OPT_SSSP_METHOD: *value = e->sssp_method; return FAP_OK;
+    case FAP_OPT_SSSP_METHOD: *value = e->sssp_method ? e->sssp_method : e->sssp_method_tuned; return FAP_OK;
     case FAP_OPT_HOST_RESULTS: *value = e->host_results; return FAP_OK;
     case FAP_OPT_INT32_FORM: *value = e->int32_form; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");

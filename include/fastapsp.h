@@ -208,23 +208,27 @@ int fap_precondition(fap_engine *e);
  *                      run times both widths and keeps the faster (not for
  *                      results in mapped host memory); otherwise 64 for
  *                      K <= 48 and 128 above.  Changes speed only.
- *   FAP_OPT_SSSP_METHOD how the boundary SSSP rows of a solve are made:
- *                      0 (default) = through the boundary graph where its
+ *   FAP_OPT_SSSP_METHOD how the boundary SSSP rows of a solve are made.
+ *                      The boundary-graph method (local rows of every part
+ *                      from its boundary vertices, shortest paths between
+ *                      all boundary vertices over the cut edges and those
+ *                      rows, then a min-plus per part) applies where its
  *                      arithmetic is exact -- int32 engines, and FP32
  *                      engines with FAP_OPT_SSSP_FP64 whose weights are
  *                      multiples of one power of two 2^-s with
  *                      (n-1) * max weight < 2^(52-s) (64-bit fixed point) --
  *                      and its tables fit in shared memory (up to about
- *                      3,200 boundary vertices for FP32, 5,800 for int32):
- *                      local rows of every part from its boundary vertices,
- *                      shortest paths between all boundary vertices over
- *                      the cut edges and those rows, then a min-plus per
- *                      part; otherwise the whole-graph search.  1 = always
- *                      the whole-graph search.  Both give the same
- *                      distances (int32: identical; FP32: the exactly
- *                      rounded distance, which equals the FP64 search's
- *                      whenever its sums are exact) and the same
- *                      predecessor rule.
+ *                      3,200 boundary vertices for FP32, 5,800 for int32);
+ *                      elsewhere the whole-graph search runs.  0 (default)
+ *                      = automatic: while FAP_OPT_AUTOTUNE is on, the first
+ *                      run of a plan where the boundary graph applies times
+ *                      both methods and keeps the faster (fap_get_option
+ *                      then reports 1 or 2); 1 = always the whole-graph
+ *                      search; 2 = the boundary graph wherever it applies.
+ *                      Both give the same distances (int32: identical;
+ *                      FP32: the exactly rounded distance, which equals the
+ *                      FP64 search's whenever its sums are exact) and the
+ *                      same predecessor rule.
  *   FAP_OPT_HOST_RESULTS results in page-locked host memory: 0 (default) =
  *                      solved into a device copy that the copy engines then
  *                      move to the host rows, when the device has room for

@@ -1,4 +1,4 @@
-"""The boundary SSSP through the boundary graph (FAP_OPT_SSSP_METHOD = 0,
+"""The boundary SSSP through the boundary graph (FAP_OPT_SSSP_METHOD = 2,
 csrc/bgraph.cu) against the whole-graph search (FAP_OPT_SSSP_METHOD = 1),
 whose rows equal the reference's Dijkstra (fap/kernel/batch_sssp.h:79-114)
 bit for bit: whole solves must agree bit for bit -- distances and
@@ -6,7 +6,8 @@ predecessors -- on int32 graphs and on FP32 graphs with the FP64 option whose
 weights fit the fixed point (there the FP64 search's sums are exact too).
 Graphs cover directed and undirected inputs, parallel edges and self loops,
 one part, parts without boundary vertices and many small parts; both solve
-forms and single-part solves."""
+forms and single-part solves; the automatic choice (0) picks one of them on
+the first run and reports it."""
 import numpy as np
 import pytest
 import torch
@@ -71,14 +72,16 @@ def test_boundary_graph_equals_whole_graph_search(gpu, name, mode):
         gid, _ = gpu.partition(g.row_offset, g.col_val, K)
     dtype = gpu.DTYPE_I32 if is_int else gpu.DTYPE_F32
     fp64 = 0 if is_int else 1
-    d0, p0, st0, parts0 = _solve(gpu, g, K, gid, dtype, 0, mode, fp64)
+    d0, p0, st0, parts0 = _solve(gpu, g, K, gid, dtype, 2, mode, fp64)
     d1, p1, st1, parts1 = _solve(gpu, g, K, gid, dtype, 1, mode, fp64)
+    da, pa, _, _ = _solve(gpu, g, K, gid, dtype, 0, mode, fp64)
     # the boundary graph ran (no search batches) unless the graph has no boundary
     assert st1["batches"] > 0 or st1["steps"] == 0
     if K > 1:
         assert st0["batches"] == 0, st0
     assert torch.equal(d0, d1), "distances differ between the two SSSP methods"
     assert torch.equal(p0, p1), "predecessors differ between the two SSSP methods"
+    assert torch.equal(da, d1) and torch.equal(pa, p1), "the automatic choice differs"
     for (a, b), (c, e) in zip(parts0, parts1):
         assert torch.equal(a, c) and torch.equal(b, e), "single-part solves differ"
 
@@ -90,18 +93,21 @@ def test_fp32_without_fixed_point_falls_back_to_the_search(gpu):
     rng = np.random.default_rng(3)
     g.weight[:] = (10.0 ** rng.uniform(-7, 7, size=g.m)).astype(np.float32)
     gid, _ = gpu.partition(g.row_offset, g.col_val, 6)
-    d0, p0, st0, _ = _solve(gpu, g, 6, gid, gpu.DTYPE_F32, 0, 1, fp64=1)
+    d0, p0, st0, _ = _solve(gpu, g, 6, gid, gpu.DTYPE_F32, 2, 1, fp64=1)
     d1, p1, st1, _ = _solve(gpu, g, 6, gid, gpu.DTYPE_F32, 1, 1, fp64=1)
     assert st0["batches"] > 0  # the search ran
     assert torch.equal(d0, d1) and torch.equal(p0, p1)
 
 
 def test_sssp_method_option_values(gpu):
-    g = graphs.grid_graph(8, 8, seed=1)
-    with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 2, dtype=gpu.DTYPE_I32) as eng:
-        assert eng.get_option(gpu._lib.OPT_SSSP_METHOD) == 0
+    g = graphs.grid_graph(32, 32, seed=1)
+    with gpu.Engine(g.n, g.row_offset, g.col_val, g.weight, 4, dtype=gpu.DTYPE_I32) as eng:
+        assert eng.get_option(gpu._lib.OPT_SSSP_METHOD) == 0  # automatic, not tuned yet
+        d = torch.empty((g.n, g.n), dtype=torch.int32, device="cuda")
+        eng.solve(d, None)
+        assert eng.get_option(gpu._lib.OPT_SSSP_METHOD) in (1, 2)  # the trial's choice
         eng.set_option(gpu._lib.OPT_SSSP_METHOD, 1)
         assert eng.get_option(gpu._lib.OPT_SSSP_METHOD) == 1
         with pytest.raises(gpu._lib.FapError):
-            eng.set_option(gpu._lib.OPT_SSSP_METHOD, 2)
+            eng.set_option(gpu._lib.OPT_SSSP_METHOD, 3)
         assert eng.get_option(gpu._lib.OPT_SSSP_METHOD) == 1
