@@ -653,6 +653,39 @@ def run_c5(args):
             "pairs": npairs, "dtype": "f32"}
 
 
+def run_profile(args):
+    """Device-resident solves only, for ncu: the workload graph (or, with
+    --profile-n, a road-like graph of that size in parts of about 900
+    vertices, partitioned by the engine) solved --profile-solves times; prints
+    the launches of the first solve (tuning included) and of each later one,
+    so that a capture can skip to one whole solve."""
+    import torch
+
+    import fastapsp_gb300 as fap
+
+    wl = WORKLOADS[args.config]
+    if args.profile_n:
+        g = load_graphs_module().road_like(args.profile_n)
+        K = max(2, round(args.profile_n / 895))
+        gid, _ = fap.partition(g.row_offset, g.col_val, K)
+    else:
+        g, K, gid, _ = load_workload(args.config)
+    f32 = wl["dtype"] == "f32" or bool(args.profile_n)
+    eng = fap.Engine(g.n, g.row_offset, g.col_val, g.weight, K, graph_id=gid,
+                     dtype=fap.DTYPE_F32 if f32 else fap.DTYPE_I32)
+    if f32:
+        eng.set_option(fap._lib.OPT_SSSP_FP64, 1)
+    d = torch.empty((g.n, g.n), dtype=torch.float32 if f32 else torch.int32, device="cuda")
+    p = torch.empty((g.n, g.n), dtype=torch.int32, device="cuda")
+    counts = []
+    for _ in range(args.profile_solves):
+        eng.solve(d, p)
+        torch.cuda.synchronize()
+        counts.append(eng.last_launches())
+    print(json.dumps({"profile": args.config, "n": g.n, "K": K, "launches_per_solve": counts,
+                      "phase_ms": eng.last_times()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -668,6 +701,10 @@ def main():
     ap.add_argument("--shard", choices=["parts", "replicas"], default="parts",
                     help="under torchrun: share the graph's parts out over the ranks (default) or solve "
                          "the whole graph on every rank")
+    ap.add_argument("--profile", action="store_true",
+                    help="only device-resident solves of the workload (for ncu); see run_profile")
+    ap.add_argument("--profile-n", type=int, default=0, help="--profile on a road-like graph of this size")
+    ap.add_argument("--profile-solves", type=int, default=4)
     ap.add_argument("--no-c3", dest="with_c3", action="store_false",
                     help="leave out the dense batched FW of 512 instances from the solve line")
     ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c4",
@@ -686,6 +723,12 @@ def main():
             return
         if rank == 0:
             print(json.dumps(run_reference(args)))
+        return
+    if args.profile and args.config in WORKLOADS:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        run_profile(args)
         return
     if args.config not in WORKLOADS:
         import torch

@@ -1415,13 +1415,15 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     e->plans.push_back(std::move(np));
     pl = e->plans.back().get();
   }
-  if (pl->pack < 0) {
+  if (pl->pack < 0) {  // first run: trials and tuners, then the plan without a graph
+    const int c0 = fapk::launch_count();
     if (pl->method_trial && (rc = trial_sssp_method(e, *pl, st)) != FAP_OK) return rc;
     if (e->autotune && e->sssp_delta <= 0 && !pl->bsssp && (rc = autotune_sssp(e, *pl, st)) != FAP_OK)
       return rc;
     if ((rc = first_run(e, *pl, st)) != FAP_OK) return rc;
     e->fw_host_work += pl->pack == 1 ? pl->fw_pivot_work : pl->fw_tile_work;
-    if (e->autotune && e->tile_cols == 0) return autotune_tiles(e, *pl, st);
+    if (e->autotune && e->tile_cols == 0 && (rc = autotune_tiles(e, *pl, st)) != FAP_OK) return rc;
+    e->last_launches = fapk::launch_count() - c0;  // every kernel of this call, trials included
     return FAP_OK;
   }
   if (mode == FAP_MODE_BATCHED) {
