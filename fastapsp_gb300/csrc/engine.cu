@@ -159,6 +159,7 @@ struct Plan {
     int mp_cls_first[kMaxCls] = {}, mp_cls_nseg[kMaxCls] = {};
     int mp_cls_strips[kMaxCls] = {}, mp_cls_max_k[kMaxCls] = {};
     int mp_cls_cols[kMaxCls] = {};  // tile columns the tuner chose (0: the class default)
+    bool mp_aligned = true;  // every strip segment's result rows start on 16-byte boundaries
     int max_sub = 0;  // largest part of the group (bound of the packed form)
     int64_t out_lo = 0, out_elems = 0;  // the group's result rows: elements [out_lo, out_lo + out_elems)
   };
@@ -552,6 +553,13 @@ MpSegment mp_segment(const void *A, int64_t lda, const void *B, int64_t ldb, con
   return s;
 }
 
+// Whether a min-plus segment's result rows (and predecessor rows) all start
+// on 16-byte boundaries.
+bool rows_aligned16(const MpSegment &s) {
+  const bool c = (s.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(s.C) & 15) == 0;
+  return c && (s.Cp == nullptr || ((s.ldcp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Cp) & 15) == 0));
+}
+
 // CTAs of a segment in the tile form of the min-plus (no skipped blocks).
 int mp_tiles_of(const MpSegment &s) {
   const int T = fapk::minplus_tile_rows();
@@ -728,6 +736,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         s.strip_begin = G.mp_cls_strips[c];
         G.mp_cls_strips[c] += mp_strips_of(s);
         G.mp_cls_max_k[c] = std::max(G.mp_cls_max_k[c], s.K);
+        G.mp_aligned = G.mp_aligned && rows_aligned16(s);
       }
       mps.insert(mps.end(), mps_cls[c].begin(), mps_cls[c].end());
     }
@@ -1035,7 +1044,7 @@ struct Issuer {
         FAP_CUDA(fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
                                              G.mp_cls_strips[c], G.mp_cls_max_k[c],
                                              fork && c > 0 ? e->side : st, f32,
-                                             e->tile_cols ? e->tile_cols : G.mp_cls_cols[c]));
+                                             e->tile_cols ? e->tile_cols : G.mp_cls_cols[c], G.mp_aligned));
       FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.mp, G.mp_nseg, G.mp_tiles - G.mp_strip_tiles,
                                           packed, st, G.mp_strip_tiles));
       if (fork) {  // join
@@ -1246,7 +1255,8 @@ int autotune_tiles(fap_engine *e, Plan &pl, cudaStream_t st) {
           cudaError_t ce = cudaEventRecord(a, st);
           if (ce == cudaSuccess)
             ce = fapk::launch_minplus_strips(pred, G.mp + G.mp_cls_first[c], G.mp_cls_nseg[c],
-                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st, false, cols);
+                                             G.mp_cls_strips[c], G.mp_cls_max_k[c], st, false, cols,
+                                             G.mp_aligned);
           if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
           if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
           float ms = 0;
@@ -2116,7 +2126,7 @@ int fap_minplus(fap_engine *e, int32_t dtype, int32_t M, int32_t N, int32_t K, c
   if ((packed || (!i32 && K > 0)) && K <= fapk::minplus_strip_max_k() && ldc < (1 << 24) &&
       (!Cpath || ldcp < (1 << 24)))
     FAP_CUDA(fapk::launch_minplus_strips(Cpath != nullptr, dseg, 1, mp_strips_of(s), K, st, !i32,
-                                         e->tile_cols));
+                                         e->tile_cols, rows_aligned16(s)));
   else
     FAP_CUDA(fapk::launch_minplus_tiles(!i32, Cpath != nullptr, dseg, 1, tiles, packed, st));
   FAP_CUDA(cudaStreamSynchronize(st));
@@ -2359,7 +2369,7 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes, int32
 }
 
 int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s) {
-  if (!e || !ops_per_s || mode < 0 || mode > 9) return set_error(FAP_ERR_INVALID, "fap_addmin_peak: bad arguments");
+  if (!e || !ops_per_s || mode < 0 || mode > 11) return set_error(FAP_ERR_INVALID, "fap_addmin_peak: bad arguments");
   std::lock_guard<std::mutex> lk(e->mu);
   DeviceGuard dg(e->device);
   FAP_CUDA(fapk::measure_addmin_peak(mode, e->sm_count, ops_per_s));

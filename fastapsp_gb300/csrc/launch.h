@@ -28,8 +28,11 @@ cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, i
 // f32: FP32 distances (any range) instead of the packed int32 form.
 // tile_cols (packed form): 64 or 128-column tiles, 0 = the default of the
 // K class (minplus_strip_class_cols); the FP32 form always takes 64.
+// aligned: every segment's C (and Cp) rows start on 16-byte boundaries (the
+// other form realigns its 16-byte stores row by row).
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                                  int max_k, cudaStream_t st, bool f32 = false, int tile_cols = 0);
+                                  int max_k, cudaStream_t st, bool f32 = false, int tile_cols = 0,
+                                  bool aligned = true);
 int minplus_strip_class_cols(int c);
 int minplus_strip_tiles();
 // Strip form of the FW remaining-tile phase (packed int32, or FP32 with

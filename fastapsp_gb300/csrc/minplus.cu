@@ -211,6 +211,43 @@ __device__ __forceinline__ bool fw_column(const MpSegment &s, int col, int64_t &
 }
 
 // Whether the output rows allow 16-byte stores of 4 consecutive columns.
+// Stores the values of a 64-column row segment held by 16 lanes (4
+// consecutive columns a lane; p = this lane's first column) where the row is
+// not 16-byte aligned: each lane stores the aligned 16-byte chunk that starts
+// inside its quad, completed with the next lane's first values; the ragged
+// ends of the segment (lane 0's values before the first boundary, lane 15's
+// after the last) go as single stores.  All 32 lanes call it (the values
+// move by shuffles within each half-warp); `ok` drops the stores of a row
+// outside the matrix.
+template <typename V>
+__device__ __forceinline__ void store_quad_unaligned(V *p, const V v[4], int tx, bool ok) {
+  V nx[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) nx[q] = __shfl_down_sync(0xffffffffu, v[q], 1, 16);
+  if (!ok) return;
+  const int o = (int)((reinterpret_cast<uintptr_t>(p) >> 2) & 3);  // the same for the whole segment
+  if (o == 0) {
+    __stcs(reinterpret_cast<uint4 *>(p), make_uint4((unsigned)v[0], (unsigned)v[1], (unsigned)v[2], (unsigned)v[3]));
+    return;
+  }
+  if (tx < 15) {  // chunk [p + 4 - o, p + 8 - o): v[4 - o .. 3], then nx[0 .. 3 - o]
+    const V w0 = o == 1 ? v[3] : o == 2 ? v[2] : v[1];
+    const V w1 = o == 1 ? nx[0] : o == 2 ? v[3] : v[2];
+    const V w2 = o == 1 ? nx[1] : o == 2 ? nx[0] : v[3];
+    const V w3 = o == 1 ? nx[2] : o == 2 ? nx[1] : nx[0];
+    __stcs(reinterpret_cast<uint4 *>(p + 4 - o), make_uint4((unsigned)w0, (unsigned)w1, (unsigned)w2, (unsigned)w3));
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (q >= 4 - o) p[q] = v[q];
+  }
+  if (tx == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (q < 4 - o) p[q] = v[q];
+  }
+}
+
 template <bool PRED>
 __device__ __forceinline__ bool vec_stores_ok(const MpSegment &s) {
   bool ok = (s.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(s.C) & 15) == 0;
@@ -572,6 +609,8 @@ __global__ void __launch_bounds__(kThreads, 2)
 // per tile.  Shared memory (ks = K rounded up to 4):
 //   B[2][ks][TN] | Bp[1 + ks][TN] | colp[2][TN] | coll[2][TN] | ownidx[2][TN] |
 //   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
+// and, FP32 only, Ar[128][kseg] (A row-major) | Bc[64][strip_bc_stride(kseg)]
+// (the current tile's B column-major).
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
 // Work counters of the strip min-plus (diagnostics): [tiles, tiles with no
@@ -594,11 +633,18 @@ constexpr int kStripClassK[] = {48, kStripMaxK};
 constexpr int kStripClassTN[] = {64, 128};
 constexpr int kStripClasses = 2;
 
-// Shared memory of the strip kernel with TN-column tiles, in bytes.
-template <int TN>
+// Row stride of the FP32 strip kernel's column-major copy of B for kseg
+// steps: kseg, or kseg + 4 when kseg / 4 is even, so that the stride in
+// 16-byte units is odd.
+__host__ __device__ constexpr int strip_bc_stride(int kseg) { return ((kseg >> 2) & 1) ? kseg : kseg + 4; }
+
+// Shared memory of the strip kernel with TN-column tiles, in bytes; F32 adds
+// the row-major copy of A ([128][ks]) and the column-major copy of B
+// ([64][ks + 4] at most).
+template <int TN, bool F32 = false>
 __host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
   return ((size_t)2 * ks * TN + (size_t)(ks + 1) * TN + 6 * TN + (size_t)2 * kOwnCap * kTile +
-          (size_t)ks * kTile) * 4;
+          (size_t)ks * kTile + (F32 ? (size_t)kTile * ks + (size_t)TN * (ks + 4) : 0)) * 4;
 }
 
 __device__ __forceinline__ const MpSegment &find_strip_segment(const MpSegment *__restrict__ segs,
@@ -611,11 +657,24 @@ __device__ __forceinline__ const MpSegment &find_strip_segment(const MpSegment *
   return segs[lo];
 }
 
+// Layout of the FP32 strip kernels' operands in shared memory: entry (k, m)
+// of A^T and entry (k, col) of B sit at row k, position m ^ swz(k) and
+// col ^ swz(k) -- the 4-entry chunks of step group k / 4 permuted by XOR with
+// its low three bits.  Within a group the permutation is the same, so a
+// thread's four consecutive rows or columns stay one aligned 16-byte chunk;
+// after the add-mins, threads that look up entries of different step groups
+// of the same rows or columns hit different banks.  The packed form keeps
+// the plain layout (SWZ false).
+template <bool SWZ>
+__device__ __forceinline__ int swz(int k) {
+  return SWZ ? ((k >> 2) & 7) << 2 : 0;
+}
+
 // Copies a ks x TN tile of a row-major 4-byte matrix (rows < K, columns
-// [col0, col0 + TN) < N) into dst[ks][TN]; each thread moves 4 consecutive
-// columns of a row per pass (one 16-byte copy when `vec`), and writes `fill`
-// where the source is outside the matrix.
-template <int TN>
+// [col0, col0 + TN) < N) into dst[ks][TN] (SWZ: chunks permuted by swz);
+// each thread moves 4 consecutive columns of a row per pass (one 16-byte
+// copy when `vec`), and writes `fill` where the source is outside the matrix.
+template <int TN, bool SWZ = false>
 __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *src, int64_t ld,
                                                 int K, int N, int ks, int col0, bool vec,
                                                 unsigned fill) {
@@ -624,7 +683,7 @@ __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *s
   const int j = (t % TPR) * 4;
   const int col = col0 + j;
   for (int kk = t / TPR; kk < ks; kk += kThreads / TPR) {
-    unsigned *d = dst + kk * TN + j;
+    unsigned *d = dst + kk * TN + (j ^ swz<SWZ>(kk));
     const unsigned *g = src + (int64_t)kk * ld + col;
     if (kk < K && vec && col + 3 < N) {
       cp_async16(d, g);
@@ -641,10 +700,13 @@ __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *s
 // Turns the B values this thread copied (same mapping as strip_load_rows)
 // into keys (d << 7) | (k + 1), and sets bit k of kmask (a 128-bit mask in
 // shared memory) for every row k that has a finite entry in the tile.
-// F32: the values stay (FP32 bits, "unreached" = the bits of 1e8); only the
-// row bits are set.
+// F32 (TN = 64): the values stay (FP32 bits, "unreached" = the bits of 1e8);
+// the row bits are set and the values are also written to Bc, the tile's
+// column-major copy (column col at row (col & 3) * 16 + (col >> 2), stride
+// bcs).
 template <int TN, bool F32 = false>
-__device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kmask) {
+__device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kmask,
+                                             unsigned *Bc = nullptr, int bcs = 0) {
   constexpr int TPR = TN / 4;
   const int t = threadIdx.x;
   const int j = (t % TPR) * 4;
@@ -655,6 +717,11 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
     if (F32) {
       if (min(min(v.x, v.y), min(v.z, v.w)) < __float_as_uint(Dist<float>::inf()))
         atomicOr(&kmask[kk >> 5], 1u << (kk & 31));
+      // column j + q goes to row q * 16 + j / 4 of the column-major copy
+      Bc[(0 * 16 + (j >> 2)) * bcs + kk] = v.x;
+      Bc[(1 * 16 + (j >> 2)) * bcs + kk] = v.y;
+      Bc[(2 * 16 + (j >> 2)) * bcs + kk] = v.z;
+      Bc[(3 * 16 + (j >> 2)) * bcs + kk] = v.w;
       continue;
     }
     const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < kPackH;
@@ -681,20 +748,155 @@ __device__ __forceinline__ void strip_addmin(unsigned &acc, int &arg, unsigned a
   }
 }
 
-// Two add-mins of the FP32 strip kernel, steps idx0 and idx0 + 1 (the later
-// one second): one 3-input minimum over the value bits, then the step of the
-// last strict improvement -- idx0 + 1 only if its value is below both the
-// current one and step idx0's, idx0 if its value is below the current one
-// and not above step idx0 + 1's -- the same result as two strip_addmin calls
-// in order, with 2.5 instead of 3 ALU-pipe instructions per add-min.
-__device__ __forceinline__ void strip_addmin2_f32(unsigned &acc, int &arg, unsigned a0, unsigned b0,
-                                                  unsigned a1, unsigned b1, int idx0) {
-  const unsigned v0 = __float_as_uint(__uint_as_float(a0) + __uint_as_float(b0));
-  const unsigned v1 = __float_as_uint(__uint_as_float(a1) + __uint_as_float(b1));
-  const unsigned m = __vimin3_u32(acc, v0, v1);
-  const int pick = v0 == m ? idx0 : idx0 + 1;
-  arg = m < acc ? pick : arg;
-  acc = m;
+// Four add-mins of the FP32 strip kernel, steps k0 .. k0 + 3: the minimum of
+// the four sums, and the current value and group tag (k0 + 1) replaced only
+// on a strict improvement.  That leaves the step of the last strict
+// improvement in the tagged group: its first step whose sum equals the final
+// value, since every earlier step's sum is above it (strip_resolve_f32 finds
+// it after the loop).  Nine instructions per four add-mins.
+__device__ __forceinline__ void strip_addmin4_f32(unsigned &acc, int &tag, const unsigned a[4],
+                                                  const unsigned b[4], int grp) {
+  const unsigned v0 = __float_as_uint(__fadd_rn(__uint_as_float(a[0]), __uint_as_float(b[0])));
+  const unsigned v1 = __float_as_uint(__fadd_rn(__uint_as_float(a[1]), __uint_as_float(b[1])));
+  const unsigned v2 = __float_as_uint(__fadd_rn(__uint_as_float(a[2]), __uint_as_float(b[2])));
+  const unsigned v3 = __float_as_uint(__fadd_rn(__uint_as_float(a[3]), __uint_as_float(b[3])));
+  const unsigned t = min(__vimin3_u32(v0, v1, v2), v3);
+  const bool imp = t < acc;
+  acc = imp ? t : acc;
+  tag = imp ? grp : tag;
+}
+
+// The step idx (k + 1) of an output whose last strict improvement fell in the
+// group tagged `tag` (0: none): the group's first step whose sum has the
+// final value's bits.  ap / bp point at the output's A and B entries of the
+// group's first step (strides sa, sb between steps).
+__device__ __forceinline__ int strip_resolve_f32(unsigned acc, int tag, const unsigned *ap, int sa,
+                                                 const unsigned *bp, int sb) {
+  const unsigned v0 = __float_as_uint(__fadd_rn(__uint_as_float(ap[0]), __uint_as_float(bp[0])));
+  const unsigned v1 = __float_as_uint(__fadd_rn(__uint_as_float(ap[sa]), __uint_as_float(bp[sb])));
+  const unsigned v2 = __float_as_uint(__fadd_rn(__uint_as_float(ap[2 * sa]), __uint_as_float(bp[2 * sb])));
+  const int j = v0 == acc ? 0 : v1 == acc ? 1 : v2 == acc ? 2 : 3;
+  return tag > 0 ? tag + j : 0;
+}
+
+// FP32 add-mins of a thread's 8 x 4 outputs over steps [0, kseg) (kseg a
+// multiple of 4) in groups of four, then, with PRED, each output's group
+// resolved to the step idx (k + 1) of its last strict improvement -- the
+// same values and steps as single add-mins in ascending order.  As: A^T
+// [k][sa] and Bs: B [k][sb] in the swizzled layout (swz); the thread's rows
+// are a0 .. a0 + 3 and a0 + kBlk .. a0 + kBlk + 3, its columns b0 .. b0 + 3.
+// With LEAN, the B operands load two columns at a time (24 operands live
+// instead of 32).
+template <bool PRED, bool LEAN = false>
+__device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&arg)[8][4],
+                                                  const unsigned *As, int sa, int a0,
+                                                  const unsigned *Bs, int sb, int b0, int kseg) {
+  for (int kk = 0; kk < kseg; kk += 4) {
+    const unsigned *acol = As + kk * sa + (a0 ^ swz<true>(kk));
+    const unsigned *bcol = Bs + kk * sb + (b0 ^ swz<true>(kk));
+    unsigned b[4][4];  // [column][step]
+    if (!LEAN) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(bcol + j * sb);
+        b[0][j] = v.x, b[1][j] = v.y, b[2][j] = v.z, b[3][j] = v.w;
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      unsigned a[4][4];  // [row of the half][step]
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(acol + j * sa + h * kBlk);
+        a[0][j] = v.x, a[1][j] = v.y, a[2][j] = v.z, a[3][j] = v.w;
+      }
+#pragma unroll
+      for (int ch = 0; ch < 2; ch++) {
+        if (LEAN) {
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const uint2 v = *reinterpret_cast<const uint2 *>(bcol + j * sb + ch * 2);
+            b[ch * 2][j] = v.x, b[ch * 2 + 1][j] = v.y;
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+          for (int c = ch * 2; c < ch * 2 + 2; c++)
+            strip_addmin4_f32(acc[h * 4 + r][c], arg[h * 4 + r][c], a[r], b[c], kk + 1);
+      }
+    }
+  }
+  if (PRED) {
+#pragma unroll
+    for (int r = 0; r < 8; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int k0 = arg[r][c] > 0 ? arg[r][c] - 1 : 0;
+        const int sw = swz<true>(k0);
+        arg[r][c] = strip_resolve_f32(acc[r][c], arg[r][c], As + k0 * sa + (a0 ^ sw) + (r >> 2) * kBlk + (r & 3),
+                                      sa, Bs + k0 * sb + (b0 ^ sw) + c, sb);
+      }
+  }
+}
+
+// The same for the strip min-plus, from row-major copies of the operands:
+// Ar[128][kseg] (row m's steps contiguous) and Bc, the tile's B
+// column-major (column col at row (col & 3) * 16 + (col >> 2), stride bcs,
+// bcs / 4 odd).  One 16-byte load gives a row's or a column's four steps of
+// a group, so the resolve takes two loads per output; the eight rows of Bc
+// that a 16-byte load phase reads (eight consecutive columns' chunks) lie in
+// eight different bank groups.  The thread's rows are r0 .. r0 + 3 and
+// r0 + 64 .. r0 + 67, its columns tx * 4 .. tx * 4 + 3.  B operands load
+// two columns at a time (24 operands live).
+template <bool PRED>
+__device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], int (&arg)[8][4],
+                                                       const unsigned *Ar, int kseg, int r0,
+                                                       const unsigned *Bc, int bcs, int tx) {
+  const unsigned *arow = Ar + r0 * kseg;  // row r0 + m at arow + m * kseg
+  const unsigned *bcol = Bc + tx * bcs;   // column tx * 4 + c at bcol + c * 16 * bcs
+  for (int kk = 0; kk < kseg; kk += 4) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      unsigned a[4][4];  // [row of the half][step]
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(arow + (h * kBlk + r) * kseg + kk);
+        a[r][0] = v.x, a[r][1] = v.y, a[r][2] = v.z, a[r][3] = v.w;
+      }
+#pragma unroll
+      for (int ch = 0; ch < 2; ch++) {
+        unsigned b[2][4];  // [column of the pair][step]
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          const uint4 v = *reinterpret_cast<const uint4 *>(bcol + (ch * 2 + c) * 16 * bcs + kk);
+          b[c][0] = v.x, b[c][1] = v.y, b[c][2] = v.z, b[c][3] = v.w;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+          for (int c = 0; c < 2; c++)
+            strip_addmin4_f32(acc[h * 4 + r][ch * 2 + c], arg[h * 4 + r][ch * 2 + c], a[r], b[c], kk + 1);
+      }
+    }
+  }
+  if (PRED) {
+#pragma unroll
+    for (int r = 0; r < 8; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int tag = arg[r][c];
+        const int k0 = tag > 0 ? tag - 1 : 0;
+        const uint4 av = *reinterpret_cast<const uint4 *>(arow + ((r >> 2) * kBlk + (r & 3)) * kseg + k0);
+        const uint4 bv = *reinterpret_cast<const uint4 *>(bcol + c * 16 * bcs + k0);
+        const unsigned v0 = __float_as_uint(__fadd_rn(__uint_as_float(av.x), __uint_as_float(bv.x)));
+        const unsigned v1 = __float_as_uint(__fadd_rn(__uint_as_float(av.y), __uint_as_float(bv.y)));
+        const unsigned v2 = __float_as_uint(__fadd_rn(__uint_as_float(av.z), __uint_as_float(bv.z)));
+        const unsigned m = acc[r][c];
+        const int j = v0 == m ? 0 : v1 == m ? 1 : v2 == m ? 2 : 3;
+        arg[r][c] = tag > 0 ? tag + j : 0;
+      }
+  }
 }
 
 // TN = 64 (the class K <= 48): 128x64 tiles, 8x4 outputs per thread, up to
@@ -706,7 +908,7 @@ __device__ __forceinline__ void strip_addmin2_f32(unsigned &acc, int &arg, unsig
 // current value was kept (non-negative floats order like their bits) -- the
 // reference's strict-<, ascending-k rule, as in the packed form.  TN = 64
 // only, two CTAs per SM.
-template <bool PRED, int TN, bool F32 = false>
+template <bool PRED, int TN, bool F32 = false, bool UA = false>
 __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
     mp_strip_kernel(const MpSegment *__restrict__ segs, int nseg, int ks) {
   constexpr int CH = TN / 64;  // 64-column halves of a thread's outputs
@@ -719,6 +921,8 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
   unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + 2 * TN);  // [kOwnCap][128 rows]
   int32_t *Fpst = reinterpret_cast<int32_t *>(Fst + kOwnCap * kTile);  // [kOwnCap][128 rows]
   unsigned *As = reinterpret_cast<unsigned *>(Fpst + kOwnCap * kTile);  // A^T [ks][128]
+  unsigned *Ar = As + ks * kTile;  // F32: A row-major [128][kseg]
+  unsigned *Bc = Ar + kTile * ks;  // F32: the tile's B column-major [64][bcs]
   __shared__ MpSegment seg;
   __shared__ int s_own[2];                   // own columns of the tile (per tile parity)
   __shared__ int16_t s_ownlist[2][kOwnCap];  // their tile columns, by slot
@@ -743,6 +947,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
   const unsigned INF = F32 ? __float_as_uint(Dist<float>::inf()) : Dist<uint32_t>::inf();
   const int kseg = (s.K + 3) & ~3;  // this segment's K rounded up to 4 (<= ks)
+  const int bcs = strip_bc_stride(kseg);
   const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
   const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
   const bool vec_c = vec_stores_ok<PRED>(s);
@@ -802,10 +1007,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
   for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
     const int kk = idx >> 7, m = idx & (kTile - 1);
     unsigned *d = &As[idx];
-    if (row0 + m < s.M && kk < s.K)
-      cp_async4(d, static_cast<const unsigned *>(s.A) + (int64_t)(row0 + m) * s.lda + kk);
-    else
+    if (row0 + m < s.M && kk < s.K) {
+      const unsigned *g = static_cast<const unsigned *>(s.A) + (int64_t)(row0 + m) * s.lda + kk;
+      cp_async4(d, g);
+      if (F32) cp_async4(&Ar[m * kseg + kk], g);
+    } else {
       *d = INF;
+      if (F32) Ar[m * kseg + kk] = INF;
+    }
   }
   strip_load_rows<TN>(Bs, static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, kseg, jt0 * TN, vec_b, INF);
   load_flags(jt0 * TN, 0);
@@ -833,7 +1042,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
         if (__any_sync(0xffffffffu, F32 ? v < INF : v < kPackH) && (threadIdx.x & 31) == 0)
           atomicOr(&s_amask[kk >> 5], 1u << (kk & 31));
       }
-    strip_keys_b<TN, F32>(Bcur, kseg, s_kmask[buf]);
+    strip_keys_b<TN, F32>(Bcur, kseg, s_kmask[buf], Bc, bcs);
     // List the tile's own columns (threads 0..TN-1 copied their column's
     // flags; slots are taken in any order through a counter).
     if (threadIdx.x == 0) s_own[buf ^ 1] = 0;  // used by the next tile
@@ -877,7 +1086,8 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
     const int nact = __popcll(mlo) + __popcll(mhi);
     n_tiles++;
     n_empty += nact == 0;
-    n_steps += (unsigned long long)nact * kTile * TN;
+    // (FP32 with at least half of the steps active runs all of them)
+    n_steps += (unsigned long long)(F32 && CH == 1 && nact > 0 && 2 * nact >= kseg ? kseg : nact) * kTile * TN;
     if (PRED && nact == s.K && s.K > 0)  // every step active: all rows, 16-byte copies spread over the CTA
       strip_load_rows<TN>(reinterpret_cast<unsigned *>(Bps + TN), reinterpret_cast<const unsigned *>(s.Bp),
                           s.ldbp, s.K, s.N, kseg, jt * TN, vec_bp, 0xffffffffu);
@@ -903,41 +1113,29 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
     // reachability most steps are skipped.  Either way the next step's
     // operands load while the current step's add-mins issue.
     {
-      const unsigned *acol = As + ty * 4;
-      const unsigned *bcol = Bcur + tx * 4;
-      if (F32 && CH == 1 && nact == s.K && s.K > 0) {
-        // FP32, every step active: two steps per pass (kseg is a multiple
-        // of 4; steps at or past K hold "unreached" and never win)
-        for (int kk = 0; kk < kseg; kk += 2) {
-          const uint4 na0 = *reinterpret_cast<const uint4 *>(acol + kk * kTile);
-          const uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kk * kTile + kBlk);
-          const uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * TN);
-          const uint4 ma0 = *reinterpret_cast<const uint4 *>(acol + (kk + 1) * kTile);
-          const uint4 ma1 = *reinterpret_cast<const uint4 *>(acol + (kk + 1) * kTile + kBlk);
-          const uint4 mb0 = *reinterpret_cast<const uint4 *>(bcol + (kk + 1) * TN);
-          const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
-          const unsigned b[4] = {nb0.x, nb0.y, nb0.z, nb0.w};
-          const unsigned a2[8] = {ma0.x, ma0.y, ma0.z, ma0.w, ma1.x, ma1.y, ma1.z, ma1.w};
-          const unsigned b2[4] = {mb0.x, mb0.y, mb0.z, mb0.w};
-#pragma unroll
-          for (int r = 0; r < 8; r++)
-#pragma unroll
-            for (int c = 0; c < 4; c++) strip_addmin2_f32(acc[r][c], arg[r][c], a[r], b[c], a2[r], b2[c], kk + 1);
-        }
+      // the thread's operands of step k
+      auto a_at = [&](int k) { return As + k * kTile + ty * 4; };
+      auto b_at = [&](int k) { return Bcur + k * TN + tx * 4; };
+      // FP32 with at least half of the steps active: all steps in groups
+      // of four (steps that are not active, or at or past K, hold
+      // "unreached" on one side and never win).
+      const bool grouped = F32 && CH == 1 && nact > 0 && 2 * nact >= kseg;
+      if (grouped) {
+        if constexpr (F32 && CH == 1) addmin_groups_rows_f32<PRED>(acc, arg, Ar, kseg, ty * 4, Bc, bcs, tx);
       } else if (nact == s.K && s.K > 0) {
-        uint4 na0 = *reinterpret_cast<const uint4 *>(acol);
-        uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kBlk);
-        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol);
-        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kBlk) : nb0;
+        uint4 na0 = *reinterpret_cast<const uint4 *>(a_at(0));
+        uint4 na1 = *reinterpret_cast<const uint4 *>(a_at(0) + kBlk);
+        uint4 nb0 = *reinterpret_cast<const uint4 *>(b_at(0));
+        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(b_at(0) + kBlk) : nb0;
 #pragma unroll 2
         for (int kk = 0; kk < kseg; kk++) {
           const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
           const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
           const int kn = kk + 1 < kseg ? kk + 1 : kk;
-          na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
-          na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
-          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
-          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
+          na0 = *reinterpret_cast<const uint4 *>(a_at(kn));
+          na1 = *reinterpret_cast<const uint4 *>(a_at(kn) + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(b_at(kn));
+          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(b_at(kn) + kBlk);
 #pragma unroll
           for (int r = 0; r < 8; r++)
 #pragma unroll
@@ -958,20 +1156,20 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
           return -1;
         };
         int kk = next_k();
-        uint4 na0 = *reinterpret_cast<const uint4 *>(acol + kk * kTile);
-        uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kk * kTile + kBlk);
-        uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * TN);
-        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(bcol + kk * TN + kBlk) : nb0;
+        uint4 na0 = *reinterpret_cast<const uint4 *>(a_at(kk));
+        uint4 na1 = *reinterpret_cast<const uint4 *>(a_at(kk) + kBlk);
+        uint4 nb0 = *reinterpret_cast<const uint4 *>(b_at(kk));
+        uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(b_at(kk) + kBlk) : nb0;
         while (kk >= 0) {
           const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
           const unsigned b[8] = {nb0.x, nb0.y, nb0.z, nb0.w, nb1.x, nb1.y, nb1.z, nb1.w};
           const int cur = kk;
           kk = next_k();
           const int kn = kk >= 0 ? kk : 0;
-          na0 = *reinterpret_cast<const uint4 *>(acol + kn * kTile);
-          na1 = *reinterpret_cast<const uint4 *>(acol + kn * kTile + kBlk);
-          nb0 = *reinterpret_cast<const uint4 *>(bcol + kn * TN);
-          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(bcol + kn * TN + kBlk);
+          na0 = *reinterpret_cast<const uint4 *>(a_at(kn));
+          na1 = *reinterpret_cast<const uint4 *>(a_at(kn) + kBlk);
+          nb0 = *reinterpret_cast<const uint4 *>(b_at(kn));
+          if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(b_at(kn) + kBlk);
 #pragma unroll
           for (int r = 0; r < 8; r++)
 #pragma unroll
@@ -992,32 +1190,40 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
       for (int c = 0; c < 4 * CH; c++)
         if (ownidx[buf * TN + (c >> 2) * kBlk + tx * 4 + (c & 3)] != -1) ownmask |= 1u << c;
     }
+    // The unaligned store form (UA) masks rows and columns outside the
+    // matrix per lane instead of skipping them: it moves values between lanes.
+    const bool cols_full = colbase + TN <= n_cols;  // uniform over the CTA
 #pragma unroll
     for (int r = 0; r < 8; r++) {
       const int rr = (r >> 2) * kBlk + (r & 3);  // row offset from this thread's first row
       const int row = row0 + ty * 4 + rr;
-      if (row >= m_rows) continue;
+      const bool row_ok = row < m_rows;
+      if (!UA && !row_ok) continue;
       unsigned *crow = c_thr + rr * ldc;
       int32_t *prow = PRED ? p_thr + rr * ldcp : nullptr;
 #pragma unroll
       for (int h = 0; h < CH; h++) {
         const int sc0 = h * kBlk + tx * 4;
         const int col0 = colbase + sc0;
-        if (col0 >= n_cols) continue;
+        const bool ok = row_ok && col0 < n_cols;
+        if (!UA && !ok) continue;
         unsigned d[4] = {INF, INF, INF, INF};
         int32_t p[4] = {-1, -1, -1, -1};
-        // a quad of unreached outputs (the common case on sparse graphs) needs
-        // no decode and no predecessor gathers
-        const unsigned qmin = min(min(acc[r][h * 4], acc[r][h * 4 + 1]),
-                                  min(acc[r][h * 4 + 2], acc[r][h * 4 + 3]));
-        if (qmin < (F32 ? INF : kPackH << kIdxBits)) {
+        if (F32) {  // the value is at most "unreached"; step idx 0 reads predecessor -1
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            const unsigned key = acc[r][h * 4 + q];
-            if (F32) {
-              d[q] = key >= INF ? INF : key;
-              if (PRED) p[q] = Bps[arg[r][h * 4 + q] * TN + sc0 + q];
-            } else {
+            d[q] = acc[r][h * 4 + q];
+            if (PRED) p[q] = Bps[arg[r][h * 4 + q] * TN + sc0 + q];
+          }
+        } else {
+          // a quad of unreached outputs (the common case on sparse graphs)
+          // needs no decode and no predecessor gathers
+          const unsigned qmin = min(min(acc[r][h * 4], acc[r][h * 4 + 1]),
+                                    min(acc[r][h * 4 + 2], acc[r][h * 4 + 3]));
+          if (qmin < (kPackH << kIdxBits)) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const unsigned key = acc[r][h * 4 + q];
               const unsigned dist = key >> kIdxBits;
               d[q] = dist >= kPackH ? INF : dist;
               if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
@@ -1032,17 +1238,20 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
             if (oi >= 0) {  // own-part column: the FW value, staged
               d[q] = Fst[oi * kTile + row - row0];
               if (PRED) p[q] = Fpst[oi * kTile + row - row0];
-            } else if (oi == -2) {  // own-part column beyond the staging slots
+            } else if (oi == -2 && ok) {  // own-part column beyond the staging slots
               const int64_t fj = coll[buf * TN + sc0 + q] - s.local0;
               d[q] = static_cast<const unsigned *>(s.F)[(int64_t)row * s.ldf + fj];
               if (PRED) p[q] = s.Fp[(int64_t)row * s.ldf + fj];
             }
           }
         }
-        if (vec_c && col0 + 3 < n_cols) {  // streaming stores: the rows are not read again here
+        if (vec_c && ok && col0 + 3 < n_cols) {  // streaming stores: the rows are not read again here
           __stcs(reinterpret_cast<uint4 *>(crow + col0), make_uint4(d[0], d[1], d[2], d[3]));
           if (PRED) __stcs(reinterpret_cast<int4 *>(prow + col0), make_int4(p[0], p[1], p[2], p[3]));
-        } else {
+        } else if (UA && !vec_c && cols_full) {  // rows not 16-byte aligned: realigned 16-byte stores
+          store_quad_unaligned(crow + col0, d, tx, row_ok);
+          if (PRED) store_quad_unaligned(prow + col0, p, tx, row_ok);
+        } else if (ok) {
 #pragma unroll
           for (int q = 0; q < 4; q++)
             if (col0 + q < n_cols) {
@@ -1091,9 +1300,9 @@ __device__ __forceinline__ int fw_strips_x(const MpSegment &s) {
 
 // Copies rows [0, 64) of B-like data (row k at src + k * ld, columns of the
 // tile's 64-column blocks starting at cbase.x / cbase.y, -1 for none) into
-// dst[64][TN]; 16-byte copies of 4 columns where aligned, `fill` outside the
-// matrix.
-template <int TN>
+// dst[64][TN] (SWZ: chunks permuted by swz); 16-byte copies of 4 columns
+// where aligned, `fill` outside the matrix.
+template <int TN, bool SWZ = false>
 __device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, int64_t ld, int K,
                                           int N, int2 cbase, bool vec, unsigned fill) {
   constexpr int TPR = TN / 4;  // threads per row
@@ -1102,7 +1311,7 @@ __device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, in
   const int cb = (j >> 6) ? cbase.y : cbase.x;
   const int col = cb + (j & 63);
   for (int kk = t / TPR; kk < kBlk; kk += kThreads / TPR) {
-    unsigned *d = dst + kk * TN + j;
+    unsigned *d = dst + kk * TN + (j ^ swz<SWZ>(kk));
     const unsigned *g = src + (int64_t)kk * ld + col;
     if (cb >= 0 && kk < K && vec && col + 3 < N) {
       cp_async16(d, g);
@@ -1172,14 +1381,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     const int kk = idx >> 7, m = idx & (kTile - 1);
     const int rb = (m >> 6) ? rbase1 : rbase0;
     const int row = rb + (m & 63);
-    unsigned *d = &sm.A[kk][m];
+    unsigned *d = &sm.A[kk][m ^ swz<F32>(kk)];
     if (rb >= 0 && row < s.M && kk < s.K)
       cp_async4(d, static_cast<const unsigned *>(s.A) + (int64_t)row * s.lda + kk);
     else
       *d = INF;
   }
   int2 cb = col_bases(jt0);
-  fw_load_b<TN>(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
+  fw_load_b<TN, F32>(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
   cp_async_commit();
   // The epilogue's view of C in registers (the descriptor is in shared memory).
   unsigned *const c_mat = static_cast<unsigned *>(s.C);
@@ -1192,7 +1401,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     const int buf = (jt - jt0) & 1;
     cb = col_bases(jt);
     if (jt + 1 < jt1)
-      fw_load_b<TN>(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
+      fw_load_b<TN, F32>(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
                 col_bases(jt + 1), vec_b, INF);
     cp_async_commit();
     cp_async_wait_1();  // A and this tile's B have landed
@@ -1274,14 +1483,22 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       unsigned long long msk = (unsigned long long)(s_kmask[buf][0] & s_amask[0]) |
                                ((unsigned long long)(s_kmask[buf][1] & s_amask[1]) << 32);
       if (kseg < 64) msk &= (1ull << kseg) - 1ull;
-      n_work += (unsigned long long)(__popcll(msk) == s.K ? kseg : __popcll(msk)) * kTile * TN;
-      if (F32 && msk) {
-        while (msk) {
+      const int nact = __popcll(msk);
+      // FP32 with at least half of the steps active: all steps in groups of
+      // four (steps that are not active hold "unreached" on one side)
+      const bool grouped = F32 && CH == 1 && nact > 0 && 2 * nact >= kseg;
+      n_work += (unsigned long long)(nact == s.K || grouped ? kseg : nact) * kTile * TN;
+      if (grouped) {
+        if constexpr (F32 && CH == 1)
+          addmin_groups_f32<PRED>(acc, arg, &sm.A[0][0], kTile, ty * 4, &sm.B[buf][0][0], TN, tx * 4, kseg);
+      } else if (F32 && msk) {
+        while (msk) {  // (the swizzled layout)
           const int kk = __ffsll(msk) - 1;
           msk &= msk - 1ull;
-          const uint4 na0 = *reinterpret_cast<const uint4 *>(acol + kk * kTile);
-          const uint4 na1 = *reinterpret_cast<const uint4 *>(acol + kk * kTile + kBlk);
-          const uint4 nb0 = *reinterpret_cast<const uint4 *>(bcol + kk * TN);
+          const unsigned *ak = &sm.A[kk][(ty * 4) ^ swz<true>(kk)];
+          const uint4 na0 = *reinterpret_cast<const uint4 *>(ak);
+          const uint4 na1 = *reinterpret_cast<const uint4 *>(ak + kBlk);
+          const uint4 nb0 = *reinterpret_cast<const uint4 *>(&sm.B[buf][kk][(tx * 4) ^ swz<true>(kk)]);
           const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
           const unsigned b[4] = {nb0.x, nb0.y, nb0.z, nb0.w};
 #pragma unroll
@@ -1827,10 +2044,15 @@ cudaError_t launch_packed_t(const MpSegment *d_segs, int nseg, int tiles, int ti
 }
 
 template <bool PRED, int TN, bool F32 = false>
-cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks, cudaStream_t st) {
+cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks, cudaStream_t st,
+                           bool aligned) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
   ++launch_count();
-  mp_strip_kernel<PRED, TN, F32><<<strips, kThreads, strip_smem_bytes<TN>(ks), st>>>(d_segs, nseg, ks);
+  if (aligned)
+    mp_strip_kernel<PRED, TN, F32><<<strips, kThreads, strip_smem_bytes<TN, F32>(ks), st>>>(d_segs, nseg, ks);
+  else
+    mp_strip_kernel<PRED, TN, F32, true>
+        <<<strips, kThreads, strip_smem_bytes<TN, F32>(ks), st>>>(d_segs, nseg, ks);
   return cudaGetLastError();
 }
 
@@ -1868,19 +2090,19 @@ cudaError_t launch_minplus_tiles(bool f32, bool pred, const MpSegment *d_segs, i
 }
 
 cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                                  int max_k, cudaStream_t st, bool f32, int tile_cols) {
+                                  int max_k, cudaStream_t st, bool f32, int tile_cols, bool aligned) {
   if (max_k < 0 || max_k > kStripMaxK) return cudaErrorInvalidValue;
   const int ks = (max_k + 3) & ~3;
   if (f32)  // 128 x 64 tiles at every K (the argmin registers leave no room for 128 x 128)
-    return pred ? launch_strip_t<true, 64, true>(d_segs, nseg, strips, ks, st)
-                : launch_strip_t<false, 64, true>(d_segs, nseg, strips, ks, st);
+    return pred ? launch_strip_t<true, 64, true>(d_segs, nseg, strips, ks, st, aligned)
+                : launch_strip_t<false, 64, true>(d_segs, nseg, strips, ks, st, aligned);
   const int tn = tile_cols ? tile_cols : kStripClassTN[max_k <= kStripClassK[0] ? 0 : 1];
   if (tn == 64)
-    return pred ? launch_strip_t<true, 64>(d_segs, nseg, strips, ks, st)
-                : launch_strip_t<false, 64>(d_segs, nseg, strips, ks, st);
+    return pred ? launch_strip_t<true, 64>(d_segs, nseg, strips, ks, st, aligned)
+                : launch_strip_t<false, 64>(d_segs, nseg, strips, ks, st, aligned);
   if (tn == 128)
-    return pred ? launch_strip_t<true, 128>(d_segs, nseg, strips, ks, st)
-                : launch_strip_t<false, 128>(d_segs, nseg, strips, ks, st);
+    return pred ? launch_strip_t<true, 128>(d_segs, nseg, strips, ks, st, aligned)
+                : launch_strip_t<false, 128>(d_segs, nseg, strips, ks, st, aligned);
   return cudaErrorInvalidValue;
 }
 
@@ -1957,25 +2179,21 @@ cudaError_t init_minplus_kernels() {
   static_assert(kStripClassTN[0] == 64 && kStripClassTN[1] == 128, "strip tile widths");
   const int smax0 = (int)strip_smem_bytes<64>((kStripMaxK + 3) & ~3);
   const int smax1 = (int)strip_smem_bytes<128>((kStripMaxK + 3) & ~3);
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 64>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax0)) != cudaSuccess)
+#define FAP_STRIP_ATTR(P, TN, F, SMAX)                                                            \
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<P, TN, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                SMAX)) != cudaSuccess)                                             \
+    return e;                                                                                      \
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<P, TN, F, true>,                                   \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMAX)) != cudaSuccess) \
     return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 64>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax0)) != cudaSuccess)
-    return e;
-  const int smaxf = (int)strip_smem_bytes<64>((kStripMaxK + 3) & ~3);
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 64, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smaxf)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 64, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smaxf)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<true, 128>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax1)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<false, 128>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smax1)) != cudaSuccess)
-    return e;
+  FAP_STRIP_ATTR(true, 64, false, smax0)
+  FAP_STRIP_ATTR(false, 64, false, smax0)
+  const int smaxf = (int)strip_smem_bytes<64, true>((kStripMaxK + 3) & ~3);
+  FAP_STRIP_ATTR(true, 64, true, smaxf)
+  FAP_STRIP_ATTR(false, 64, true, smaxf)
+  FAP_STRIP_ATTR(true, 128, false, smax1)
+  FAP_STRIP_ATTR(false, 128, false, smax1)
+#undef FAP_STRIP_ATTR
 
   if ((e = cudaFuncSetAttribute(fw_pivot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(PivotSmem))) != cudaSuccess)

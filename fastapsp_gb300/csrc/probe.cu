@@ -1,12 +1,13 @@
 // probe.cu -- add-min issue-rate microbenchmark (the roofline denominator of
 // the Floyd-Warshall and min-plus phases; no counterpart in the reference).
 //
-// Each thread keeps 64 independent accumulators and applies the add-min
-// operation of the chosen kind to them from register operands only (no
-// memory traffic), so the kernel runs at the SM's issue limit for that
-// instruction sequence.  Operands rotate over 4 register sets and one set is
-// bumped per pass so that the compiler cannot fold repeated minima; the bump
-// costs 16 of every 272 instructions, which makes the measured peak a slight
+// Each thread keeps 64 independent accumulators (32 for the forms that keep
+// an index beside each value) and applies the add-min operation of the
+// chosen kind to them from register operands only (no memory traffic), so
+// the kernel runs at the SM's issue limit for that instruction sequence.
+// Operands rotate over 4 register sets and one set is bumped per pass so
+// that the compiler cannot fold repeated minima; the bump costs one
+// instruction per 16 add-mins, which makes the measured peak a slight
 // underestimate.
 //   mode 0: int32 DPX add-min   acc = __viaddmin_u32(a, b, acc)
 //   mode 1: FP32 add-min        acc = fminf(a + b, acc)
@@ -19,7 +20,14 @@
 //           improvement (the FP32 strip kernel's step), written four ways:
 //           6 __vibmin_s32 (values are non-negative floats), 7 one unsigned
 //           compare and two predicated moves, 8 a float compare, fminf and a
-//           select, 9 __vibmin_u32 (the form the FP32 kernels use)
+//           select, 9 __vibmin_u32 (the single-step form of the FP32
+//           kernels)
+//   mode 10: FP32 add-mins in groups of four steps keeping the group of the
+//           last strict improvement (the FP32 strip kernels' dense loop):
+//           four adds, a 3-input and a 2-input minimum, one compare, two
+//           selects
+//   mode 11: mode 10 with the four adds as two paired adds (add.f32x2) on
+//           operands held as step pairs
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -46,36 +54,75 @@ __device__ __forceinline__ float2 add_f32x2(float2 a, float2 b) {
   return make_float2(__uint_as_float((unsigned)z), __uint_as_float((unsigned)(z >> 32)));
 }
 
+// Output columns per thread (4 rows each): 16, or 8 for the forms that keep
+// an index beside each value, so that the outputs and operands stay in
+// registers.
+__host__ __device__ constexpr int probe_cols(int mode) { return mode == 2 || mode == 3 || mode >= 6 ? 8 : 16; }
+
 template <int MODE>
 __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int iters, unsigned seed) {
   constexpr bool F = (MODE == 1 || MODE == 3 || MODE == 5 || MODE >= 6);
+  constexpr bool GROUPED = MODE >= 10;
   constexpr bool ARG = (MODE == 2 || MODE == 3 || MODE >= 6);
   using T = typename std::conditional<F, float, unsigned>::type;
-  T a[4][4], b[4][16], acc[4][16];
-  int arg[4][16];
+  constexpr int NC = probe_cols(MODE);
+  T a[4][4], b[4][NC], acc[4][NC];
+  int arg[4][NC];
   const unsigned t = threadIdx.x + blockIdx.x * blockDim.x + seed;
 #pragma unroll
   for (int s = 0; s < 4; s++)
 #pragma unroll
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < NC; i++) {
       if (i < 4) a[s][i] = (T)((t * 7 + s * 13 + i * 3) & 1023);
       b[s][i] = (T)((t * 5 + s * 11 + i * 17) & 1023);
     }
 #pragma unroll
   for (int r = 0; r < 4; r++)
 #pragma unroll
-    for (int c = 0; c < 16; c++) {
+    for (int c = 0; c < NC; c++) {
       acc[r][c] = (T)(1 << 20);
       arg[r][c] = 0;
     }
-  for (int it = 0; it < iters; it++) {
-    if constexpr (MODE == 4 || MODE == 5) {
+  // four passes per trip, so that the bumped register set has a fixed index
+  // (a register-array index that varies at run time puts the array in local
+  // memory)
+  for (int it0 = 0; it0 < iters; it0 += 4)
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const int it = it0 + u;
+    if constexpr (GROUPED) {
+      const int grp = it * 4 + 1;
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+          unsigned v0, v1, v2, v3;
+          if (MODE == 10) {
+            v0 = __float_as_uint(__fadd_rn((float)a[0][r], (float)b[0][c]));
+            v1 = __float_as_uint(__fadd_rn((float)a[1][r], (float)b[1][c]));
+            v2 = __float_as_uint(__fadd_rn((float)a[2][r], (float)b[2][c]));
+            v3 = __float_as_uint(__fadd_rn((float)a[3][r], (float)b[3][c]));
+          } else {
+            const float2 p01 = add_f32x2(make_float2((float)a[0][r], (float)a[1][r]),
+                                         make_float2((float)b[0][c], (float)b[1][c]));
+            const float2 p23 = add_f32x2(make_float2((float)a[2][r], (float)a[3][r]),
+                                         make_float2((float)b[2][c], (float)b[3][c]));
+            v0 = __float_as_uint(p01.x), v1 = __float_as_uint(p01.y);
+            v2 = __float_as_uint(p23.x), v3 = __float_as_uint(p23.y);
+          }
+          const unsigned t = min(__vimin3_u32(v0, v1, v2), v3);
+          const unsigned ac = __float_as_uint((float)acc[r][c]);
+          const bool imp = t < ac;
+          acc[r][c] = (T)__uint_as_float(imp ? t : ac);
+          arg[r][c] = imp ? grp : arg[r][c];
+        }
+    } else if constexpr (MODE == 4 || MODE == 5) {
 #pragma unroll
       for (int s = 0; s < 4; s += 2)
 #pragma unroll
         for (int r = 0; r < 4; r++)
 #pragma unroll
-          for (int c = 0; c < 16; c++) {
+          for (int c = 0; c < NC; c++) {
             if (MODE == 4) {
               acc[r][c] = (T)min3_u32((unsigned)acc[r][c], (unsigned)a[s][r] + (unsigned)b[s][c],
                                       (unsigned)a[s + 1][r] + (unsigned)b[s + 1][c]);
@@ -91,7 +138,7 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
 #pragma unroll
         for (int r = 0; r < 4; r++)
 #pragma unroll
-          for (int c = 0; c < 16; c++) {
+          for (int c = 0; c < NC; c++) {
             const T x = a[s][r], y = b[s][c];
             const int idx = it * 4 + s + 1;
             if (MODE == 0) {
@@ -134,13 +181,13 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
       }
     }
 #pragma unroll
-    for (int i = 0; i < 16; i++) b[it & 3][i] = b[it & 3][i] - (T)1;
+    for (int i = 0; i < NC; i++) b[u][i] = b[u][i] - (T)1;
   }
   unsigned x = 0;
 #pragma unroll
   for (int r = 0; r < 4; r++)
 #pragma unroll
-    for (int c = 0; c < 16; c++) {
+    for (int c = 0; c < NC; c++) {
       unsigned v;
       if (F) v = __float_as_uint((float)acc[r][c]); else v = (unsigned)acc[r][c];
       x ^= v + (ARG ? (unsigned)arg[r][c] : 0u);
@@ -179,7 +226,9 @@ cudaError_t measure_addmin_peak(int mode, int sm_count, double *ops_per_s) {
       case 6: e = run_mode<6>(buf, blocks, iters, 0); break;
       case 7: e = run_mode<7>(buf, blocks, iters, 0); break;
       case 8: e = run_mode<8>(buf, blocks, iters, 0); break;
-      default: e = run_mode<9>(buf, blocks, iters, 0); break;
+      case 9: e = run_mode<9>(buf, blocks, iters, 0); break;
+      case 10: e = run_mode<10>(buf, blocks, iters, 0); break;
+      default: e = run_mode<11>(buf, blocks, iters, 0); break;
     }
     cudaEventRecord(b, 0);
     if (e != cudaSuccess) break;
@@ -193,7 +242,8 @@ cudaError_t measure_addmin_peak(int mode, int sm_count, double *ops_per_s) {
   cudaEventDestroy(b);
   cudaFree(buf);
   if (e != cudaSuccess) return e;
-  const double ops = (double)blocks * 256 * iters * 4 * 4 * 16;
+  const int cols = probe_cols(mode);
+  const double ops = (double)blocks * 256 * iters * 4 * 4 * cols;
   *ops_per_s = ops / (best * 1e-3);
   return cudaSuccess;
 }

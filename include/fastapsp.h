@@ -399,7 +399,10 @@ int fap_sssp_stats(fap_engine *e, uint64_t *out5);
  * min; 5: FP32, two add-mins as one paired add (add.f32x2) and one 3-input
  * min; 6-9: FP32 add-min keeping the step of the last strict improvement,
  * as __vibmin_s32 (6), a compare and two predicated moves (7), a float
- * compare, fminf and a select (8), __vibmin_u32 (9). */
+ * compare, fminf and a select (8), __vibmin_u32 (9); 10: FP32 add-mins in
+ * groups of four steps keeping the group of the last strict improvement
+ * (the FP32 strip kernels' dense loop); 11: mode 10 with paired adds
+ * (add.f32x2). */
 int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s);
 
 #ifdef __cplusplus

@@ -44,6 +44,10 @@ def cases():
     # 2^24 - 1, where the engine must leave its packed keys for the wide form
     # and where the reference's FP32 arithmetic is no longer exact
     yield "bigw300_dir_wide", graphs.small_random_graph(300, 650, True, True, seed=10, wmax=3_500_000), 4
+    # rows of n = 301 and 303 entries are not 16-byte aligned: the min-plus
+    # stores them with its realigned form
+    yield "knn301_dir_int", graphs.geometric_knn(301, seed=12), 5
+    yield "road303_f32", graphs.road_like(303, seed=13), 6
 
 
 def main():
