@@ -143,6 +143,9 @@ struct Plan {
     // strip form
     std::vector<const MpSegment *> rests;
     std::vector<int> rests_nseg, rests_strips;
+    // FP32 form: round r's row and column panels, strip form
+    std::vector<const MpSegment *> pstrips;
+    std::vector<int> pstrips_nseg, pstrips_strips;
     // boundary rows in their own buffer (host results): per part {element
     // offset in the results, element offset in the buffer, elements}, copied
     // out as soon as the SSSP has written them
@@ -516,6 +519,22 @@ int fw_strips_of(const MpSegment &s, int tiles_y) {
   return tiles_y * ((s.tiles_x + T - 1) / T);
 }
 
+// FP32 form: fw_segments' two panels of pivot block r of nb as strip-form
+// segments, appended to `out` from CTA `strips` on.  Each reads and writes
+// the same entries (the row panel is B and C, the column panel A and C); a
+// CTA reads the entries it writes into shared memory before its epilogue,
+// and no two CTAs write the same entries.
+void fw_panel_strips(const MpSegment &rowp, const MpSegment &colp, int nb, std::vector<MpSegment> &out,
+                     int &strips) {
+  MpSegment a = rowp, c = colp;
+  a.strip_begin = strips;
+  strips += fw_strips_of(rowp, 1);
+  out.push_back(a);
+  c.strip_begin = strips;
+  strips += fw_strips_of(colp, nb / 2);  // (nb - 1) row blocks in pairs
+  out.push_back(c);
+}
+
 // Lookahead form of fw_segments' `rest` for pivot block r of nb: the rows and
 // columns other than r and r + 1 (block row and column r + 1 get round r's
 // update inside pivot step r + 1).  Returns its CTAs in the strip form.
@@ -625,7 +644,7 @@ int build_plan(fap_engine *e, Plan &pl) {
   TableBuilder tb;
   struct GroupOffs {
     size_t batches, batches_alt, pdesc, row_begin, dec_begin, mp, bjobs, bsrc;
-    std::vector<size_t> diag, panel, rest, rest2, rests;
+    std::vector<size_t> diag, panel, rest, rest2, rests, pstrips;
   };
   std::vector<GroupOffs> goffs(groups.size());
   pl.groups.assign(groups.size(), Plan::Group{});
@@ -762,14 +781,17 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.rests_nseg.assign(maxnb, 0);
     G.rests_strips.assign(maxnb, 0);
     O.rests.assign(maxnb, 0);
+    G.pstrips_nseg.assign(maxnb, 0);
+    G.pstrips_strips.assign(maxnb, 0);
+    O.pstrips.assign(maxnb, 0);
     O.diag.assign(maxnb, 0);
     O.panel.assign(maxnb, 0);
     O.rest.assign(maxnb, 0);
     O.rest2.assign(maxnb, 0);
     for (int r = 0; r < maxnb; r++) {
       std::vector<FwDiagJob> dj;
-      std::vector<MpSegment> ps, rs, r2s, rss;
-      int pt = 0, rt = 0, r2strips = 0, rsstrips = 0;
+      std::vector<MpSegment> ps, rs, r2s, rss, pss;
+      int pt = 0, rt = 0, r2strips = 0, rsstrips = 0, psstrips = 0;
       for (const PartDesc &d : pdesc) {
         int nb = d.ld / B;
         if (r >= nb) continue;
@@ -786,7 +808,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         {  // 64^3 block products: pivot step (lookahead update, closure, panels); tile form (all blocks)
           const unsigned long long blk = (unsigned long long)B * B * B;
           pl.fw_pivot_work += blk * ((r > 0 ? 2ull * (nb - 2) + 1 : 0ull) + 1ull + 2ull * (nb - 1));
-          pl.fw_tile_work += blk * (e->f32() ? 2ull * nb - 1 : (unsigned long long)nb * nb);
+          pl.fw_tile_work += blk * (e->f32() ? 1ull : (unsigned long long)nb * nb);
         }
         if (nb > 1) {
           MpSegment rp, cp, rest;
@@ -801,6 +823,7 @@ int build_plan(fap_engine *e, Plan &pl) {
           rest.tile_begin = rt;
           rt += a3;
           rs.push_back(rest);
+          fw_panel_strips(rp, cp, nb, pss, psstrips);
           MpSegment rest2 = rest;
           const int s2 = r + 1 < nb ? fw_rest_lookahead(rest2, nb, r) : fw_strips_of(rest, rest.tiles_x);
           if (s2 > 0) {
@@ -831,6 +854,9 @@ int build_plan(fap_engine *e, Plan &pl) {
       G.rests_nseg[r] = (int)rss.size();
       G.rests_strips[r] = rsstrips;
       O.rests[r] = tb.add(rss.data(), rss.size());
+      G.pstrips_nseg[r] = (int)pss.size();
+      G.pstrips_strips[r] = psstrips;
+      O.pstrips[r] = tb.add(pss.data(), pss.size());
     }
   }
   int st = pl.tables.ensure(std::max<size_t>(tb.bytes.size(), 64));
@@ -856,12 +882,14 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.rest.resize(R);
     G.rest2.resize(R);
     G.rests.resize(R);
+    G.pstrips.resize(R);
     for (size_t r = 0; r < R; r++) {
       G.diag[r] = reinterpret_cast<const FwDiagJob *>(base + O.diag[r]);
       G.panel[r] = reinterpret_cast<const MpSegment *>(base + O.panel[r]);
       G.rest[r] = reinterpret_cast<const MpSegment *>(base + O.rest[r]);
       G.rest2[r] = reinterpret_cast<const MpSegment *>(base + O.rest2[r]);
       G.rests[r] = reinterpret_cast<const MpSegment *>(base + O.rests[r]);
+      G.pstrips[r] = reinterpret_cast<const MpSegment *>(base + O.pstrips[r]);
     }
   }
   return FAP_OK;
@@ -1009,11 +1037,13 @@ struct Issuer {
         FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
       } else {
         FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
-        FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
-        if (f32)  // FP32: remaining tiles in the strip form
+        if (f32) {  // FP32: panels, then the remaining tiles, in the strip form
+          FAP_CUDA(fapk::launch_fw_strips(pred, G.pstrips[r], G.pstrips_nseg[r], G.pstrips_strips[r], st, true));
           FAP_CUDA(fapk::launch_fw_strips(pred, G.rests[r], G.rests_nseg[r], G.rests_strips[r], st, true));
-        else
+        } else {
+          FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
           FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
+        }
       }
     }
     if (packed && rounds > 0) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (rounds - 1) % 2], 0));  // join
@@ -2156,13 +2186,13 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
   TableBuilder tb;
-  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb), ors(maxnb);
+  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb), ors(maxnb), ops(maxnb);
   std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), nr2(maxnb), sr2(maxnb), nrs(maxnb),
-      srs(maxnb);
+      srs(maxnb), nps(maxnb), sps(maxnb);
   for (int r = 0; r < maxnb; r++) {
     std::vector<FwDiagJob> dj;
-    std::vector<MpSegment> ps, rs, r2s, rss;
-    int pt = 0, rt = 0, r2strips = 0, rsstrips = 0;
+    std::vector<MpSegment> ps, rs, r2s, rss, pss;
+    int pt = 0, rt = 0, r2strips = 0, rsstrips = 0, psstrips = 0;
     for (int32_t b = 0; b < count; b++) {
       int nb = (sizes[b] + Bk - 1) / Bk;
       if (r >= nb) continue;
@@ -2188,6 +2218,7 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
         rest.tile_begin = rt;
         rt += t3;
         rs.push_back(rest);
+        fw_panel_strips(a, c, nb, pss, psstrips);
         MpSegment rest2 = rest;
         const int s2 = r + 1 < nb ? fw_rest_lookahead(rest2, nb, r) : fw_strips_of(rest, rest.tiles_x);
         if (s2 > 0) {
@@ -2210,6 +2241,9 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
     nrs[r] = (int)rss.size();
     srs[r] = rsstrips;
     ors[r] = tb.add(rss.data(), rss.size());
+    nps[r] = (int)pss.size();
+    sps[r] = psstrips;
+    ops[r] = tb.add(pss.data(), pss.size());
     nd[r] = (int)dj.size();
     od[r] = tb.add(dj.data(), dj.size());
     np[r] = (int)ps.size();
@@ -2255,13 +2289,17 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
       FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
     } else {
       FAP_CUDA(fapk::launch_fw_diag(f32, pred, djobs, nd[r], st));
-      FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r], tp[r], packed, st));
-      if (f32)
+      if (f32) {  // panels, then the remaining tiles, in the strip form
+        FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ops[r]), nps[r],
+                                        sps[r], st, true));
         FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ors[r]), nrs[r],
                                         srs[r], st, true));
-      else
+      } else {
+        FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r],
+                                            tp[r], packed, st));
         FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]),
                                             nr[r], tr[r], packed, st));
+      }
     }
   }
   if (packed) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (maxnb - 1) % 2], 0));  // join

@@ -218,7 +218,8 @@ __device__ __forceinline__ bool fw_column(const MpSegment &s, int col, int64_t &
 // ends of the segment (lane 0's values before the first boundary, lane 15's
 // after the last) go as single stores.  All 32 lanes call it (the values
 // move by shuffles within each half-warp); `ok` drops the stores of a row
-// outside the matrix.
+// outside the matrix.  (A case split on the misalignment, which is the same
+// for the whole warp, measured slower than these selects.)
 template <typename V>
 __device__ __forceinline__ void store_quad_unaligned(V *p, const V v[4], int tx, bool ok) {
   V nx[4];
