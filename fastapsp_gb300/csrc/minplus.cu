@@ -610,7 +610,8 @@ __global__ void __launch_bounds__(kThreads, 2)
 // per tile.  Shared memory (ks = K rounded up to 4):
 //   B[2][ks][TN] | Bp[1 + ks][TN] | colp[2][TN] | coll[2][TN] | ownidx[2][TN] |
 //   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
-// and, FP32 only, Ar[128][kseg] (A row-major) | Bc[64][strip_bc_stride(kseg)]
+// and, FP32 only, Ar[128][strip_bc_stride(kseg)] (A row-major) |
+// Bc[64][strip_bc_stride(kseg)]
 // (the current tile's B column-major).
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
@@ -640,12 +641,12 @@ constexpr int kStripClasses = 2;
 __host__ __device__ constexpr int strip_bc_stride(int kseg) { return ((kseg >> 2) & 1) ? kseg : kseg + 4; }
 
 // Shared memory of the strip kernel with TN-column tiles, in bytes; F32 adds
-// the row-major copy of A ([128][ks]) and the column-major copy of B
-// ([64][ks + 4] at most).
+// the row-major copy of A ([128][ks + 4] at most) and the column-major copy
+// of B ([64][ks + 4] at most).
 template <int TN, bool F32 = false>
 __host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
   return ((size_t)2 * ks * TN + (size_t)(ks + 1) * TN + 6 * TN + (size_t)2 * kOwnCap * kTile +
-          (size_t)ks * kTile + (F32 ? (size_t)kTile * ks + (size_t)TN * (ks + 4) : 0)) * 4;
+          (size_t)ks * kTile + (F32 ? (size_t)(kTile + TN) * (ks + 4) : 0)) * 4;
 }
 
 __device__ __forceinline__ const MpSegment &find_strip_segment(const MpSegment *__restrict__ segs,
@@ -698,16 +699,29 @@ __device__ __forceinline__ void strip_load_rows(unsigned *dst, const unsigned *s
   }
 }
 
+// Sets the bits of kmask for the warp's rows of a B tile (two rows of 16
+// lanes for TN = 64, starting at lane 0's row kk, which is even; one row for
+// TN = 128) that have a finite entry: one ballot and one atomic per warp.
+template <int TN>
+__device__ __forceinline__ void strip_mark_rows(unsigned *kmask, int kk, bool fin) {
+  const unsigned bal = __ballot_sync(0xffffffffu, fin);
+  if ((threadIdx.x & 31) == 0) {  // lane 0 holds the warp's first (even) row
+    const unsigned bits = TN == 64 ? ((bal & 0xffffu) ? 1u : 0u) | ((bal >> 16) ? 2u : 0u) : (bal ? 1u : 0u);
+    if (bits) atomicOr(&kmask[kk >> 5], bits << (kk & 31));
+  }
+}
+
 // Turns the B values this thread copied (same mapping as strip_load_rows)
 // into keys (d << 7) | (k + 1), and sets bit k of kmask (a 128-bit mask in
 // shared memory) for every row k that has a finite entry in the tile.
 // F32 (TN = 64): the values stay (FP32 bits, "unreached" = the bits of 1e8);
 // the row bits are set and the values are also written to Bc, the tile's
-// column-major copy (column col at row (col & 3) * 16 + (col >> 2), stride
-// bcs).
+// column-major copy (column col at row col, stride bcs).  ks is a multiple of 4, so a warp's rows are all below ks or all at
+// or past it, and the warp's lanes run the loop together.
 template <int TN, bool F32 = false>
 __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kmask,
                                              unsigned *Bc = nullptr, int bcs = 0) {
+  static_assert(TN == 64 || TN == 128, "row marks assume 16 or 32 lanes a row");
   constexpr int TPR = TN / 4;
   const int t = threadIdx.x;
   const int j = (t % TPR) * 4;
@@ -716,13 +730,11 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
     const unsigned idx = (unsigned)(kk & kMaxPackedK) + 1u;
     uint4 v = *p;
     if (F32) {
-      if (min(min(v.x, v.y), min(v.z, v.w)) < __float_as_uint(Dist<float>::inf()))
-        atomicOr(&kmask[kk >> 5], 1u << (kk & 31));
-      // column j + q goes to row q * 16 + j / 4 of the column-major copy
-      Bc[(0 * 16 + (j >> 2)) * bcs + kk] = v.x;
-      Bc[(1 * 16 + (j >> 2)) * bcs + kk] = v.y;
-      Bc[(2 * 16 + (j >> 2)) * bcs + kk] = v.z;
-      Bc[(3 * 16 + (j >> 2)) * bcs + kk] = v.w;
+      strip_mark_rows<TN>(kmask, kk, min(min(v.x, v.y), min(v.z, v.w)) < __float_as_uint(Dist<float>::inf()));
+      Bc[(j + 0) * bcs + kk] = v.x;  // column j + q is row j + q of the column-major copy
+      Bc[(j + 1) * bcs + kk] = v.y;
+      Bc[(j + 2) * bcs + kk] = v.z;
+      Bc[(j + 3) * bcs + kk] = v.w;
       continue;
     }
     const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < kPackH;
@@ -731,7 +743,7 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
     v.z = (min(v.z, kPackH) << kIdxBits) | idx;
     v.w = (min(v.w, kPackH) << kIdxBits) | idx;
     *p = v;
-    if (fin) atomicOr(&kmask[kk >> 5], 1u << (kk & 31));
+    strip_mark_rows<TN>(kmask, kk, fin);
   }
 }
 
@@ -750,11 +762,13 @@ __device__ __forceinline__ void strip_addmin(unsigned &acc, int &arg, unsigned a
 }
 
 // Four add-mins of the FP32 strip kernel, steps k0 .. k0 + 3: the minimum of
-// the four sums, and the current value and group tag (k0 + 1) replaced only
-// on a strict improvement.  That leaves the step of the last strict
-// improvement in the tagged group: its first step whose sum equals the final
-// value, since every earlier step's sum is above it (strip_resolve_f32 finds
-// it after the loop).  Nine instructions per four add-mins.
+// the current value and the four sums, and the group tag (k0 + 1) replaced
+// when that minimum is below the current value (a strict improvement).  That
+// leaves the step of the last strict improvement in the tagged group: its
+// first step whose sum equals the final value, since every earlier step's sum
+// is above it (strip_resolve_f32 finds it after the loop).  Eight
+// instructions per four add-mins: four FP32 adds, two 3-input minimums, a
+// compare and a select.
 __device__ __forceinline__ void strip_addmin4_f32(unsigned &acc, int &tag, const unsigned a[4],
                                                   const unsigned b[4], int grp) {
   const unsigned v0 = __float_as_uint(__fadd_rn(__uint_as_float(a[0]), __uint_as_float(b[0])));
@@ -842,27 +856,29 @@ __device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&a
 }
 
 // The same for the strip min-plus, from row-major copies of the operands:
-// Ar[128][kseg] (row m's steps contiguous) and Bc, the tile's B
-// column-major (column col at row (col & 3) * 16 + (col >> 2), stride bcs,
-// bcs / 4 odd).  One 16-byte load gives a row's or a column's four steps of
-// a group, so the resolve takes two loads per output; the eight rows of Bc
-// that a 16-byte load phase reads (eight consecutive columns' chunks) lie in
-// eight different bank groups.  The thread's rows are r0 .. r0 + 3 and
-// r0 + 64 .. r0 + 67, its columns tx * 4 .. tx * 4 + 3.  B operands load
-// two columns at a time (24 operands live).
+// Ar[128][ars] (row m's steps contiguous, ars = strip_bc_stride(kseg)) and
+// Bc, the tile's B column-major (column col at row col, stride bcs = ars).
+// One 16-byte load gives a row's or a column's four steps of a group, so the
+// resolve takes two loads per output.  Both strides are odd in 16-byte
+// units: the eight rows of Bc that a 16-byte load phase reads (eight
+// consecutive columns) lie in eight different bank groups, and so do the two
+// rows of Ar (four apart) that a warp reads.  The thread's rows are r0 ..
+// r0 + 3 and r0 + 64 .. r0 + 67, its columns tx, tx + 16, tx + 32 and
+// tx + 48.  B operands load two columns at a time (24 operands live).
 template <bool PRED>
 __device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], int (&arg)[8][4],
                                                        const unsigned *Ar, int kseg, int r0,
                                                        const unsigned *Bc, int bcs, int tx) {
-  const unsigned *arow = Ar + r0 * kseg;  // row r0 + m at arow + m * kseg
-  const unsigned *bcol = Bc + tx * bcs;   // column tx * 4 + c at bcol + c * 16 * bcs
+  const int ars = bcs;                   // Ar's row stride
+  const unsigned *arow = Ar + r0 * ars;  // row r0 + m at arow + m * ars
+  const unsigned *bcol = Bc + tx * bcs;   // column tx + 16 c at bcol + c * 16 * bcs
   for (int kk = 0; kk < kseg; kk += 4) {
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       unsigned a[4][4];  // [row of the half][step]
 #pragma unroll
       for (int r = 0; r < 4; r++) {
-        const uint4 v = *reinterpret_cast<const uint4 *>(arow + (h * kBlk + r) * kseg + kk);
+        const uint4 v = *reinterpret_cast<const uint4 *>(arow + (h * kBlk + r) * ars + kk);
         a[r][0] = v.x, a[r][1] = v.y, a[r][2] = v.z, a[r][3] = v.w;
       }
 #pragma unroll
@@ -888,7 +904,7 @@ __device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], in
       for (int c = 0; c < 4; c++) {
         const int tag = arg[r][c];
         const int k0 = tag > 0 ? tag - 1 : 0;
-        const uint4 av = *reinterpret_cast<const uint4 *>(arow + ((r >> 2) * kBlk + (r & 3)) * kseg + k0);
+        const uint4 av = *reinterpret_cast<const uint4 *>(arow + ((r >> 2) * kBlk + (r & 3)) * ars + k0);
         const uint4 bv = *reinterpret_cast<const uint4 *>(bcol + c * 16 * bcs + k0);
         const unsigned v0 = __float_as_uint(__fadd_rn(__uint_as_float(av.x), __uint_as_float(bv.x)));
         const unsigned v1 = __float_as_uint(__fadd_rn(__uint_as_float(av.y), __uint_as_float(bv.y)));
@@ -922,8 +938,8 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
   unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + 2 * TN);  // [kOwnCap][128 rows]
   int32_t *Fpst = reinterpret_cast<int32_t *>(Fst + kOwnCap * kTile);  // [kOwnCap][128 rows]
   unsigned *As = reinterpret_cast<unsigned *>(Fpst + kOwnCap * kTile);  // A^T [ks][128]
-  unsigned *Ar = As + ks * kTile;  // F32: A row-major [128][kseg]
-  unsigned *Bc = Ar + kTile * ks;  // F32: the tile's B column-major [64][bcs]
+  unsigned *Ar = As + ks * kTile;        // F32: A row-major [128][bcs]
+  unsigned *Bc = Ar + kTile * (ks + 4);  // F32: the tile's B column-major [64][bcs]
   __shared__ MpSegment seg;
   __shared__ int s_own[2];                   // own columns of the tile (per tile parity)
   __shared__ int16_t s_ownlist[2][kOwnCap];  // their tile columns, by slot
@@ -1004,17 +1020,24 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
     }
   };
 
-  // Prologue: A, B and the column flags of the first tile.
+  // Prologue: A, B and the column flags of the first tile.  A^T is copied
+  // with consecutive threads on consecutive rows (its shared-memory rows are
+  // contiguous), the FP32 row-major copy with consecutive threads on
+  // consecutive steps of a row (contiguous in both memories).
   for (int idx = threadIdx.x; idx < kTile * kseg; idx += kThreads) {
     const int kk = idx >> 7, m = idx & (kTile - 1);
     unsigned *d = &As[idx];
-    if (row0 + m < s.M && kk < s.K) {
-      const unsigned *g = static_cast<const unsigned *>(s.A) + (int64_t)(row0 + m) * s.lda + kk;
-      cp_async4(d, g);
-      if (F32) cp_async4(&Ar[m * kseg + kk], g);
-    } else {
+    if (row0 + m < s.M && kk < s.K)
+      cp_async4(d, static_cast<const unsigned *>(s.A) + (int64_t)(row0 + m) * s.lda + kk);
+    else
       *d = INF;
-      if (F32) Ar[m * kseg + kk] = INF;
+    if (F32) {
+      const int mr = idx / kseg, kr = idx - mr * kseg;
+      unsigned *dr = &Ar[mr * bcs + kr];
+      if (row0 + mr < s.M && kr < s.K)
+        cp_async4(dr, static_cast<const unsigned *>(s.A) + (int64_t)(row0 + mr) * s.lda + kr);
+      else
+        *dr = INF;
     }
   }
   strip_load_rows<TN>(Bs, static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, kseg, jt0 * TN, vec_b, INF);
@@ -1117,6 +1140,16 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
       // the thread's operands of step k
       auto a_at = [&](int k) { return As + k * kTile + ty * 4; };
       auto b_at = [&](int k) { return Bcur + k * TN + tx * 4; };
+      // B operands of step k: four consecutive columns (packed keys), or
+      // the FP32 thread's columns tx + 16 c (lanes of a row read
+      // consecutive words)
+      auto load_b = [&](int k) {
+        if (F32) {
+          const unsigned *q = Bcur + k * TN + tx;
+          return make_uint4(q[0], q[16], q[32], q[48]);
+        }
+        return *reinterpret_cast<const uint4 *>(b_at(k));
+      };
       // FP32 with at least half of the steps active: all steps in groups
       // of four (steps that are not active, or at or past K, hold
       // "unreached" on one side and never win).
@@ -1126,7 +1159,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
       } else if (nact == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(a_at(0));
         uint4 na1 = *reinterpret_cast<const uint4 *>(a_at(0) + kBlk);
-        uint4 nb0 = *reinterpret_cast<const uint4 *>(b_at(0));
+        uint4 nb0 = load_b(0);
         uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(b_at(0) + kBlk) : nb0;
 #pragma unroll 2
         for (int kk = 0; kk < kseg; kk++) {
@@ -1135,7 +1168,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
           const int kn = kk + 1 < kseg ? kk + 1 : kk;
           na0 = *reinterpret_cast<const uint4 *>(a_at(kn));
           na1 = *reinterpret_cast<const uint4 *>(a_at(kn) + kBlk);
-          nb0 = *reinterpret_cast<const uint4 *>(b_at(kn));
+          nb0 = load_b(kn);
           if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(b_at(kn) + kBlk);
 #pragma unroll
           for (int r = 0; r < 8; r++)
@@ -1159,7 +1192,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
         int kk = next_k();
         uint4 na0 = *reinterpret_cast<const uint4 *>(a_at(kk));
         uint4 na1 = *reinterpret_cast<const uint4 *>(a_at(kk) + kBlk);
-        uint4 nb0 = *reinterpret_cast<const uint4 *>(b_at(kk));
+        uint4 nb0 = load_b(kk);
         uint4 nb1 = CH == 2 ? *reinterpret_cast<const uint4 *>(b_at(kk) + kBlk) : nb0;
         while (kk >= 0) {
           const unsigned a[8] = {na0.x, na0.y, na0.z, na0.w, na1.x, na1.y, na1.z, na1.w};
@@ -1169,7 +1202,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
           const int kn = kk >= 0 ? kk : 0;
           na0 = *reinterpret_cast<const uint4 *>(a_at(kn));
           na1 = *reinterpret_cast<const uint4 *>(a_at(kn) + kBlk);
-          nb0 = *reinterpret_cast<const uint4 *>(b_at(kn));
+          nb0 = load_b(kn);
           if (CH == 2) nb1 = *reinterpret_cast<const uint4 *>(b_at(kn) + kBlk);
 #pragma unroll
           for (int r = 0; r < 8; r++)
@@ -1185,6 +1218,48 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
     // columns from the part's Floyd-Warshall matrix (only when the tile has
     // any; the test is uniform over the CTA).
     const int colbase = jt * TN;
+    if constexpr (F32) {
+      // FP32: the thread's columns are tx + 16 c, so each of the four
+      // 4-byte streaming stores of a row writes 64 consecutive bytes per
+      // half-warp, whatever the alignment of the row.  The value is at most
+      // "unreached"; step idx 0 reads predecessor -1.
+      unsigned ownm = 0;  // bit c: column tx + 16 c is the part's own
+      if (nown > 0) {
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+          if (ownidx[buf * TN + tx + 16 * c] != -1) ownm |= 1u << c;
+      }
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        const int rr = (r >> 2) * kBlk + (r & 3);  // row offset from this thread's first row
+        const int row = row0 + ty * 4 + rr;
+        if (row >= m_rows) continue;
+        unsigned *crow = c_thr + rr * ldc;
+        int32_t *prow = PRED ? p_thr + rr * ldcp : nullptr;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int sc = tx + 16 * c, col = colbase + sc;
+          unsigned d = acc[r][c];
+          int32_t pv = PRED ? Bps[arg[r][c] * TN + sc] : -1;
+          if ((ownm >> c) & 1u) {
+            const int oi = ownidx[buf * TN + sc];
+            if (oi >= 0) {  // own-part column: the FW value, staged
+              d = Fst[oi * kTile + row - row0];
+              if (PRED) pv = Fpst[oi * kTile + row - row0];
+            } else if (oi == -2 && col < n_cols) {  // own-part column beyond the staging slots
+              const int64_t fj = coll[buf * TN + sc] - s.local0;
+              d = static_cast<const unsigned *>(s.F)[(int64_t)row * s.ldf + fj];
+              if (PRED) pv = s.Fp[(int64_t)row * s.ldf + fj];
+            }
+          }
+          if (col < n_cols) {  // streaming stores: the rows are not read again here
+            __stcs(crow + col, d);
+            if (PRED) __stcs(prow + col, pv);
+          }
+        }
+      }
+      continue;
+    }
     unsigned ownmask = 0;  // bit h * 4 + q: this thread's column sc0 + q of half h is the part's own
     if (nown > 0) {
 #pragma unroll
@@ -1210,25 +1285,17 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
         if (!UA && !ok) continue;
         unsigned d[4] = {INF, INF, INF, INF};
         int32_t p[4] = {-1, -1, -1, -1};
-        if (F32) {  // the value is at most "unreached"; step idx 0 reads predecessor -1
+        // a quad of unreached outputs (the common case on sparse graphs)
+        // needs no decode and no predecessor gathers
+        const unsigned qmin = min(min(acc[r][h * 4], acc[r][h * 4 + 1]),
+                                  min(acc[r][h * 4 + 2], acc[r][h * 4 + 3]));
+        if (qmin < (kPackH << kIdxBits)) {
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            d[q] = acc[r][h * 4 + q];
-            if (PRED) p[q] = Bps[arg[r][h * 4 + q] * TN + sc0 + q];
-          }
-        } else {
-          // a quad of unreached outputs (the common case on sparse graphs)
-          // needs no decode and no predecessor gathers
-          const unsigned qmin = min(min(acc[r][h * 4], acc[r][h * 4 + 1]),
-                                    min(acc[r][h * 4 + 2], acc[r][h * 4 + 3]));
-          if (qmin < (kPackH << kIdxBits)) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-              const unsigned key = acc[r][h * 4 + q];
-              const unsigned dist = key >> kIdxBits;
-              d[q] = dist >= kPackH ? INF : dist;
-              if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
-            }
+            const unsigned key = acc[r][h * 4 + q];
+            const unsigned dist = key >> kIdxBits;
+            d[q] = dist >= kPackH ? INF : dist;
+            if (PRED) p[q] = Bps[(key & kIdxMask) * TN + sc0 + q];
           }
         }
         if ((ownmask >> (h * 4)) & 0xfu) {
@@ -2049,11 +2116,11 @@ cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks
                            bool aligned) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
   ++launch_count();
-  if (aligned)
+  if (aligned || F32)  // the FP32 epilogue stores 4-byte words at any alignment
     mp_strip_kernel<PRED, TN, F32><<<strips, kThreads, strip_smem_bytes<TN, F32>(ks), st>>>(d_segs, nseg, ks);
-  else
-    mp_strip_kernel<PRED, TN, F32, true>
-        <<<strips, kThreads, strip_smem_bytes<TN, F32>(ks), st>>>(d_segs, nseg, ks);
+  else if constexpr (!F32)
+    mp_strip_kernel<PRED, TN, false, true>
+        <<<strips, kThreads, strip_smem_bytes<TN, false>(ks), st>>>(d_segs, nseg, ks);
   return cudaGetLastError();
 }
 
@@ -2180,21 +2247,23 @@ cudaError_t init_minplus_kernels() {
   static_assert(kStripClassTN[0] == 64 && kStripClassTN[1] == 128, "strip tile widths");
   const int smax0 = (int)strip_smem_bytes<64>((kStripMaxK + 3) & ~3);
   const int smax1 = (int)strip_smem_bytes<128>((kStripMaxK + 3) & ~3);
-#define FAP_STRIP_ATTR(P, TN, F, SMAX)                                                            \
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<P, TN, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                SMAX)) != cudaSuccess)                                             \
-    return e;                                                                                      \
-  if ((e = cudaFuncSetAttribute(mp_strip_kernel<P, TN, F, true>,                                   \
+#define FAP_STRIP_ATTR1(P, TN, F, UA, SMAX)                                                    \
+  if ((e = cudaFuncSetAttribute(mp_strip_kernel<P, TN, F, UA>,                                    \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMAX)) != cudaSuccess) \
     return e;
-  FAP_STRIP_ATTR(true, 64, false, smax0)
-  FAP_STRIP_ATTR(false, 64, false, smax0)
+#define FAP_STRIP_ATTR(P, TN, SMAX)  \
+  FAP_STRIP_ATTR1(P, TN, false, false, SMAX) \
+  FAP_STRIP_ATTR1(P, TN, false, true, SMAX)
+  FAP_STRIP_ATTR(true, 64, smax0)
+  FAP_STRIP_ATTR(false, 64, smax0)
+  FAP_STRIP_ATTR(true, 128, smax1)
+  FAP_STRIP_ATTR(false, 128, smax1)
+  // FP32: one form for every row alignment
   const int smaxf = (int)strip_smem_bytes<64, true>((kStripMaxK + 3) & ~3);
-  FAP_STRIP_ATTR(true, 64, true, smaxf)
-  FAP_STRIP_ATTR(false, 64, true, smaxf)
-  FAP_STRIP_ATTR(true, 128, false, smax1)
-  FAP_STRIP_ATTR(false, 128, false, smax1)
+  FAP_STRIP_ATTR1(true, 64, true, false, smaxf)
+  FAP_STRIP_ATTR1(false, 64, true, false, smaxf)
 #undef FAP_STRIP_ATTR
+#undef FAP_STRIP_ATTR1
 
   if ((e = cudaFuncSetAttribute(fw_pivot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(PivotSmem))) != cudaSuccess)

@@ -44,10 +44,14 @@ def test_minplus_matches_oracle(ctx, oracle_lib, f32, M, N, K):
     rng = np.random.default_rng(M * 1000 + N * 10 + K)
     A = rand_dist(rng, (M, K), 0.2, f32)
     B = rand_dist(rng, (K, N), 0.2, f32)
-    # ties: force duplicate minima so the first-k rule matters
-    if K > 3 and not f32:
+    # ties: force duplicate minima so the first-k rule matters, within a group
+    # of four steps (k = 0, 1) and across groups (k = 2, 6)
+    if K > 3:
         B[1] = B[0]
         A[:, 1] = A[:, 0]
+    if K > 6:
+        B[6] = B[2]
+        A[:, 6] = A[:, 2]
     Bp = rng.integers(0, 10**6, size=(K, N)).astype(np.int32)
     ref_c, ref_p = oracle_lib.min_plus(as_oracle(A), as_oracle(B), Bp)
     dt = torch.float32 if f32 else torch.int32
