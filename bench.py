@@ -300,9 +300,13 @@ def run_solve(args, name, rank, world, local_rank):
     f32 = dtype == fap.DTYPE_F32
     # add-min peaks from registers, measured in this run: int32 DPX add-min,
     # and the form the min-plus runs (int32 with argmin, or FP32 with argmin)
+    # (FP32: the kernels' own form, add-mins in groups of four steps keeping
+    # the group of the last strict improvement, mode 10; int32: packed keys,
+    # one DPX add-min each, mode 0; mode 3 is the one-step FP32 form)
     peak_dpx = eng_ctx_peak(fap, dev, 0)
-    peak_mp = eng_ctx_peak(fap, dev, 3 if f32 else 2)
-    peak_fw = eng_ctx_peak(fap, dev, 3 if f32 else 0)
+    peak_mp = eng_ctx_peak(fap, dev, 10 if f32 else 0)
+    peak_fw = peak_mp
+    peak_f32_step = eng_ctx_peak(fap, dev, 3) if f32 else None
 
     def rate(x, ms):
         return x / (ms / 1e3) if ms and ms > 0 else float("nan")
@@ -350,10 +354,29 @@ def run_solve(args, name, rank, world, local_rank):
     gid_h = torch.from_numpy(gid).pin_memory()
     e2e_ms, e2e_parts = [], []
     host_alloc = None
+    link_gbs = None
     if args.e2e_steps > 0:
         npdt = np.float32 if f32 else np.int32
         dist_h, free_d, host_alloc = pinned_host((max(rows, 1), n), npdt)
         pred_h, free_p, _ = pinned_host((max(rows, 1), n), np.int32)
+        # The host link's own rate into the same rows: a plain device-to-host
+        # copy of the distance rows (each e2e step moves twice these bytes).
+        try:
+            dev_rows = torch.empty((max(rows, 1), n), dtype=tdt, device="cuda")
+            dev_rows.zero_()
+            host_view = torch.from_numpy(dist_h)
+            best = float("inf")
+            for _ in range(2):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                host_view.copy_(dev_rows, non_blocking=True)
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            link_gbs = dev_rows.numel() * 4 / best / 1e9
+            del dev_rows, host_view
+            torch.cuda.empty_cache()
+        except RuntimeError:
+            link_gbs = None
         for i in range(1 + args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -400,6 +423,8 @@ def run_solve(args, name, rank, world, local_rank):
                 "ms_per_step": e2e_ms_step,
                 "create_solve_destroy_ms": [statistics.mean(x) for x in zip(*e2e_parts)] if e2e_parts else None,
                 "solve_ms_each": [round(x[1], 1) for x in e2e_parts], "host_rows": host_alloc,
+                "host_link_d2h_gbs": link_gbs,
+                "host_link_floor_ms": d2h / (link_gbs * 1e9) * 1e3 if link_gbs else None,
                 "what": "fap_create (CSR from page-locked host arrays) + fap_solve into page-locked host rows "
                         "(n x n distances + predecessors) + fap_destroy, SSSP settings as tuned on this graph"},
         "gpu_launches": launches_per_step * args.steps,
@@ -423,10 +448,12 @@ def run_solve(args, name, rank, world, local_rank):
                 "unit": "Gaddmin/s", "frac": rate(executed, ph["min_plus"]) / peak_mp,
                 "dense_addmins_per_launch": addmin_mp,
                 "strip_tiles": mpc["tiles"], "tiles_without_active_step": mpc["empty_tiles"],
-                "peak_source": ("fap_addmin_peak mode 3 (FP32 add-min keeping the argmin)" if f32 else
-                                "fap_addmin_peak mode 2 (int32 add-min keeping the argmin)")
+                "peak_source": ("fap_addmin_peak mode 10 (FP32 add-mins in groups of four steps keeping the "
+                                "group of the last strict improvement, the kernel's form)" if f32 else
+                                "fap_addmin_peak mode 0 (int32 DPX add-min on packed keys, the kernel's form)")
                                + " from registers, measured in this run",
                 "peak_dpx_int32": peak_dpx / 1e9,
+                "peak_f32_one_step_argmin": peak_f32_step / 1e9 if peak_f32_step else None,
             },
         },
         "roofline_fw": {"achieved": rate(fw_executed, ph["floyd"]) / 1e9, "peak": peak_fw / 1e9,
@@ -436,7 +463,8 @@ def run_solve(args, name, rank, world, local_rank):
                         "dense_equivalent_rate": rate(addmin_fw, ph["floyd"]) / 1e9,
                         "note": "executed add-mins (fap_fw_counters: the remaining-tile strips' device counter "
                                 "plus the pivot or tile launches' block products) per FW phase time, against "
-                                + ("fap_addmin_peak mode 3 (FP32 add-min keeping the argmin)" if f32 else
+                                + ("fap_addmin_peak mode 10 (FP32 add-mins in groups of four keeping the "
+                                   "group of the last strict improvement)" if f32 else
                                    "fap_addmin_peak mode 0 (int32 DPX add-min)")},
         "roofline_sssp": {"bound": "hbm", "achieved": rate(sssp_bytes, ph["sssp"]) / 1e9, "peak": hbm,
                           "unit": "GB/s", "frac": rate(sssp_bytes, ph["sssp"]) / 1e9 / hbm,
@@ -678,12 +706,40 @@ def run_profile(args):
     d = torch.empty((g.n, g.n), dtype=torch.float32 if f32 else torch.int32, device="cuda")
     p = torch.empty((g.n, g.n), dtype=torch.int32, device="cuda")
     counts = []
-    for _ in range(args.profile_solves):
+    for i in range(args.profile_solves):
+        if i == args.profile_solves - 1:  # work counters of the last solve
+            eng.minplus_counters(reset=True)
+            eng.fw_counters(reset=True)
         eng.solve(d, p)
         torch.cuda.synchronize()
         counts.append(eng.last_launches())
     print(json.dumps({"profile": args.config, "n": g.n, "K": K, "launches_per_solve": counts,
-                      "phase_ms": eng.last_times()}))
+                      "phase_ms": eng.last_times(), "minplus_counters": eng.minplus_counters(reset=True),
+                      "fw_counters": eng.fw_counters(reset=True)}))
+
+
+def run_profile_c3(args):
+    """The batched Floyd-Warshall of the 512 dense instances only (for ncu),
+    --profile-solves times, each on a fresh copy of the inputs."""
+    import torch
+
+    import fastapsp_gb300 as fap
+    from fastapsp_gb300 import graphs
+
+    mats = graphs.dense_instances()
+    ctx = fap.Context(0)
+    ms = []
+    for _ in range(args.profile_solves):
+        dev = [torch.from_numpy(m).cuda() for m in mats]
+        preds = [torch.where(d < (1 << 30), torch.arange(d.shape[0], dtype=torch.int32, device="cuda")[:, None],
+                             torch.full((1, 1), -1, dtype=torch.int32, device="cuda")).contiguous() for d in dev]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.floyd_batched(1, dev, preds)
+        torch.cuda.synchronize()
+        ms.append((time.perf_counter() - t0) * 1e3)
+    ctx.close()
+    print(json.dumps({"profile": "c3", "instances": len(mats), "ms_per_run": ms}))
 
 
 def main():
@@ -729,6 +785,12 @@ def main():
 
         torch.cuda.set_device(local_rank)
         run_profile(args)
+        return
+    if args.profile and args.config == "c3":
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        run_profile_c3(args)
         return
     if args.config not in WORKLOADS:
         import torch

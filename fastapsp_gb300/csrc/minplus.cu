@@ -761,24 +761,34 @@ __device__ __forceinline__ void strip_addmin(unsigned &acc, int &arg, unsigned a
   }
 }
 
-// Four add-mins of the FP32 strip kernel, steps k0 .. k0 + 3: the minimum of
-// the current value and the four sums, and the group tag (k0 + 1) replaced
-// when that minimum is below the current value (a strict improvement).  That
-// leaves the step of the last strict improvement in the tagged group: its
-// first step whose sum equals the final value, since every earlier step's sum
-// is above it (strip_resolve_f32 finds it after the loop).  Eight
-// instructions per four add-mins: four FP32 adds, two 3-input minimums, a
-// compare and a select.
+// Four add-mins of the FP32 strip kernels, steps k0 .. k0 + 3: the current
+// value replaced by the minimum of the four sums when that is below it (a
+// strict improvement), and then the group tag (k0 + 1) too.  That leaves the
+// step of the last strict improvement in the tagged group: its first step
+// whose sum equals the final value, since every earlier step's sum is above
+// it (strip_resolve_f32 finds it after the loop).  Four FP32 adds, then
+// either a 3-input and a 2-input minimum, a compare and two selects, or
+// (MIN3ACC) two 3-input minimums with the current value as an input, a
+// compare and one select: fewer ALU instructions, but the current value and
+// the new one are live together, which cost the min-plus (at 128 registers a
+// thread) more in spills than it saved and made the FW tiles faster.
+template <bool MIN3ACC>
 __device__ __forceinline__ void strip_addmin4_f32(unsigned &acc, int &tag, const unsigned a[4],
                                                   const unsigned b[4], int grp) {
   const unsigned v0 = __float_as_uint(__fadd_rn(__uint_as_float(a[0]), __uint_as_float(b[0])));
   const unsigned v1 = __float_as_uint(__fadd_rn(__uint_as_float(a[1]), __uint_as_float(b[1])));
   const unsigned v2 = __float_as_uint(__fadd_rn(__uint_as_float(a[2]), __uint_as_float(b[2])));
   const unsigned v3 = __float_as_uint(__fadd_rn(__uint_as_float(a[3]), __uint_as_float(b[3])));
-  const unsigned t = min(__vimin3_u32(v0, v1, v2), v3);
-  const bool imp = t < acc;
-  acc = imp ? t : acc;
-  tag = imp ? grp : tag;
+  if constexpr (MIN3ACC) {
+    const unsigned nacc = __vimin3_u32(acc, __vimin3_u32(v0, v1, v2), v3);
+    tag = nacc != acc ? grp : tag;
+    acc = nacc;
+  } else {
+    const unsigned t = min(__vimin3_u32(v0, v1, v2), v3);
+    const bool imp = t < acc;
+    acc = imp ? t : acc;
+    tag = imp ? grp : tag;
+  }
 }
 
 // The step idx (k + 1) of an output whose last strict improvement fell in the
@@ -838,7 +848,7 @@ __device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&a
         for (int r = 0; r < 4; r++)
 #pragma unroll
           for (int c = ch * 2; c < ch * 2 + 2; c++)
-            strip_addmin4_f32(acc[h * 4 + r][c], arg[h * 4 + r][c], a[r], b[c], kk + 1);
+            strip_addmin4_f32<true>(acc[h * 4 + r][c], arg[h * 4 + r][c], a[r], b[c], kk + 1);
       }
     }
   }
@@ -893,7 +903,7 @@ __device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], in
         for (int r = 0; r < 4; r++)
 #pragma unroll
           for (int c = 0; c < 2; c++)
-            strip_addmin4_f32(acc[h * 4 + r][ch * 2 + c], arg[h * 4 + r][ch * 2 + c], a[r], b[c], kk + 1);
+            strip_addmin4_f32<false>(acc[h * 4 + r][ch * 2 + c], arg[h * 4 + r][ch * 2 + c], a[r], b[c], kk + 1);
       }
     }
   }
