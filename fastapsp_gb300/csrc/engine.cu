@@ -145,6 +145,7 @@ struct Plan {
     std::vector<int> rests_nseg, rests_strips;
     // FP32 form: round r's row and column panels, strip form
     std::vector<const MpSegment *> pstrips;
+    const void *tmaps = nullptr;  // tensor-map pairs of the FW matrices (null: none)
     std::vector<int> pstrips_nseg, pstrips_strips;
     // boundary rows in their own buffer (host results): per part {element
     // offset in the results, element offset in the buffer, elements}, copied
@@ -189,6 +190,11 @@ struct Plan {
 
 // Host-side table builder: appends POD records into one byte buffer and
 // remembers offsets, which become device pointers after the upload.
+// Storage of one CUtensorMap (encoded by fapk::encode_fw_tmaps).
+struct alignas(64) TmapBlob {
+  unsigned char bytes[128];
+};
+
 struct TableBuilder {
   std::vector<unsigned char> bytes;
   template <typename T>
@@ -468,12 +474,14 @@ bool is_device_ptr(const void *p) {
 // the remaining tiles).  Matrices are size x size with leading dimension ld.
 void fw_segments(void *D, int32_t *P, int64_t ld, int size, int r, MpSegment &rowp,
                  MpSegment &colp, MpSegment &rest, int &t_rowp, int &t_colp, int &t_rest,
-                 bool f32) {
+                 bool f32, int32_t tmap1 = 0) {
   const int B = fapk::fw_block();
   const int nb = (size + B - 1) / B;
   const size_t es = 4;
   (void)f32;
   MpSegment s{};
+  s.tmap1 = tmap1;  // the strips' bulk tensor copies, when the matrix has a map pair
+  s.b_row0 = r * B;
   s.A = static_cast<const unsigned char *>(D) + (size_t)r * B * es;
   s.lda = ld;
   s.B = static_cast<const unsigned char *>(D) + (size_t)r * B * ld * es;
@@ -645,6 +653,8 @@ int build_plan(fap_engine *e, Plan &pl) {
   struct GroupOffs {
     size_t batches, batches_alt, pdesc, row_begin, dec_begin, mp, bjobs, bsrc;
     std::vector<size_t> diag, panel, rest, rest2, rests, pstrips;
+    size_t tmaps = 0;
+    bool has_tmaps = false;
   };
   std::vector<GroupOffs> goffs(groups.size());
   pl.groups.assign(groups.size(), Plan::Group{});
@@ -788,11 +798,33 @@ int build_plan(fap_engine *e, Plan &pl) {
     O.panel.assign(maxnb, 0);
     O.rest.assign(maxnb, 0);
     O.rest2.assign(maxnb, 0);
+    // Tensor-map pairs (distances, predecessors) of the parts' FW matrices
+    // for the strips' bulk tensor copies; a part without one (no encoder)
+    // keeps the per-thread copies.
+    std::vector<int32_t> tmap1(pdesc.size(), 0);
+    {
+      std::vector<TmapBlob> maps;
+      for (size_t i = 0; i < pdesc.size(); i++) {
+        const PartDesc &d = pdesc[i];
+        TmapBlob two[2];
+        if (fapk::encode_fw_tmaps(two, fwd + (size_t)d.mat_off * 4, pred ? fwp + d.mat_off : nullptr, d.ld,
+                                  d.ld, d.ld)) {
+          tmap1[i] = (int32_t)(maps.size() / 2) + 1;
+          maps.push_back(two[0]);
+          maps.push_back(two[1]);
+        }
+      }
+      if (!maps.empty()) {
+        O.tmaps = tb.add(maps.data(), maps.size());
+        O.has_tmaps = true;
+      }
+    }
     for (int r = 0; r < maxnb; r++) {
       std::vector<FwDiagJob> dj;
       std::vector<MpSegment> ps, rs, r2s, rss, pss;
       int pt = 0, rt = 0, r2strips = 0, rsstrips = 0, psstrips = 0;
-      for (const PartDesc &d : pdesc) {
+      for (size_t pi = 0; pi < pdesc.size(); pi++) {
+        const PartDesc &d = pdesc[pi];
         int nb = d.ld / B;
         if (r >= nb) continue;
         void *D = fwd + (size_t)d.mat_off * 4;
@@ -813,7 +845,7 @@ int build_plan(fap_engine *e, Plan &pl) {
         if (nb > 1) {
           MpSegment rp, cp, rest;
           int a1, a2, a3;
-          fw_segments(D, P, d.ld, d.ld, r, rp, cp, rest, a1, a2, a3, e->f32());
+          fw_segments(D, P, d.ld, d.ld, r, rp, cp, rest, a1, a2, a3, e->f32(), tmap1[pi]);
           rp.tile_begin = pt;
           pt += a1;
           ps.push_back(rp);
@@ -876,6 +908,7 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.row_begin = reinterpret_cast<const int64_t *>(base + O.row_begin);
     G.dec_begin = reinterpret_cast<const int64_t *>(base + O.dec_begin);
     G.mp = reinterpret_cast<const MpSegment *>(base + O.mp);
+    G.tmaps = O.has_tmaps ? static_cast<const void *>(base + O.tmaps) : nullptr;
     size_t R = O.diag.size();
     G.diag.resize(R);
     G.panel.resize(R);
@@ -1033,13 +1066,16 @@ struct Issuer {
         FAP_CUDA(fapk::launch_fw_pivot(pred, G.diag[r], G.diag_cnt[r], st));
         FAP_CUDA(cudaEventRecord(e->ev_fw[0], st));
         FAP_CUDA(cudaStreamWaitEvent(e->side, e->ev_fw[0], 0));
-        FAP_CUDA(fapk::launch_fw_strips(pred, G.rest2[r], G.rest2_nseg[r], G.rest2_strips[r], e->side));
+        FAP_CUDA(fapk::launch_fw_strips(pred, G.rest2[r], G.rest2_nseg[r], G.rest2_strips[r], e->side, false,
+                                        G.tmaps));
         FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
       } else {
         FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
         if (f32) {  // FP32: panels, then the remaining tiles, in the strip form
-          FAP_CUDA(fapk::launch_fw_strips(pred, G.pstrips[r], G.pstrips_nseg[r], G.pstrips_strips[r], st, true));
-          FAP_CUDA(fapk::launch_fw_strips(pred, G.rests[r], G.rests_nseg[r], G.rests_strips[r], st, true));
+          FAP_CUDA(fapk::launch_fw_strips(pred, G.pstrips[r], G.pstrips_nseg[r], G.pstrips_strips[r], st, true,
+                                          G.tmaps));
+          FAP_CUDA(fapk::launch_fw_strips(pred, G.rests[r], G.rests_nseg[r], G.rests_strips[r], st, true,
+                                          G.tmaps));
         } else {
           FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
           FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
@@ -1350,6 +1386,9 @@ int check_status(fap_engine *e) {
     if (h & fapk::kErrSsspCap) return set_error(FAP_ERR_NOT_CONVERGED, "SSSP reached its iteration cap");
     return set_error(FAP_ERR_INVALID, "a kernel saw an out-of-range index");
   }
+  unsigned t = 0;
+  FAP_CUDA(fapk::tma_status(&t, true));
+  if (t) return set_error(FAP_ERR_CUDA, "a bulk tensor copy of the Floyd-Warshall tiles did not complete");
   return FAP_OK;
 }
 
@@ -2189,6 +2228,26 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb), ors(maxnb), ops(maxnb);
   std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), nr2(maxnb), sr2(maxnb), nrs(maxnb),
       srs(maxnb), nps(maxnb), sps(maxnb);
+  // tensor-map pairs of the matrices that meet the copy unit's alignment
+  // rules (16-byte base and row stride); the others keep per-thread copies
+  std::vector<int32_t> tmap1(count, 0);
+  size_t o_tmaps = 0;
+  bool has_tmaps = false;
+  {
+    std::vector<TmapBlob> maps;
+    for (int32_t b = 0; b < count; b++) {
+      TmapBlob two[2];
+      if (sizes[b] > Bk && fapk::encode_fw_tmaps(two, D[b], pred ? P[b] : nullptr, ld[b], sizes[b], sizes[b])) {
+        tmap1[b] = (int32_t)(maps.size() / 2) + 1;
+        maps.push_back(two[0]);
+        maps.push_back(two[1]);
+      }
+    }
+    if (!maps.empty()) {
+      o_tmaps = tb.add(maps.data(), maps.size());
+      has_tmaps = true;
+    }
+  }
   for (int r = 0; r < maxnb; r++) {
     std::vector<FwDiagJob> dj;
     std::vector<MpSegment> ps, rs, r2s, rss, pss;
@@ -2208,7 +2267,7 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
         MpSegment a, c, rest;
         int t1, t2, t3;
         fw_segments(D[b], pred ? P[b] : nullptr, ld[b], sizes[b], r, a, c, rest, t1, t2, t3,
-                    dtype == FAP_DTYPE_F32);
+                    dtype == FAP_DTYPE_F32, tmap1[b]);
         a.tile_begin = pt;
         pt += t1;
         ps.push_back(a);
@@ -2266,6 +2325,7 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   if ((rc = e->small.ensure(std::max<size_t>(tb.bytes.size(), 64))) != FAP_OK) return rc;
   FAP_CUDA(cudaMemcpyAsync(e->small.p, tb.bytes.data(), tb.bytes.size(), cudaMemcpyHostToDevice, st));
   unsigned char *base = static_cast<unsigned char *>(e->small.p);
+  const void *tmaps = has_tmaps ? static_cast<const void *>(base + o_tmaps) : nullptr;
   bool packed = false;
   if (!f32) {
     // a finite shortest distance is at most (size - 1) * the largest entry
@@ -2285,15 +2345,15 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
       FAP_CUDA(cudaEventRecord(e->ev_fw[0], st));
       FAP_CUDA(cudaStreamWaitEvent(e->side, e->ev_fw[0], 0));
       FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + or2[r]), nr2[r],
-                                      sr2[r], e->side));
+                                      sr2[r], e->side, false, tmaps));
       FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
     } else {
       FAP_CUDA(fapk::launch_fw_diag(f32, pred, djobs, nd[r], st));
       if (f32) {  // panels, then the remaining tiles, in the strip form
         FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ops[r]), nps[r],
-                                        sps[r], st, true));
+                                        sps[r], st, true, tmaps));
         FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ors[r]), nrs[r],
-                                        srs[r], st, true));
+                                        srs[r], st, true, tmaps));
       } else {
         FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r],
                                             tp[r], packed, st));

@@ -72,6 +72,11 @@ struct MpSegment {
   const int32_t *Fp;
   int64_t ldf;
   int32_t part, local0;
+  // Floyd-Warshall strips: 1 + the index of the matrix's tensor-map pair in
+  // the launch's table (0: none, per-thread copies) and the first row of B
+  // (the pivot block row) in the matrix.
+  int32_t tmap1;
+  int32_t b_row0;
 };
 
 // FW diagonal-block job: close the 64x64 pivot block of one matrix.

@@ -37,9 +37,20 @@ int minplus_strip_class_cols(int c);
 int minplus_strip_tiles();
 // Strip form of the FW remaining-tile phase (packed int32, or FP32 with
 // f32; init_from_c = 1, K <= 64): CTAs numbered by MpSegment::strip_begin,
-// tiles_y x ceil(tiles_x / fw_strip_tiles()) strips per segment.
+// tiles_y x ceil(tiles_x / fw_strip_tiles()) strips per segment.  tmaps:
+// device array of CUtensorMap pairs (distances, predecessors) indexed by
+// MpSegment::tmap1 - 1 (64-byte aligned; null: no segment uses one).
 cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                             cudaStream_t st, bool f32 = false);
+                             cudaStream_t st, bool f32 = false, const void *tmaps = nullptr);
+// Nonzero when a bulk tensor copy of the FW strips did not complete (the
+// strip was abandoned: the results are not valid); optionally reset.
+cudaError_t tma_status(unsigned *out, bool reset);
+// Encodes the tensor-map pair of one 4-byte matrix (rows x cols, row
+// stride ld elements) for the FW strips' 64 x 64 boxes into out[0] (d) and
+// out[1] (p, or d again when p is null); false when the matrix does not meet
+// the copy unit's alignment rules (16-byte base and row stride) or the
+// driver has no encoder.
+bool encode_fw_tmaps(void *out, const void *d, const void *p, int64_t ld, int rows, int cols);
 int fw_strip_tiles();
 int minplus_strip_max_k();   // largest K of the strip form
 // Segments go to the strip form in classes of K (one launch per class, each

@@ -30,6 +30,8 @@
 // follow P[i][j] = P[k][j] on strict improvement as in the reference.
 
 #include <cooperative_groups.h>
+#include <cuda.h>  // CUtensorMap (the type only; maps are encoded on the host)
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -67,6 +69,60 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_2() { asm volatile("cp.async.wait_group 2;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+// Bulk tensor copies (TMA): a 2-D box of a tensor map into shared memory,
+// completed on an mbarrier whose phase also waits for the expected bytes.
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// One arrival that also expects `bytes` of copies on the barrier's phase.
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// Waits for the phase with this parity to complete: false after `polls`
+// unsuccessful polls (each poll may suspend the thread for a short while).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int polls) {
+  const unsigned a = smem_u32(bar);
+  for (int i = 0; i < polls; i++) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// Orders this thread's earlier shared-memory accesses before later bulk
+// copies (the async proxy) into the same buffers.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+// The tensor map, copied to global memory by the host before the launch,
+// made visible to the copy unit.
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap *map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(map) : "memory");
+}
+// Box of `map` at column x, row y (x a multiple of 4 elements of 4 bytes:
+// 16-byte aligned) into dst (16-byte aligned shared memory).  Elements
+// outside the tensor arrive as zeros.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
 
 // Block index of list entry g of 0..nblocks-1 without block `skip` (and
 // `skip2`, when it is above `skip`), or of the one-block list `fix`; -1 past
@@ -1406,6 +1462,11 @@ __device__ __forceinline__ void fw_load_b(unsigned *dst, const unsigned *src, in
 // Work counter of the FW remaining-tile strips (diagnostics): add-mins
 // executed (steps run x the tile's 128 x TN outputs), summed per CTA.
 __device__ unsigned long long g_fw_counters[1];
+// Set when a bulk tensor copy of the FW strips did not complete within its
+// poll limit (the kernel then gives up on the strip; the host reports it).
+__device__ unsigned g_tma_status;
+constexpr int kTmaPolls = 1 << 22;
+constexpr unsigned kTmaBox = 64 * 64 * 4;  // bytes of one 64 x 64 box
 
 // F32: FP32 distances (value bits, "unreached" = the bits of 1e8): the
 // product keeps each output's value bits and the step (k + 1) of its last
@@ -1414,22 +1475,48 @@ __device__ unsigned long long g_fw_counters[1];
 // with the predecessor of that step -- the same result as updating the
 // current value step by step.  TN = 64.  (Two steps per pass, as in the
 // strip min-plus, measured the same here and spills more.)
+// TMA: when the segment's matrix has a tensor-map pair (tmaps[2 (tmap1 - 1)]
+// for the distances, + 1 for the predecessors: 64 x 64 boxes of 4-byte
+// elements, x = column, y = row), thread 0 stages the tile's C (two boxes),
+// B's predecessors and, for packed keys, B itself with bulk tensor copies on
+// three mbarriers (the two B buffers, C with the predecessors); the FP32 B
+// tile keeps its swizzled layout through per-thread copies.  Without a map
+// the per-thread asynchronous copies stage everything.
 template <bool PRED, int TN, bool F32 = false>
 __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
-    mp_fwstrip_kernel(const MpSegment *__restrict__ segs, int nseg) {
+    mp_fwstrip_kernel(const MpSegment *__restrict__ segs, int nseg, const CUtensorMap *__restrict__ tmaps) {
   static_assert(!F32 || TN == 64, "the FP32 form uses 64-column tiles");
   constexpr int CH = TN / 64;   // 64-column blocks of a tile
   constexpr int TPR = TN / 4;   // threads per row in the row-wise copies
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // (128-byte aligned: the bulk tensor copies' destinations are the B, Bp
+  // and C arrays, whose offsets are multiples of 16 KB)
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   FwStripSmem<TN> &sm = *reinterpret_cast<FwStripSmem<TN> *>(smem_raw);
   __shared__ MpSegment seg;
   __shared__ unsigned s_kmask[2][2];  // rows k of B with a finite entry (per tile parity)
   __shared__ unsigned s_amask[2];     // columns k of A with a finite entry (per strip)
-  if (threadIdx.x == 0) seg = find_strip_segment(segs, nseg, blockIdx.x);
+  __shared__ __align__(8) unsigned long long s_mbar[3];  // TMA: B buffers 0 and 1; C + B's predecessors
+  if (threadIdx.x == 0) {
+    seg = find_strip_segment(segs, nseg, blockIdx.x);
+    mbar_init(&s_mbar[0], 1);
+    mbar_init(&s_mbar[1], 1);
+    mbar_init(&s_mbar[2], 1);
+    mbar_init_fence();
+  }
   if (threadIdx.x < 4) (&s_kmask[0][0])[threadIdx.x] = 0u;
   if (threadIdx.x < 2) s_amask[threadIdx.x] = 0u;
   __syncthreads();
   const MpSegment &s = seg;
+  const CUtensorMap *tmap_d = (TN == 64 && tmaps != nullptr && s.tmap1 > 0) ? tmaps + 2 * (s.tmap1 - 1) : nullptr;
+  // (uniform over the CTA; the alignment tests only guard the copies' rules:
+  // 128-byte shared destinations, 64-byte tensor maps)
+  const bool tma = tmap_d != nullptr && (smem_u32(smem_raw) & 127u) == 0 &&
+                   (reinterpret_cast<uintptr_t>(tmap_d) & 63) == 0;
+  const bool tma_b = tma && !F32;
+  if (tma && threadIdx.x == 0) {
+    tmap_acquire(tmap_d);
+    if (PRED) tmap_acquire(tmap_d + 1);
+  }
   const int sx = fw_strips_x(s);
   const int local = blockIdx.x - s.strip_begin;
   const int tyt = local / sx;
@@ -1465,8 +1552,17 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
     else
       *d = INF;
   }
+  // B of a tile by TMA (thread 0): one box of pivot rows b_row0.. over the
+  // tile's column block, or an arrival without bytes when it has none.
+  auto tma_issue_b = [&](int b, int2 c) {
+    mbar_expect_tx(&s_mbar[b], c.x >= 0 ? kTmaBox : 0u);
+    if (c.x >= 0) tma_load_2d(&sm.B[b][0][0], tmap_d, c.x, s.b_row0, &s_mbar[b]);
+  };
   int2 cb = col_bases(jt0);
-  fw_load_b<TN, F32>(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
+  if (!tma_b)
+    fw_load_b<TN, F32>(&sm.B[0][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N, cb, vec_b, INF);
+  else if (threadIdx.x == 0)
+    tma_issue_b(0, cb);
   cp_async_commit();
   // The epilogue's view of C in registers (the descriptor is in shared memory).
   unsigned *const c_mat = static_cast<unsigned *>(s.C);
@@ -1477,12 +1573,18 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
 
   for (int jt = jt0; jt < jt1; jt++) {
     const int buf = (jt - jt0) & 1;
+    const unsigned use = (unsigned)(jt - jt0);  // tiles so far: B[buf] is on use >> 1, C on use
     cb = col_bases(jt);
-    if (jt + 1 < jt1)
-      fw_load_b<TN, F32>(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
-                col_bases(jt + 1), vec_b, INF);
+    if (jt + 1 < jt1) {
+      if (!tma_b)
+        fw_load_b<TN, F32>(&sm.B[buf ^ 1][0][0], static_cast<const unsigned *>(s.B), s.ldb, s.K, s.N,
+                  col_bases(jt + 1), vec_b, INF);
+      else if (threadIdx.x == 0)
+        tma_issue_b(buf ^ 1, col_bases(jt + 1));
+    }
     cp_async_commit();
     cp_async_wait_1();  // A and this tile's B have landed
+    const bool b_ok = !tma_b || mbar_wait(&s_mbar[buf], (use >> 1) & 1u, kTmaPolls);
     if (jt == jt0)  // A keys; a warp converts 32 entries of one step k and marks finite ones
       for (int idx = threadIdx.x; idx < kBlk * kTile; idx += kThreads) {
         const unsigned v = (&sm.A[0][0])[idx];
@@ -1498,6 +1600,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
         uint4 *p = reinterpret_cast<uint4 *>(&sm.B[buf][kk][j]);
         const unsigned idx = (unsigned)kk + 1u;
         uint4 v = *p;
+        if (tma_b) {  // steps past K and columns past N: the box brought other rows or zeros
+          const int col = cb.x + j;
+          const bool row_ok = cb.x >= 0 && kk < s.K;
+          if (!row_ok || col >= s.N) v.x = INF;
+          if (!row_ok || col + 1 >= s.N) v.y = INF;
+          if (!row_ok || col + 2 >= s.N) v.z = INF;
+          if (!row_ok || col + 3 >= s.N) v.w = INF;
+        }
         const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < FIN;
         if (!F32) {
           v.x = (min(v.x, kPackH) << kIdxBits) | idx;
@@ -1513,9 +1623,26 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       }
       if (threadIdx.x < 2) s_kmask[buf ^ 1][threadIdx.x] = 0u;  // for the next tile
     }
-    __syncthreads();
+    if (__syncthreads_or(!b_ok)) {  // a B copy never completed: give up on the strip
+      if (threadIdx.x == 0) atomicOr(&g_tma_status, 1u);
+      mbar_wait(&s_mbar[buf], (use >> 1) & 1u, kTmaPolls);
+      if (jt + 1 < jt1) mbar_wait(&s_mbar[buf ^ 1], ((use + 1) >> 1) & 1u, kTmaPolls);
+      cp_async_wait_0();
+      return;
+    }
     // Stage this tile's C behind the DPX loop.
-    {
+    if (tma) {
+      // C's two 64-row boxes and B's predecessors (rows b_row0..), whatever
+      // lies outside the matrix arriving as zeros: the epilogue stores no
+      // such output and reads only predecessors of steps below K.
+      if (threadIdx.x == 0) {
+        const bool c0 = cb.x >= 0 && rbase0 >= 0, c1 = cb.x >= 0 && rbase1 >= 0, bp = PRED && cb.x >= 0;
+        mbar_expect_tx(&s_mbar[2], (c0 ? kTmaBox : 0u) + (c1 ? kTmaBox : 0u) + (bp ? kTmaBox : 0u));
+        if (c0) tma_load_2d(&sm.C[0][0], tmap_d, cb.x, rbase0, &s_mbar[2]);
+        if (c1) tma_load_2d(&sm.C[kBlk][0], tmap_d, cb.x, rbase1, &s_mbar[2]);
+        if (bp) tma_load_2d(&sm.Bp[0][0], tmap_d + 1, cb.x, s.b_row0, &s_mbar[2]);
+      }
+    } else {
       const int j = (threadIdx.x % TPR) * 4;
       const int cbj = (j >> 6) ? cb.y : cb.x;
       const int col = cbj + (j & 63);
@@ -1538,8 +1665,8 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       if (PRED)
         fw_load_b<TN>(reinterpret_cast<unsigned *>(&sm.Bp[0][0]), reinterpret_cast<const unsigned *>(s.Bp),
                       s.ldbp, s.K, s.N, cb, vec_bp, 0xffffffffu);
-      cp_async_commit();
     }
+    cp_async_commit();
 
     unsigned acc[8][4 * CH];
     int arg[8][4 * CH];  // F32: step (k + 1) of the last strict improvement, 0: none
@@ -1628,7 +1755,14 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       }
     }
     cp_async_wait_0();
-    __syncthreads();  // C and the predecessors staged by every thread
+    const bool c_ok = !tma || mbar_wait(&s_mbar[2], use & 1u, kTmaPolls);
+    if (__syncthreads_or(!c_ok)) {  // C and the predecessors staged (by every thread, or the copy unit)
+      if (threadIdx.x == 0) atomicOr(&g_tma_status, 1u);
+      mbar_wait(&s_mbar[2], use & 1u, kTmaPolls);
+      if (jt + 1 < jt1 && tma_b) mbar_wait(&s_mbar[buf ^ 1], ((use + 1) >> 1) & 1u, kTmaPolls);
+      cp_async_wait_0();
+      return;
+    }
 
     // Epilogue: C joins with index 0; only strict improvements are stored.
 #pragma unroll
@@ -1661,7 +1795,10 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
         }
       }
     }
-    __syncthreads();  // C, B[buf] and the predecessors are free again
+    // C, B[buf] and the predecessors are free again (the fence orders this
+    // thread's reads and writes of them before the bulk copies that refill them)
+    if (tma) fence_proxy_async_smem();
+    __syncthreads();
   }
   cp_async_wait_0();
   if (threadIdx.x == 0 && n_work > 0) atomicAdd(&g_fw_counters[0], n_work);
@@ -2135,11 +2272,12 @@ cudaError_t launch_strip_t(const MpSegment *d_segs, int nseg, int strips, int ks
 }
 
 template <bool PRED, bool F32>
-cudaError_t launch_fwstrip_t(const MpSegment *d_segs, int nseg, int strips, cudaStream_t st) {
+cudaError_t launch_fwstrip_t(const MpSegment *d_segs, int nseg, int strips, cudaStream_t st,
+                             const void *tmaps) {
   if (strips <= 0 || nseg <= 0) return cudaSuccess;
   ++launch_count();
-  mp_fwstrip_kernel<PRED, kFwStripTN, F32>
-      <<<strips, kThreads, sizeof(FwStripSmem<kFwStripTN>), st>>>(d_segs, nseg);
+  mp_fwstrip_kernel<PRED, kFwStripTN, F32><<<strips, kThreads, sizeof(FwStripSmem<kFwStripTN>), st>>>(
+      d_segs, nseg, static_cast<const CUtensorMap *>(tmaps));
   return cudaGetLastError();
 }
 
@@ -2187,12 +2325,59 @@ cudaError_t launch_minplus_strips(bool pred, const MpSegment *d_segs, int nseg, 
 int minplus_strip_tiles() { return kStripTiles; }
 
 cudaError_t launch_fw_strips(bool pred, const MpSegment *d_segs, int nseg, int strips,
-                             cudaStream_t st, bool f32) {
+                             cudaStream_t st, bool f32, const void *tmaps) {
   if (f32)
-    return pred ? launch_fwstrip_t<true, true>(d_segs, nseg, strips, st)
-                : launch_fwstrip_t<false, true>(d_segs, nseg, strips, st);
-  return pred ? launch_fwstrip_t<true, false>(d_segs, nseg, strips, st)
-              : launch_fwstrip_t<false, false>(d_segs, nseg, strips, st);
+    return pred ? launch_fwstrip_t<true, true>(d_segs, nseg, strips, st, tmaps)
+                : launch_fwstrip_t<false, true>(d_segs, nseg, strips, st, tmaps);
+  return pred ? launch_fwstrip_t<true, false>(d_segs, nseg, strips, st, tmaps)
+              : launch_fwstrip_t<false, false>(d_segs, nseg, strips, st, tmaps);
+}
+
+// The driver's tensor-map encoder, looked up once through the runtime (the
+// library does not link the driver library itself); null when unavailable.
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      (void)cudaGetLastError();
+      f = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+bool encode_fw_tmaps(void *out, const void *d, const void *p, int64_t ld, int rows, int cols) {
+  static_assert(sizeof(CUtensorMap) == 128, "a tensor map is 128 bytes");
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+  if (!enc || !d || rows <= 0 || cols <= 0 || ((ld * 4) & 15) != 0 ||
+      (reinterpret_cast<uintptr_t>(d) & 15) != 0 || (p && (reinterpret_cast<uintptr_t>(p) & 15) != 0))
+    return false;
+  CUtensorMap *m = static_cast<CUtensorMap *>(out);
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
+  const cuuint32_t box[2] = {64, 64};
+  const cuuint32_t elem[2] = {1, 1};
+  for (int i = 0; i < 2; i++) {
+    void *base = const_cast<void *>(i == 1 && p ? p : d);
+    if (enc(&m[i], CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
+}
+
+cudaError_t tma_status(unsigned *out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_tma_status, sizeof(unsigned));
+  if (e == cudaSuccess && reset && *out) {
+    const unsigned zero = 0;
+    e = cudaMemcpyToSymbol(g_tma_status, &zero, sizeof(unsigned));
+  }
+  return e;
 }
 int fw_strip_tiles() { return kFwStripTiles; }
 int minplus_strip_max_k() { return kStripMaxK; }
