@@ -1488,10 +1488,12 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
   static_assert(!F32 || TN == 64, "the FP32 form uses 64-column tiles");
   constexpr int CH = TN / 64;   // 64-column blocks of a tile
   constexpr int TPR = TN / 4;   // threads per row in the row-wise copies
-  // (128-byte aligned: the bulk tensor copies' destinations are the B, Bp
-  // and C arrays, whose offsets are multiples of 16 KB)
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  FwStripSmem<TN> &sm = *reinterpret_cast<FwStripSmem<TN> *>(smem_raw);
+  // (a name of its own: the other kernels' dynamic shared memory, under
+  // one name, is declared 16-byte aligned; the bulk tensor copies want
+  // 128-byte aligned destinations, and B, Bp and C start at multiples of
+  // 16 KB of this array)
+  extern __shared__ __align__(128) unsigned char fw_smem[];
+  FwStripSmem<TN> &sm = *reinterpret_cast<FwStripSmem<TN> *>(fw_smem);
   __shared__ MpSegment seg;
   __shared__ unsigned s_kmask[2][2];  // rows k of B with a finite entry (per tile parity)
   __shared__ unsigned s_amask[2];     // columns k of A with a finite entry (per strip)
@@ -1510,7 +1512,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
   const CUtensorMap *tmap_d = (TN == 64 && tmaps != nullptr && s.tmap1 > 0) ? tmaps + 2 * (s.tmap1 - 1) : nullptr;
   // (uniform over the CTA; the alignment tests only guard the copies' rules:
   // 128-byte shared destinations, 64-byte tensor maps)
-  const bool tma = tmap_d != nullptr && (smem_u32(smem_raw) & 127u) == 0 &&
+  const bool tma = tmap_d != nullptr && (smem_u32(fw_smem) & 127u) == 0 &&
                    (reinterpret_cast<uintptr_t>(tmap_d) & 63) == 0;
   const bool tma_b = tma && !F32;
   if (tma && threadIdx.x == 0) {
