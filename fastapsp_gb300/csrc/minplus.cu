@@ -1289,6 +1289,21 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
       // 4-byte streaming stores of a row writes 64 consecutive bytes per
       // half-warp, whatever the alignment of the row.  The value is at most
       // "unreached"; step idx 0 reads predecessor -1.
+      if (nown == 0 && colbase + TN <= n_cols) {  // (uniform) no own column, every column inside
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          const int rr = (r >> 2) * kBlk + (r & 3);
+          if (row0 + ty * 4 + rr >= m_rows) continue;
+          unsigned *cq = c_thr + rr * ldc + colbase + tx;
+          int32_t *pq = PRED ? p_thr + rr * ldcp + colbase + tx : nullptr;
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            __stcs(cq + 16 * c, acc[r][c]);
+            if (PRED) __stcs(pq + 16 * c, Bps[arg[r][c] * TN + tx + 16 * c]);
+          }
+        }
+        continue;
+      }
       unsigned ownm = 0;  // bit c: column tx + 16 c is the part's own
       if (nown > 0) {
 #pragma unroll
