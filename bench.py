@@ -301,10 +301,10 @@ def run_solve(args, name, rank, world, local_rank):
     # add-min peaks from registers, measured in this run: int32 DPX add-min,
     # and the form the min-plus runs (int32 with argmin, or FP32 with argmin)
     # (FP32: the kernels' own form, add-mins in groups of four steps keeping
-    # the group of the last strict improvement, mode 10; int32: packed keys,
+    # the group of the last strict improvement, mode 12; int32: packed keys,
     # one DPX add-min each, mode 0; mode 3 is the one-step FP32 form)
     peak_dpx = eng_ctx_peak(fap, dev, 0)
-    peak_mp = eng_ctx_peak(fap, dev, 10 if f32 else 0)
+    peak_mp = eng_ctx_peak(fap, dev, 12 if f32 else 0)
     peak_fw = peak_mp
     peak_f32_step = eng_ctx_peak(fap, dev, 3) if f32 else None
 
@@ -448,7 +448,7 @@ def run_solve(args, name, rank, world, local_rank):
                 "unit": "Gaddmin/s", "frac": rate(executed, ph["min_plus"]) / peak_mp,
                 "dense_addmins_per_launch": addmin_mp,
                 "strip_tiles": mpc["tiles"], "tiles_without_active_step": mpc["empty_tiles"],
-                "peak_source": ("fap_addmin_peak mode 10 (FP32 add-mins in groups of four steps keeping the "
+                "peak_source": ("fap_addmin_peak mode 12 (FP32 add-mins in groups of four steps keeping the "
                                 "group of the last strict improvement, the kernel's form)" if f32 else
                                 "fap_addmin_peak mode 0 (int32 DPX add-min on packed keys, the kernel's form)")
                                + " from registers, measured in this run",
@@ -463,7 +463,7 @@ def run_solve(args, name, rank, world, local_rank):
                         "dense_equivalent_rate": rate(addmin_fw, ph["floyd"]) / 1e9,
                         "note": "executed add-mins (fap_fw_counters: the remaining-tile strips' device counter "
                                 "plus the pivot or tile launches' block products) per FW phase time, against "
-                                + ("fap_addmin_peak mode 10 (FP32 add-mins in groups of four keeping the "
+                                + ("fap_addmin_peak mode 12 (FP32 add-mins in groups of four keeping the "
                                    "group of the last strict improvement)" if f32 else
                                    "fap_addmin_peak mode 0 (int32 DPX add-min)")},
         "roofline_sssp": {"bound": "hbm", "achieved": rate(sssp_bytes, ph["sssp"]) / 1e9, "peak": hbm,

@@ -2467,7 +2467,7 @@ int fap_backward_dense(fap_engine *e, int32_t count, const int32_t *sizes, int32
 }
 
 int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s) {
-  if (!e || !ops_per_s || mode < 0 || mode > 11) return set_error(FAP_ERR_INVALID, "fap_addmin_peak: bad arguments");
+  if (!e || !ops_per_s || mode < 0 || mode > 12) return set_error(FAP_ERR_INVALID, "fap_addmin_peak: bad arguments");
   std::lock_guard<std::mutex> lk(e->mu);
   DeviceGuard dg(e->device);
   FAP_CUDA(fapk::measure_addmin_peak(mode, e->sm_count, ops_per_s));

@@ -823,11 +823,11 @@ __device__ __forceinline__ void strip_addmin(unsigned &acc, int &arg, unsigned a
 // step of the last strict improvement in the tagged group: its first step
 // whose sum equals the final value, since every earlier step's sum is above
 // it (strip_resolve_f32 finds it after the loop).  Four FP32 adds, then
-// either a 3-input and a 2-input minimum, a compare and two selects, or
-// (MIN3ACC) two 3-input minimums with the current value as an input, a
-// compare and one select: fewer ALU instructions, but the current value and
-// the new one are live together, which cost the min-plus (at 128 registers a
-// thread) more in spills than it saved and made the FW tiles faster.
+// (MIN3ACC, both strip kernels) two 3-input minimums with the current value
+// as an input, a compare and one select, or a 3-input and a 2-input minimum,
+// a compare and two selects: one ALU instruction more, but the old and the
+// new value are not live together (the min-plus took that form while its
+// epilogue still spilled at 128 registers a thread).
 template <bool MIN3ACC>
 __device__ __forceinline__ void strip_addmin4_f32(unsigned &acc, int &tag, const unsigned a[4],
                                                   const unsigned b[4], int grp) {
@@ -959,7 +959,7 @@ __device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], in
         for (int r = 0; r < 4; r++)
 #pragma unroll
           for (int c = 0; c < 2; c++)
-            strip_addmin4_f32<false>(acc[h * 4 + r][ch * 2 + c], arg[h * 4 + r][ch * 2 + c], a[r], b[c], kk + 1);
+            strip_addmin4_f32<true>(acc[h * 4 + r][ch * 2 + c], arg[h * 4 + r][ch * 2 + c], a[r], b[c], kk + 1);
       }
     }
   }

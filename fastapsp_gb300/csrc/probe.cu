@@ -23,11 +23,13 @@
 //           select, 9 __vibmin_u32 (the single-step form of the FP32
 //           kernels)
 //   mode 10: FP32 add-mins in groups of four steps keeping the group of the
-//           last strict improvement (the FP32 strip kernels' dense loop):
-//           four adds, a 3-input and a 2-input minimum, one compare, two
-//           selects
+//           last strict improvement: four adds, a 3-input and a 2-input
+//           minimum, one compare, two selects
 //   mode 11: mode 10 with the four adds as two paired adds (add.f32x2) on
 //           operands held as step pairs
+//   mode 12: the groups of four as the FP32 strip kernels run them: four
+//           adds, two 3-input minimums with the current value as an input,
+//           one compare, one select
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
 #pragma unroll
         for (int c = 0; c < NC; c++) {
           unsigned v0, v1, v2, v3;
-          if (MODE == 10) {
+          if (MODE != 11) {
             v0 = __float_as_uint(__fadd_rn((float)a[0][r], (float)b[0][c]));
             v1 = __float_as_uint(__fadd_rn((float)a[1][r], (float)b[1][c]));
             v2 = __float_as_uint(__fadd_rn((float)a[2][r], (float)b[2][c]));
@@ -110,11 +112,17 @@ __global__ void __launch_bounds__(256) addmin_peak_kernel(unsigned *out, int ite
             v0 = __float_as_uint(p01.x), v1 = __float_as_uint(p01.y);
             v2 = __float_as_uint(p23.x), v3 = __float_as_uint(p23.y);
           }
-          const unsigned t = min(__vimin3_u32(v0, v1, v2), v3);
           const unsigned ac = __float_as_uint((float)acc[r][c]);
-          const bool imp = t < ac;
-          acc[r][c] = (T)__uint_as_float(imp ? t : ac);
-          arg[r][c] = imp ? grp : arg[r][c];
+          if (MODE == 12) {
+            const unsigned na = __vimin3_u32(ac, __vimin3_u32(v0, v1, v2), v3);
+            arg[r][c] = na != ac ? grp : arg[r][c];
+            acc[r][c] = (T)__uint_as_float(na);
+          } else {
+            const unsigned t = min(__vimin3_u32(v0, v1, v2), v3);
+            const bool imp = t < ac;
+            acc[r][c] = (T)__uint_as_float(imp ? t : ac);
+            arg[r][c] = imp ? grp : arg[r][c];
+          }
         }
     } else if constexpr (MODE == 4 || MODE == 5) {
 #pragma unroll
@@ -228,7 +236,8 @@ cudaError_t measure_addmin_peak(int mode, int sm_count, double *ops_per_s) {
       case 8: e = run_mode<8>(buf, blocks, iters, 0); break;
       case 9: e = run_mode<9>(buf, blocks, iters, 0); break;
       case 10: e = run_mode<10>(buf, blocks, iters, 0); break;
-      default: e = run_mode<11>(buf, blocks, iters, 0); break;
+      case 11: e = run_mode<11>(buf, blocks, iters, 0); break;
+      default: e = run_mode<12>(buf, blocks, iters, 0); break;
     }
     cudaEventRecord(b, 0);
     if (e != cudaSuccess) break;

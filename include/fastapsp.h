@@ -401,8 +401,10 @@ int fap_sssp_stats(fap_engine *e, uint64_t *out5);
  * as __vibmin_s32 (6), a compare and two predicated moves (7), a float
  * compare, fminf and a select (8), __vibmin_u32 (9); 10: FP32 add-mins in
  * groups of four steps keeping the group of the last strict improvement
- * (the FP32 strip kernels' dense loop); 11: mode 10 with paired adds
- * (add.f32x2). */
+ * (a 3-input and a 2-input minimum, a compare, two selects); 11: mode 10
+ * with paired adds (add.f32x2); 12: the groups of four as the FP32 strip
+ * kernels run them (two 3-input minimums over the current value, a compare,
+ * one select). */
 int fap_addmin_peak(fap_engine *e, int32_t mode, double *ops_per_s);
 
 #ifdef __cplusplus

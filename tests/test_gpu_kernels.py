@@ -248,3 +248,15 @@ def test_speed_options_reject_unsupported_widths(gpu):
             with pytest.raises(gpu._lib.FapError):
                 eng.set_option(opt, bad)
             assert eng.get_option(opt) == good
+
+
+def test_addmin_peak_probe_modes(ctx):
+    """The register-only add-min probe (the roofline denominator) runs every
+    form and rejects unknown ones; the DPX form outruns the forms that keep
+    an index beside each value."""
+    rates = {m: ctx.addmin_peak(m) for m in range(13)}
+    assert all(r > 1e11 for r in rates.values()), rates
+    assert rates[0] > rates[3] and rates[12] > rates[3]
+    from fastapsp_gb300._lib import FapError
+    with pytest.raises(FapError):
+        ctx.addmin_peak(13)
