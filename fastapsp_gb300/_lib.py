@@ -33,6 +33,7 @@ OPT_TILE_COLS = 5
 OPT_SSSP_METHOD = 6
 OPT_HOST_RESULTS = 7
 OPT_INT32_FORM = 8
+OPT_HOST_GROUP_MB = 9
 INF_I32 = 1 << 30
 
 _i32 = C.c_int32

@@ -106,6 +106,10 @@ struct Plan {
   // group on the copy stream as each group finishes (null: none).
   void *hdist = nullptr;
   int32_t *hpred = nullptr;
+  // Staged host results in two slots of dist/pred (ring_elems elements
+  // each): group g computes its rows in slot g % 2, after the copy-out of
+  // group g - 2 from that slot (0: every row at its own offset).
+  int64_t ring_elems = 0;
   std::vector<const void *> sig;  // engine work buffers the tables point into
   // device tables (one allocation)
   DevBuf tables;
@@ -166,6 +170,7 @@ struct Plan {
     bool mp_aligned = true;  // every strip segment's result rows start on 16-byte boundaries
     int max_sub = 0;  // largest part of the group (bound of the packed form)
     int64_t out_lo = 0, out_elems = 0;  // the group's result rows: elements [out_lo, out_lo + out_elems)
+    int64_t dev_lo = 0;                 // where they are computed in dist/pred (out_lo, or its slot)
   };
   std::vector<Group> groups;
   size_t fw_elems = 0;  // FW arena elements needed
@@ -228,6 +233,7 @@ struct fap_engine {
   int sssp_lanes_tuned = 0;  // the width the autotuner chose (0: none yet)
   int tile_cols = 0;       // min-plus strip tile columns: 64, 128, 0 = per class
   int host_results = 0;    // FAP_OPT_HOST_RESULTS: 0 staged when the device has room, 1 direct
+  double host_group_mb = 8192.0;  // FAP_OPT_HOST_GROUP_MB: result rows per group of a host-results solve
   int int32_form = 0;      // FAP_OPT_INT32_FORM: 0 packed keys when provably exact, 1 always wide
   int sssp_method = 0;     // FAP_OPT_SSSP_METHOD: 0 auto, 1 whole-graph search, 2 boundary graph where exact
   int sssp_method_tuned = 0;  // auto: what the first run's trial chose (1 search, 2 boundary graph)
@@ -258,6 +264,7 @@ struct fap_engine {
                                   // then [0] / [1] fork and join the min-plus classes
   cudaStream_t copy = nullptr;    // early copy-out of boundary rows (host results)
   cudaEvent_t ev_copy[2] = {};    // [0] SSSP rows written, [1] their copy-out done
+  cudaEvent_t ev_slot[2] = {};    // staged host results in two slots: slot s's last copy-out done
   // work buffers
   DevBuf fw_d, fw_p;           // FW matrices arena
   DevBuf sssp_scratch, sssp_bits;
@@ -599,6 +606,28 @@ int mp_strips_of(const MpSegment &s) {
   return ((s.M + T - 1) / T) * ((s.tiles_x + S - 1) / S);
 }
 
+// Groups of a batched plan whose results are copied to host rows:
+// consecutive parts (indices into `parts`) in groups of about 8 GB of rows
+// (at most 8 groups), so that the copy of one group's rows runs while the
+// next group computes.
+std::vector<std::vector<int>> host_groups(const fap_engine *e, const std::vector<int32_t> &parts,
+                                          bool pred) {
+  std::vector<std::vector<int>> groups;
+  int64_t rows = 0;
+  for (int p : parts) rows += e->ver_num[p];
+  const double bytes = (double)rows * e->n * 4 * (pred ? 2 : 1);
+  const int ng = (int)std::min<double>(8.0, std::max(1.0, std::ceil(bytes / (e->host_group_mb * (1 << 20)))));
+  const int64_t per = (rows + ng - 1) / ng;
+  int64_t acc = 0;
+  groups.emplace_back();
+  for (size_t i = 0; i < parts.size(); i++) {
+    if (acc >= per * (int64_t)groups.size() && !groups.back().empty()) groups.emplace_back();
+    groups.back().push_back((int)i);
+    acc += e->ver_num[parts[i]];
+  }
+  return groups;
+}
+
 // Builds the plan for `parts` (row offsets into dist/pred given per part),
 // grouped one part per group (plain) or all in one group (batched).
 int build_plan(fap_engine *e, Plan &pl) {
@@ -607,21 +636,7 @@ int build_plan(fap_engine *e, Plan &pl) {
   const int64_t n = e->n;
   std::vector<std::vector<int>> groups;
   if (batched && pl.hdist) {
-    // Results copied to host rows: consecutive parts in groups of about
-    // 8 GB of rows (at most 8 groups), so that the copy of one group's rows
-    // runs while the next group computes.
-    int64_t rows = 0;
-    for (int p : pl.parts) rows += e->ver_num[p];
-    const double bytes = (double)rows * n * 4 * (pl.pred ? 2 : 1);
-    const int ng = (int)std::min<double>(8.0, std::max(1.0, std::ceil(bytes / (8.0 * (1 << 30)))));
-    const int64_t per = (rows + ng - 1) / ng;
-    int64_t acc = 0;
-    groups.emplace_back();
-    for (size_t i = 0; i < pl.parts.size(); i++) {
-      if (acc >= per * (int64_t)groups.size() && !groups.back().empty()) groups.emplace_back();
-      groups.back().push_back((int)i);
-      acc += e->ver_num[pl.parts[i]];
-    }
+    groups = host_groups(e, pl.parts, pl.pred != nullptr);
   } else if (batched) {
     groups.emplace_back();
     for (size_t i = 0; i < pl.parts.size(); i++) groups[0].push_back((int)i);
@@ -670,10 +685,16 @@ int build_plan(fap_engine *e, Plan &pl) {
     std::vector<MpSegment> mps_cls[Plan::Group::kMaxCls], mps_wide;
     const int ncls = std::min(fapk::minplus_strip_classes(), (int)Plan::Group::kMaxCls);
     int maxnb = 0;
+    {
+      const int first = groups[g].front(), last = groups[g].back();
+      G.out_lo = pl.row_offs[first];
+      G.out_elems = pl.row_offs[last] + (int64_t)e->ver_num[pl.parts[last]] * n - G.out_lo;
+      G.dev_lo = pl.ring_elems > 0 ? (int64_t)(g & 1) * pl.ring_elems : G.out_lo;
+    }
     for (int idx : groups[g]) {
       int p = pl.parts[idx];
       int sub = e->ver_num[p], bdy = e->bdy_num[p], start = e->ver_offset[p];
-      int64_t roff = pl.row_offs[idx];
+      int64_t roff = pl.row_offs[idx] - G.out_lo + G.dev_lo;  // the part's rows in dist/pred
       int64_t boff = pl.bdist ? pl.brow_offs[idx] : roff;  // first boundary row
       for (int w = 0; w < 2; w++) {
         const int L = w == 0 ? pl.sssp_lanes : pl.sssp_lanes_alt;
@@ -728,11 +749,6 @@ int build_plan(fap_engine *e, Plan &pl) {
         if (c < ncls) mps_cls[c].push_back(s);
         else mps_wide.push_back(s);
       }
-    }
-    {
-      const int first = groups[g].front(), last = groups[g].back();
-      G.out_lo = pl.row_offs[first];
-      G.out_elems = pl.row_offs[last] + (int64_t)e->ver_num[pl.parts[last]] * n - G.out_lo;
     }
     G.nbatches = (int)batches.size();
     O.batches = tb.add(batches.data(), batches.size());
@@ -1134,13 +1150,20 @@ struct Issuer {
     const Plan::Group &G = pl.groups[g];
     FAP_CUDA(cudaEventRecord(e->ev_copy[0], st));
     FAP_CUDA(cudaStreamWaitEvent(e->copy, e->ev_copy[0], 0));
-    const size_t off = (size_t)G.out_lo * 4, bytes = (size_t)G.out_elems * 4;
-    FAP_CUDA(cudaMemcpyAsync(static_cast<char *>(pl.hdist) + off, static_cast<const char *>(pl.dist) + off,
+    const size_t off = (size_t)G.out_lo * 4, doff = (size_t)G.dev_lo * 4, bytes = (size_t)G.out_elems * 4;
+    FAP_CUDA(cudaMemcpyAsync(static_cast<char *>(pl.hdist) + off, static_cast<const char *>(pl.dist) + doff,
                              bytes, cudaMemcpyDeviceToHost, e->copy));
     if (pl.hpred)
       FAP_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(pl.hpred) + off,
-                               reinterpret_cast<const char *>(pl.pred) + off, bytes,
+                               reinterpret_cast<const char *>(pl.pred) + doff, bytes,
                                cudaMemcpyDeviceToHost, e->copy));
+    if (pl.ring_elems > 0) FAP_CUDA(cudaEventRecord(e->ev_slot[g & 1], e->copy));  // the slot is free again
+    return FAP_OK;
+  }
+  // Two-slot staging: group g's first launch waits until the copy-out of
+  // group g - 2 (the slot's previous rows) has finished.
+  int slot_free(size_t g) {
+    if (pl.ring_elems > 0 && g >= 2) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_slot[g & 1], 0));
     return FAP_OK;
   }
   int join() {
@@ -1156,6 +1179,7 @@ struct Issuer {
     const int c0 = fapk::launch_count();
     FAP_CUDA(rec(0));
     for (size_t g = 0; g < pl.groups.size(); g++) {
+      if ((rc = slot_free(g)) != FAP_OK) return rc;
       if ((rc = sssp(g)) != FAP_OK) return rc;
       if (g + 1 == pl.groups.size()) FAP_CUDA(rec(1));
       if ((rc = rest(g, g + 1 == pl.groups.size())) != FAP_OK) return rc;
@@ -1404,16 +1428,18 @@ std::vector<const void *> buffer_signature(const fap_engine *e) {
           reinterpret_cast<const void *>((intptr_t)e->sssp_method),
           reinterpret_cast<const void *>((intptr_t)e->int32_form),
           e->bg_tab.p,
-          reinterpret_cast<const void *>(dbits)};
+          reinterpret_cast<const void *>(dbits),
+          reinterpret_cast<const void *>((intptr_t)std::llround(e->host_group_mb * 1024.0))};
 }
 
 Plan *find_plan(fap_engine *e, int mode, void *dist, int32_t *pred,
                 const std::vector<int32_t> &parts, const std::vector<int64_t> &offs, void *bdist,
-                int32_t *bpred, void *hdist, int32_t *hpred) {
+                int32_t *bpred, void *hdist, int32_t *hpred, int64_t ring_elems) {
   const std::vector<const void *> sig = buffer_signature(e);
   for (auto &p : e->plans)
     if (p->mode == mode && p->dist == dist && p->pred == pred && p->parts == parts &&
         p->row_offs == offs && p->bdist == bdist && p->bpred == bpred && p->hdist == hdist &&
+        p->ring_elems == ring_elems &&
         p->hpred == hpred && p->sig == sig)
       return p.get();
   return nullptr;
@@ -1425,7 +1451,7 @@ Plan *find_plan(fap_engine *e, int mode, void *dist, int32_t *pred,
 int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vector<int32_t> &parts,
               const std::vector<int64_t> &offs, cudaStream_t st, void *bdist = nullptr,
               int32_t *bpred = nullptr, const std::vector<int64_t> &boffs = {}, void *hdist = nullptr,
-              int32_t *hpred = nullptr) {
+              int32_t *hpred = nullptr, int64_t ring_elems = 0) {
   int rc;
   // work buffers
   size_t fw_elems = 0;
@@ -1471,7 +1497,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
   int slots = std::min(std::max(max_batches, 1), max_sssp_slots(e, wide));
   if ((rc = ensure_sssp_scratch(e, slots, wide)) != FAP_OK) return rc;
 
-  Plan *pl = find_plan(e, mode, dist, pred, parts, offs, bdist, bpred, hdist, hpred);
+  Plan *pl = find_plan(e, mode, dist, pred, parts, offs, bdist, bpred, hdist, hpred, ring_elems);
   if (!pl) {
     if (e->plans.size() >= 8) e->plans.erase(e->plans.begin());
     auto np = std::make_unique<Plan>();
@@ -1485,6 +1511,7 @@ int run_parts(fap_engine *e, int mode, void *dist, int32_t *pred, const std::vec
     np->brow_offs = boffs;
     np->hdist = hdist;
     np->hpred = hpred;
+    np->ring_elems = ring_elems;
     np->sig = buffer_signature(e);
     np->sssp_lanes = lanes;
     np->sssp_lanes_alt = tune_lanes ? alt_lanes : 0;
@@ -1592,6 +1619,7 @@ int init_device(fap_engine *e, int device) {
   for (auto &ev : e->ev_fw) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   FAP_CUDA(cudaStreamCreateWithFlags(&e->copy, cudaStreamNonBlocking));
   for (auto &ev : e->ev_copy) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  for (auto &ev : e->ev_slot) FAP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   // status words: [0] error flags, [1]/[2] maxima for the packed-form bound
   FAP_CUDA(cudaMalloc(&e->d_status, 4 * sizeof(unsigned)));
   FAP_CUDA(cudaMemset(e->d_status, 0, 4 * sizeof(unsigned)));
@@ -1859,6 +1887,8 @@ int fap_destroy(fap_engine *e) {
       if (ev) cudaEventDestroy(ev);
     for (auto &ev : e->ev_copy)
       if (ev) cudaEventDestroy(ev);
+    for (auto &ev : e->ev_slot)
+      if (ev) cudaEventDestroy(ev);
     if (e->copy) cudaStreamDestroy(e->copy);
     if (e->stream) cudaStreamDestroy(e->stream);
     if (e->side) cudaStreamDestroy(e->side);
@@ -1966,19 +1996,36 @@ static int solve_common(fap_engine *e, const std::vector<int32_t> &parts, int64_
   } else {
     void *dd = dist;
     int32_t *dp = pred;
-    if (!dev_d) {
-      if ((rc = e->res_d.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
-      dd = e->res_d.p;
-    }
-    if (pred && !dev_p) {
-      if ((rc = e->res_p.ensure(std::max<size_t>(bytes, 4))) != FAP_OK) return rc;
-      dp = static_cast<int32_t *>(e->res_p.p);
-    }
     // Page-locked host rows (both, when there are predecessors): the plan
     // copies each group's rows as it finishes; otherwise one copy at the end.
     const bool plan_copies = !dev_d && hd && (pred == nullptr || (!dev_p && hp));
+    // With three or more groups (FP32, batched: every group runs start to
+    // end before the next) the device copy is two group-sized slots that the
+    // groups take in turn instead of all the rows: a quarter of the device
+    // memory on the 114,599-vertex graph, and less to allocate and free.
+    int64_t ring = 0;
+    size_t dbytes = bytes;
+    if (plan_copies && mode == FAP_MODE_BATCHED && e->f32()) {
+      const std::vector<std::vector<int>> hg = host_groups(e, parts, pred != nullptr);
+      if (hg.size() >= 3) {
+        for (const auto &grp : hg) {
+          int64_t rows = 0;
+          for (int i : grp) rows += e->ver_num[parts[i]];
+          ring = std::max(ring, rows * e->n);
+        }
+        dbytes = (size_t)ring * 2 * 4;
+      }
+    }
+    if (!dev_d) {
+      if ((rc = e->res_d.ensure(std::max<size_t>(dbytes, 4))) != FAP_OK) return rc;
+      dd = e->res_d.p;
+    }
+    if (pred && !dev_p) {
+      if ((rc = e->res_p.ensure(std::max<size_t>(dbytes, 4))) != FAP_OK) return rc;
+      dp = static_cast<int32_t *>(e->res_p.p);
+    }
     if (plan_copies) {
-      if ((rc = run_parts(e, mode, dd, dp, parts, offs, st, nullptr, nullptr, {}, dist, pred)) != FAP_OK)
+      if ((rc = run_parts(e, mode, dd, dp, parts, offs, st, nullptr, nullptr, {}, dist, pred, ring)) != FAP_OK)
         return rc;
     } else {
       if ((rc = run_parts(e, mode, dd, dp, parts, offs, st)) != FAP_OK) return rc;
@@ -2513,6 +2560,10 @@ int fap_set_option(fap_engine *e, int32_t option, double value) {
       if (value != 0.0 && value != 1.0) return set_error(FAP_ERR_INVALID, "int32 form must be 0 or 1");
       e->int32_form = (int)value;
       return FAP_OK;
+    case FAP_OPT_HOST_GROUP_MB:
+      if (!(value >= 1.0) || std::isinf(value)) return set_error(FAP_ERR_INVALID, "host group size must be >= 1 MB");
+      e->host_group_mb = value;
+      return FAP_OK;
     default:
       return set_error(FAP_ERR_INVALID, "unknown option");
   }
@@ -2528,6 +2579,7 @@ int fap_get_option(const fap_engine *e, int32_t option, double *value) {
     case FAP_OPT_TILE_COLS: *value = e->tile_cols; return FAP_OK;
     case FAP_OPT_SSSP_METHOD: *value = e->sssp_method ? e->sssp_method : e->sssp_method_tuned; return FAP_OK;
     case FAP_OPT_HOST_RESULTS: *value = e->host_results; return FAP_OK;
+    case FAP_OPT_HOST_GROUP_MB: *value = e->host_group_mb; return FAP_OK;
     case FAP_OPT_INT32_FORM: *value = e->int32_form; return FAP_OK;
     default: return set_error(FAP_ERR_INVALID, "unknown option");
   }

@@ -242,6 +242,13 @@ int fap_precondition(fap_engine *e);
  *                      result stays below 2^24 - 1, else on separate values
  *                      and steps (the wide form); 1 = always the wide form.
  *                      Same rows either way.
+ *   FAP_OPT_HOST_GROUP_MB results in page-locked host memory, batched solves:
+ *                      the parts are solved in groups of about this many MB
+ *                      of result rows (default 8192; at most 8 groups), each
+ *                      group's rows copied out while the next group computes.
+ *                      FP32 engines with three or more groups hold the
+ *                      device copy in two group-sized slots that the groups
+ *                      take in turn.  Same rows for any value.
  * Setting an option takes effect from the next solve. */
 #define FAP_OPT_SSSP_FP64 1
 #define FAP_OPT_SSSP_DELTA 2
@@ -251,6 +258,7 @@ int fap_precondition(fap_engine *e);
 #define FAP_OPT_SSSP_METHOD 6
 #define FAP_OPT_HOST_RESULTS 7
 #define FAP_OPT_INT32_FORM 8
+#define FAP_OPT_HOST_GROUP_MB 9
 int fap_set_option(fap_engine *e, int32_t option, double value);
 int fap_get_option(const fap_engine *e, int32_t option, double *value);
 

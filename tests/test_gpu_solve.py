@@ -143,6 +143,42 @@ def test_solve_into_page_locked_host_rows(gpu, name, mode, with_pred, direct):
                 assert torch.equal(ph, pd.cpu())
 
 
+@pytest.mark.parametrize("f32", [True, False])
+@pytest.mark.parametrize("with_pred", [True, False])
+def test_host_rows_in_groups_and_slots(gpu, f32, with_pred):
+    """Batched solves into page-locked host rows in many groups (about 1 MB
+    of rows each, capped at 8): the FP32 engine then stages the rows in two
+    slots that the groups take in turn, the int32 engine at their own
+    offsets.  Same rows as a device-resident solve, on the first run of the
+    plan and on a replay of its captured graph."""
+    from fastapsp_gb300 import graphs
+
+    if f32:
+        g, dtype, tdt = graphs.road_like(6000, seed=8), gpu.DTYPE_F32, torch.float32
+    else:
+        g, dtype, tdt = graphs.geometric_knn(n=6000, k=3, seed=8), gpu.DTYPE_I32, torch.int32
+    n = g.n
+    with gpu.Engine(n, g.row_offset, g.col_val, g.weight, 9, dtype=dtype) as eng:
+        dd = torch.empty((n, n), dtype=tdt, device="cuda")
+        pd = torch.empty((n, n), dtype=torch.int32, device="cuda") if with_pred else None
+        eng.solve(dd, pd, 1)
+        torch.cuda.synchronize()
+        eng.set_option(gpu._lib.OPT_HOST_GROUP_MB, 1)
+        assert eng.get_option(gpu._lib.OPT_HOST_GROUP_MB) == 1
+        dh = torch.full((n, n), 7, dtype=tdt).pin_memory()
+        ph = torch.full((n, n), 7, dtype=torch.int32).pin_memory() if with_pred else None
+        for _ in range(2):
+            dh.fill_(7)
+            if with_pred:
+                ph.fill_(7)
+            eng.solve(dh, ph, 1)
+            assert torch.equal(dh, dd.cpu())
+            if with_pred:
+                assert torch.equal(ph, pd.cpu())
+        with pytest.raises(gpu.FapError):
+            eng.set_option(gpu._lib.OPT_HOST_GROUP_MB, 0.5)
+
+
 def test_batched_solve_repeats_bit_for_bit(gpu):
     """The batched form's overlapped launches (FW lookahead on two streams)
     give the same distances and predecessors on every replay of the captured
