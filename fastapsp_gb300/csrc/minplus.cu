@@ -667,8 +667,8 @@ __global__ void __launch_bounds__(kThreads, 2)
 //   B[2][ks][TN] | Bp[1 + ks][TN] | colp[2][TN] | coll[2][TN] | ownidx[2][TN] |
 //   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
 // and, FP32 only, Ar[128][strip_bc_stride(kseg)] (A row-major) |
-// Bc[64][strip_bc_stride(kseg)]
-// (the current tile's B column-major).
+// Bq[ks / 4][64] (the current tile's B by step group: 16-byte unit (g, col)
+// holds steps 4g .. 4g + 3 of column col).
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
 // with the key's idx as it is (0 when unreached).
 // Work counters of the strip min-plus (diagnostics): [tiles, tiles with no
@@ -691,14 +691,14 @@ constexpr int kStripClassK[] = {48, kStripMaxK};
 constexpr int kStripClassTN[] = {64, 128};
 constexpr int kStripClasses = 2;
 
-// Row stride of the FP32 strip kernel's column-major copy of B for kseg
+// Row stride of the FP32 strip kernel's row-major copy of A for kseg
 // steps: kseg, or kseg + 4 when kseg / 4 is even, so that the stride in
 // 16-byte units is odd.
 __host__ __device__ constexpr int strip_bc_stride(int kseg) { return ((kseg >> 2) & 1) ? kseg : kseg + 4; }
 
 // Shared memory of the strip kernel with TN-column tiles, in bytes; F32 adds
-// the row-major copy of A ([128][ks + 4] at most) and the column-major copy
-// of B ([64][ks + 4] at most).
+// the row-major copy of A ([128][ks + 4] at most) and the step-group copy
+// of B ([ks / 4][64] 16-byte units, within [64][ks + 4] words).
 template <int TN, bool F32 = false>
 __host__ __device__ constexpr size_t strip_smem_bytes(int ks) {
   return ((size_t)2 * ks * TN + (size_t)(ks + 1) * TN + 6 * TN + (size_t)2 * kOwnCap * kTile +
@@ -771,12 +771,13 @@ __device__ __forceinline__ void strip_mark_rows(unsigned *kmask, int kk, bool fi
 // into keys (d << 7) | (k + 1), and sets bit k of kmask (a 128-bit mask in
 // shared memory) for every row k that has a finite entry in the tile.
 // F32 (TN = 64): the values stay (FP32 bits, "unreached" = the bits of 1e8);
-// the row bits are set and the values are also written to Bc, the tile's
-// column-major copy (column col at row col, stride bcs).  ks is a multiple of 4, so a warp's rows are all below ks or all at
-// or past it, and the warp's lanes run the loop together.
+// the row bits are set and the values are also written to Bq, the tile's
+// copy by step group (word 4 (g TN + col) + q is step 4g + q of column col).
+// ks is a multiple of 4, so a warp's rows are all below ks or all at or past
+// it, and the warp's lanes run the loop together.
 template <int TN, bool F32 = false>
 __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kmask,
-                                             unsigned *Bc = nullptr, int bcs = 0) {
+                                             unsigned *Bq = nullptr) {
   static_assert(TN == 64 || TN == 128, "row marks assume 16 or 32 lanes a row");
   constexpr int TPR = TN / 4;
   const int t = threadIdx.x;
@@ -787,10 +788,11 @@ __device__ __forceinline__ void strip_keys_b(unsigned *Bs, int ks, unsigned *kma
     uint4 v = *p;
     if (F32) {
       strip_mark_rows<TN>(kmask, kk, min(min(v.x, v.y), min(v.z, v.w)) < __float_as_uint(Dist<float>::inf()));
-      Bc[(j + 0) * bcs + kk] = v.x;  // column j + q is row j + q of the column-major copy
-      Bc[(j + 1) * bcs + kk] = v.y;
-      Bc[(j + 2) * bcs + kk] = v.z;
-      Bc[(j + 3) * bcs + kk] = v.w;
+      unsigned *q = Bq + ((kk >> 2) * TN + j) * 4 + (kk & 3);
+      q[0] = v.x;
+      q[4] = v.y;
+      q[8] = v.z;
+      q[12] = v.w;
       continue;
     }
     const bool fin = min(min(v.x, v.y), min(v.z, v.w)) < kPackH;
@@ -923,21 +925,24 @@ __device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&a
 
 // The same for the strip min-plus, from row-major copies of the operands:
 // Ar[128][ars] (row m's steps contiguous, ars = strip_bc_stride(kseg)) and
-// Bc, the tile's B column-major (column col at row col, stride bcs = ars).
+// Bq, the tile's B by step group (16-byte unit g * 64 + col: steps 4g ..
+// 4g + 3 of column col).
 // One 16-byte load gives a row's or a column's four steps of a group, so the
-// resolve takes two loads per output.  Both strides are odd in 16-byte
-// units: the eight rows of Bc that a 16-byte load phase reads (eight
-// consecutive columns) lie in eight different bank groups, and so do the two
-// rows of Ar (four apart) that a warp reads.  The thread's rows are r0 ..
-// r0 + 3 and r0 + 64 .. r0 + 67, its columns tx, tx + 16, tx + 32 and
-// tx + 48.  B operands load two columns at a time (24 operands live).
+// resolve takes two loads per output.  Eight consecutive columns of one step
+// group are eight consecutive units of Bq, in eight different bank groups,
+// and so they stay when the lanes' step groups differ (the resolve); Ar's
+// stride is odd in 16-byte units, so the two rows (four apart) that a warp
+// reads in the loop lie in different bank groups, and one row's different
+// step groups (the resolve) too, up to eight groups apart.  The thread's
+// rows are r0 .. r0 + 3 and r0 + 64 .. r0 + 67, its columns tx, tx + 16,
+// tx + 32 and tx + 48.  B operands load two columns at a time (24 operands
+// live).
 template <bool PRED>
 __device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], int (&arg)[8][4],
-                                                       const unsigned *Ar, int kseg, int r0,
-                                                       const unsigned *Bc, int bcs, int tx) {
-  const int ars = bcs;                   // Ar's row stride
+                                                       const unsigned *Ar, int ars, int kseg, int r0,
+                                                       const unsigned *Bq, int tx) {
   const unsigned *arow = Ar + r0 * ars;  // row r0 + m at arow + m * ars
-  const unsigned *bcol = Bc + tx * bcs;   // column tx + 16 c at bcol + c * 16 * bcs
+  const uint4 *bq = reinterpret_cast<const uint4 *>(Bq) + tx;  // (g, tx + 16 c) at bq[g * 64 + 16 c]
   for (int kk = 0; kk < kseg; kk += 4) {
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -952,7 +957,7 @@ __device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], in
         unsigned b[2][4];  // [column of the pair][step]
 #pragma unroll
         for (int c = 0; c < 2; c++) {
-          const uint4 v = *reinterpret_cast<const uint4 *>(bcol + (ch * 2 + c) * 16 * bcs + kk);
+          const uint4 v = bq[(kk >> 2) * 64 + (ch * 2 + c) * 16];
           b[c][0] = v.x, b[c][1] = v.y, b[c][2] = v.z, b[c][3] = v.w;
         }
 #pragma unroll
@@ -971,7 +976,7 @@ __device__ __forceinline__ void addmin_groups_rows_f32(unsigned (&acc)[8][4], in
         const int tag = arg[r][c];
         const int k0 = tag > 0 ? tag - 1 : 0;
         const uint4 av = *reinterpret_cast<const uint4 *>(arow + ((r >> 2) * kBlk + (r & 3)) * ars + k0);
-        const uint4 bv = *reinterpret_cast<const uint4 *>(bcol + c * 16 * bcs + k0);
+        const uint4 bv = bq[(k0 >> 2) * 64 + c * 16];
         const unsigned v0 = __float_as_uint(__fadd_rn(__uint_as_float(av.x), __uint_as_float(bv.x)));
         const unsigned v1 = __float_as_uint(__fadd_rn(__uint_as_float(av.y), __uint_as_float(bv.y)));
         const unsigned v2 = __float_as_uint(__fadd_rn(__uint_as_float(av.z), __uint_as_float(bv.z)));
@@ -1004,8 +1009,8 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
   unsigned *Fst = reinterpret_cast<unsigned *>(ownidx + 2 * TN);  // [kOwnCap][128 rows]
   int32_t *Fpst = reinterpret_cast<int32_t *>(Fst + kOwnCap * kTile);  // [kOwnCap][128 rows]
   unsigned *As = reinterpret_cast<unsigned *>(Fpst + kOwnCap * kTile);  // A^T [ks][128]
-  unsigned *Ar = As + ks * kTile;        // F32: A row-major [128][bcs]
-  unsigned *Bc = Ar + kTile * (ks + 4);  // F32: the tile's B column-major [64][bcs]
+  unsigned *Ar = As + ks * kTile;        // F32: A row-major [128][ars]
+  unsigned *Bq = Ar + kTile * (ks + 4);  // F32: the tile's B by step group [ks / 4][64][4]
   __shared__ MpSegment seg;
   __shared__ int s_own[2];                   // own columns of the tile (per tile parity)
   __shared__ int16_t s_ownlist[2][kOwnCap];  // their tile columns, by slot
@@ -1030,7 +1035,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
   const unsigned INF = F32 ? __float_as_uint(Dist<float>::inf()) : Dist<uint32_t>::inf();
   const int kseg = (s.K + 3) & ~3;  // this segment's K rounded up to 4 (<= ks)
-  const int bcs = strip_bc_stride(kseg);
+  const int ars = strip_bc_stride(kseg);  // F32: Ar's row stride
   const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
   const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
   const bool vec_c = vec_stores_ok<PRED>(s);
@@ -1099,7 +1104,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
       *d = INF;
     if (F32) {
       const int mr = idx / kseg, kr = idx - mr * kseg;
-      unsigned *dr = &Ar[mr * bcs + kr];
+      unsigned *dr = &Ar[mr * ars + kr];
       if (row0 + mr < s.M && kr < s.K)
         cp_async4(dr, static_cast<const unsigned *>(s.A) + (int64_t)(row0 + mr) * s.lda + kr);
       else
@@ -1132,7 +1137,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
         if (__any_sync(0xffffffffu, F32 ? v < INF : v < kPackH) && (threadIdx.x & 31) == 0)
           atomicOr(&s_amask[kk >> 5], 1u << (kk & 31));
       }
-    strip_keys_b<TN, F32>(Bcur, kseg, s_kmask[buf], Bc, bcs);
+    strip_keys_b<TN, F32>(Bcur, kseg, s_kmask[buf], Bq);
     // List the tile's own columns (threads 0..TN-1 copied their column's
     // flags; slots are taken in any order through a counter).
     if (threadIdx.x == 0) s_own[buf ^ 1] = 0;  // used by the next tile
@@ -1221,7 +1226,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
       // "unreached" on one side and never win).
       const bool grouped = F32 && CH == 1 && nact > 0 && 2 * nact >= kseg;
       if (grouped) {
-        if constexpr (F32 && CH == 1) addmin_groups_rows_f32<PRED>(acc, arg, Ar, kseg, ty * 4, Bc, bcs, tx);
+        if constexpr (F32 && CH == 1) addmin_groups_rows_f32<PRED>(acc, arg, Ar, ars, kseg, ty * 4, Bq, tx);
       } else if (nact == s.K && s.K > 0) {
         uint4 na0 = *reinterpret_cast<const uint4 *>(a_at(0));
         uint4 na1 = *reinterpret_cast<const uint4 *>(a_at(0) + kBlk);
