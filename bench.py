@@ -46,7 +46,7 @@ HBM_PEAK_FALLBACK = 6800.0
 # DRAM read+write bytes per algorithmic byte of the min-plus launch, from ncu
 # captures of the same kernel on smaller cases of each workload (scaled by the
 # output bytes, which grow with the work); None where no capture was taken.
-MP_TRAFFIC_PER_BYTE = {"c2": 1.136, "c4": 1.188, "c1": None}
+MP_TRAFFIC_PER_BYTE = {"c2": 1.136, "c4": 1.181, "c1": None}
 
 # Solve workloads: the synthetic graph, its part count, the engine's distance
 # type, the committed partition (tests/golden/partitions/make_partitions.py) and, for
