@@ -1804,9 +1804,13 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
           const int col = cbh + tx * 4 + q;
           const unsigned cq = q == 0 ? cv.x : q == 1 ? cv.y : q == 2 ? cv.z : cv.w;
           if constexpr (F32) {  // strict improvements only: ties keep the current value
+            // (the addresses from the descriptor in shared memory, read
+            // again after every barrier: with the register copies the
+            // compiler kept the rows' 64-bit offsets live across the tile
+            // loop, beside the 64 value and step registers, and spilled)
             if (!(acc[r][h * 4 + q] < cq) || col >= n_cols) continue;
-            c_mat[(int64_t)row * ldc + col] = acc[r][h * 4 + q];
-            if (PRED) p_mat[(int64_t)row * ldcp + col] = sm.Bp[arg[r][h * 4 + q] - 1][sc0 + q];
+            static_cast<unsigned *>(s.C)[(int64_t)row * s.ldc + col] = acc[r][h * 4 + q];
+            if (PRED) s.Cp[(int64_t)row * s.ldcp + col] = sm.Bp[arg[r][h * 4 + q] - 1][sc0 + q];
           } else {
             const unsigned key = min(min(cq, kPackH) << kIdxBits, acc[r][h * 4 + q]);
             const unsigned idx = key & kIdxMask;
