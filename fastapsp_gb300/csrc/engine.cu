@@ -139,16 +139,17 @@ struct Plan {
     std::vector<int> panel_nseg, panel_tiles;
     std::vector<const MpSegment *> rest;
     std::vector<int> rest_nseg, rest_tiles;
-    // packed form with lookahead: the remaining tiles of round r without block
-    // row and column r + 1 (which pivot step r + 1 updates itself), strip form
+    // lookahead (packed and FP32 forms): the remaining tiles of round r
+    // without block row and column r + 1 (which the pivot step or chain of
+    // round r + 1 updates itself), strip form
     std::vector<const MpSegment *> rest2;
     std::vector<int> rest2_nseg, rest2_strips;
-    // FP32 form: round r's remaining tiles (all but block row and column r),
-    // strip form
-    std::vector<const MpSegment *> rests;
-    std::vector<int> rests_nseg, rests_strips;
     // FP32 form: round r's row and column panels, strip form
     std::vector<const MpSegment *> pstrips;
+    // FP32 form with lookahead: round r - 1's update of block row and column
+    // r (the tiles `rest2` of round r - 1 leaves out), strip form
+    std::vector<const MpSegment *> look;
+    std::vector<int> look_nseg, look_strips;
     const void *tmaps = nullptr;  // tensor-map pairs of the FW matrices (null: none)
     std::vector<int> pstrips_nseg, pstrips_strips;
     // boundary rows in their own buffer (host results): per part {element
@@ -561,6 +562,31 @@ int fw_rest_lookahead(MpSegment &rest, int nb, int r) {
   return fw_strips_of(rest, pairs);
 }
 
+// FP32 form with lookahead: round r - 1's update of block row and column r
+// of nb (r >= 1; the tiles that fw_rest_lookahead leaves out of round
+// r - 1) as strip-form segments appended to `out` from CTA `strips` on:
+// block row r over the columns other than r - 1 (the pivot block (r, r)
+// with them), and block column r over the rows other than r - 1 and r.  The
+// two write disjoint blocks and read block row and column r - 1 only, which
+// neither writes; no tile reads entries it or another tile writes.
+void fw_look_strips(void *D, int32_t *P, int64_t ld, int size, int r, int nb, int32_t tmap1,
+                    std::vector<MpSegment> &out, int &strips) {
+  MpSegment rowp, colp, rest;
+  int t1, t2, t3;
+  fw_segments(D, P, ld, size, r - 1, rowp, colp, rest, t1, t2, t3, true, tmap1);
+  rowp.row_fix = r;  // (the row panel of pivot r - 1, moved to block row r)
+  rowp.strip_begin = strips;
+  strips += fw_strips_of(rowp, 1);
+  out.push_back(rowp);
+  if (nb > 2) {
+    colp.col_fix = r;  // (the column panel, moved to block column r, without row r)
+    colp.row_skip2 = r;
+    colp.strip_begin = strips;
+    strips += fw_strips_of(colp, (nb - 1) / 2);  // (nb - 2) row blocks in pairs
+    out.push_back(colp);
+  }
+}
+
 // Min-plus segment C = A (x) B (fresh C), tiled in 128x128.
 MpSegment mp_segment(const void *A, int64_t lda, const void *B, int64_t ldb, const int32_t *Bp,
                      int64_t ldbp, void *C, int64_t ldc, int32_t *Cp, int64_t ldcp, int M, int N,
@@ -667,7 +693,7 @@ int build_plan(fap_engine *e, Plan &pl) {
   TableBuilder tb;
   struct GroupOffs {
     size_t batches, batches_alt, pdesc, row_begin, dec_begin, mp, bjobs, bsrc;
-    std::vector<size_t> diag, panel, rest, rest2, rests, pstrips;
+    std::vector<size_t> diag, panel, rest, rest2, pstrips, look;
     size_t tmaps = 0;
     bool has_tmaps = false;
   };
@@ -804,12 +830,12 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.rest_tiles.assign(maxnb, 0);
     G.rest2_nseg.assign(maxnb, 0);
     G.rest2_strips.assign(maxnb, 0);
-    G.rests_nseg.assign(maxnb, 0);
-    G.rests_strips.assign(maxnb, 0);
-    O.rests.assign(maxnb, 0);
     G.pstrips_nseg.assign(maxnb, 0);
     G.pstrips_strips.assign(maxnb, 0);
     O.pstrips.assign(maxnb, 0);
+    G.look_nseg.assign(maxnb, 0);
+    G.look_strips.assign(maxnb, 0);
+    O.look.assign(maxnb, 0);
     O.diag.assign(maxnb, 0);
     O.panel.assign(maxnb, 0);
     O.rest.assign(maxnb, 0);
@@ -837,8 +863,8 @@ int build_plan(fap_engine *e, Plan &pl) {
     }
     for (int r = 0; r < maxnb; r++) {
       std::vector<FwDiagJob> dj;
-      std::vector<MpSegment> ps, rs, r2s, rss, pss;
-      int pt = 0, rt = 0, r2strips = 0, rsstrips = 0, psstrips = 0;
+      std::vector<MpSegment> ps, rs, r2s, pss, ls;
+      int pt = 0, rt = 0, r2strips = 0, psstrips = 0, lstrips = 0;
       for (size_t pi = 0; pi < pdesc.size(); pi++) {
         const PartDesc &d = pdesc[pi];
         int nb = d.ld / B;
@@ -862,6 +888,7 @@ int build_plan(fap_engine *e, Plan &pl) {
           MpSegment rp, cp, rest;
           int a1, a2, a3;
           fw_segments(D, P, d.ld, d.ld, r, rp, cp, rest, a1, a2, a3, e->f32(), tmap1[pi]);
+          if (e->f32() && r > 0) fw_look_strips(D, P, d.ld, d.ld, r, nb, tmap1[pi], ls, lstrips);
           rp.tile_begin = pt;
           pt += a1;
           ps.push_back(rp);
@@ -879,13 +906,6 @@ int build_plan(fap_engine *e, Plan &pl) {
             r2strips += s2;
             r2s.push_back(rest2);
           }
-          MpSegment rests = rest;
-          const int s3 = fw_strips_of(rest, rest.tiles_x);
-          if (s3 > 0) {
-            rests.strip_begin = rsstrips;
-            rsstrips += s3;
-            rss.push_back(rests);
-          }
         }
       }
       G.diag_cnt[r] = (int)dj.size();
@@ -899,12 +919,12 @@ int build_plan(fap_engine *e, Plan &pl) {
       G.rest2_nseg[r] = (int)r2s.size();
       G.rest2_strips[r] = r2strips;
       O.rest2[r] = tb.add(r2s.data(), r2s.size());
-      G.rests_nseg[r] = (int)rss.size();
-      G.rests_strips[r] = rsstrips;
-      O.rests[r] = tb.add(rss.data(), rss.size());
       G.pstrips_nseg[r] = (int)pss.size();
       G.pstrips_strips[r] = psstrips;
       O.pstrips[r] = tb.add(pss.data(), pss.size());
+      G.look_nseg[r] = (int)ls.size();
+      G.look_strips[r] = lstrips;
+      O.look[r] = tb.add(ls.data(), ls.size());
     }
   }
   int st = pl.tables.ensure(std::max<size_t>(tb.bytes.size(), 64));
@@ -930,15 +950,15 @@ int build_plan(fap_engine *e, Plan &pl) {
     G.panel.resize(R);
     G.rest.resize(R);
     G.rest2.resize(R);
-    G.rests.resize(R);
     G.pstrips.resize(R);
+    G.look.resize(R);
     for (size_t r = 0; r < R; r++) {
       G.diag[r] = reinterpret_cast<const FwDiagJob *>(base + O.diag[r]);
       G.panel[r] = reinterpret_cast<const MpSegment *>(base + O.panel[r]);
       G.rest[r] = reinterpret_cast<const MpSegment *>(base + O.rest[r]);
       G.rest2[r] = reinterpret_cast<const MpSegment *>(base + O.rest2[r]);
-      G.rests[r] = reinterpret_cast<const MpSegment *>(base + O.rests[r]);
       G.pstrips[r] = reinterpret_cast<const MpSegment *>(base + O.pstrips[r]);
+      G.look[r] = reinterpret_cast<const MpSegment *>(base + O.look[r]);
     }
   }
   return FAP_OK;
@@ -1085,20 +1105,35 @@ struct Issuer {
         FAP_CUDA(fapk::launch_fw_strips(pred, G.rest2[r], G.rest2_nseg[r], G.rest2_strips[r], e->side, false,
                                         G.tmaps));
         FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
-      } else {
+      } else if (f32) {
+        // FP32 lookahead, in strip launches: the pivot chain of round r
+        // (round r - 1's update of block row and column r, the closure of
+        // pivot block r, both panels) on the issuing stream, round r's
+        // remaining tiles other than block row and column r + 1 (`rest2`) on
+        // the side stream, beside the pivot chain of round r + 1.  The events
+        // and the entries each side touches are those of the packed form.
+        if (r >= 2) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + r % 2], 0));
+        if (G.look_nseg[r] > 0)
+          FAP_CUDA(fapk::launch_fw_strips(pred, G.look[r], G.look_nseg[r], G.look_strips[r], st, true, G.tmaps));
         FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
-        if (f32) {  // FP32: panels, then the remaining tiles, in the strip form
+        if (G.pstrips_nseg[r] > 0)
           FAP_CUDA(fapk::launch_fw_strips(pred, G.pstrips[r], G.pstrips_nseg[r], G.pstrips_strips[r], st, true,
                                           G.tmaps));
-          FAP_CUDA(fapk::launch_fw_strips(pred, G.rests[r], G.rests_nseg[r], G.rests_strips[r], st, true,
+        FAP_CUDA(cudaEventRecord(e->ev_fw[0], st));
+        FAP_CUDA(cudaStreamWaitEvent(e->side, e->ev_fw[0], 0));
+        if (G.rest2_nseg[r] > 0)
+          FAP_CUDA(fapk::launch_fw_strips(pred, G.rest2[r], G.rest2_nseg[r], G.rest2_strips[r], e->side, true,
                                           G.tmaps));
-        } else {
+        FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
+      } else {
+        FAP_CUDA(fapk::launch_fw_diag(f32, pred, G.diag[r], G.diag_cnt[r], st));
+        {
           FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.panel[r], G.panel_nseg[r], G.panel_tiles[r], packed, st));
           FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, G.rest[r], G.rest_nseg[r], G.rest_tiles[r], packed, st));
         }
       }
     }
-    if (packed && rounds > 0) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (rounds - 1) % 2], 0));  // join
+    if ((packed || f32) && rounds > 0) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (rounds - 1) % 2], 0));  // join
     if (last) FAP_CUDA(rec(3));
     // Host results: the decode (own-part columns of the boundary rows, written
     // straight into the host rows) runs on the copy stream beside the
@@ -2272,9 +2307,9 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   DeviceGuard g(e->device);
   cudaStream_t st = pick_stream(e, stream);
   TableBuilder tb;
-  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb), ors(maxnb), ops(maxnb);
-  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), nr2(maxnb), sr2(maxnb), nrs(maxnb),
-      srs(maxnb), nps(maxnb), sps(maxnb);
+  std::vector<size_t> od(maxnb), op(maxnb), orr(maxnb), or2(maxnb), ops(maxnb), ols(maxnb);
+  std::vector<int> nd(maxnb), np(maxnb), tp(maxnb), nr(maxnb), tr(maxnb), nr2(maxnb), sr2(maxnb), nps(maxnb),
+      sps(maxnb), nls(maxnb), sls(maxnb);
   // tensor-map pairs of the matrices that meet the copy unit's alignment
   // rules (16-byte base and row stride); the others keep per-thread copies
   std::vector<int32_t> tmap1(count, 0);
@@ -2297,8 +2332,8 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
   }
   for (int r = 0; r < maxnb; r++) {
     std::vector<FwDiagJob> dj;
-    std::vector<MpSegment> ps, rs, r2s, rss, pss;
-    int pt = 0, rt = 0, r2strips = 0, rsstrips = 0, psstrips = 0;
+    std::vector<MpSegment> ps, rs, r2s, pss, ls;
+    int pt = 0, rt = 0, r2strips = 0, psstrips = 0, lstrips = 0;
     for (int32_t b = 0; b < count; b++) {
       int nb = (sizes[b] + Bk - 1) / Bk;
       if (r >= nb) continue;
@@ -2315,6 +2350,8 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
         int t1, t2, t3;
         fw_segments(D[b], pred ? P[b] : nullptr, ld[b], sizes[b], r, a, c, rest, t1, t2, t3,
                     dtype == FAP_DTYPE_F32, tmap1[b]);
+        if (dtype == FAP_DTYPE_F32 && r > 0)
+          fw_look_strips(D[b], pred ? P[b] : nullptr, ld[b], sizes[b], r, nb, tmap1[b], ls, lstrips);
         a.tile_begin = pt;
         pt += t1;
         ps.push_back(a);
@@ -2332,24 +2369,17 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
           r2strips += s2;
           r2s.push_back(rest2);
         }
-        MpSegment rests = rest;  // FP32: all remaining tiles, strip form
-        const int s3 = fw_strips_of(rest, rest.tiles_x);
-        if (s3 > 0) {
-          rests.strip_begin = rsstrips;
-          rsstrips += s3;
-          rss.push_back(rests);
-        }
       }
     }
     nr2[r] = (int)r2s.size();
     sr2[r] = r2strips;
     or2[r] = tb.add(r2s.data(), r2s.size());
-    nrs[r] = (int)rss.size();
-    srs[r] = rsstrips;
-    ors[r] = tb.add(rss.data(), rss.size());
     nps[r] = (int)pss.size();
     sps[r] = psstrips;
     ops[r] = tb.add(pss.data(), pss.size());
+    nls[r] = (int)ls.size();
+    sls[r] = lstrips;
+    ols[r] = tb.add(ls.data(), ls.size());
     nd[r] = (int)dj.size();
     od[r] = tb.add(dj.data(), dj.size());
     np[r] = (int)ps.size();
@@ -2394,14 +2424,24 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
       FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + or2[r]), nr2[r],
                                       sr2[r], e->side, false, tmaps));
       FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
-    } else {
+    } else if (f32) {  // FP32 lookahead, as in the solve's issue order
+      if (r >= 2) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + r % 2], 0));
+      if (nls[r] > 0)
+        FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ols[r]), nls[r],
+                                        sls[r], st, true, tmaps));
       FAP_CUDA(fapk::launch_fw_diag(f32, pred, djobs, nd[r], st));
-      if (f32) {  // panels, then the remaining tiles, in the strip form
+      if (nps[r] > 0)
         FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ops[r]), nps[r],
                                         sps[r], st, true, tmaps));
-        FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + ors[r]), nrs[r],
-                                        srs[r], st, true, tmaps));
-      } else {
+      FAP_CUDA(cudaEventRecord(e->ev_fw[0], st));
+      FAP_CUDA(cudaStreamWaitEvent(e->side, e->ev_fw[0], 0));
+      if (nr2[r] > 0)
+        FAP_CUDA(fapk::launch_fw_strips(pred, reinterpret_cast<const MpSegment *>(base + or2[r]), nr2[r],
+                                        sr2[r], e->side, true, tmaps));
+      FAP_CUDA(cudaEventRecord(e->ev_fw[1 + r % 2], e->side));
+    } else {
+      FAP_CUDA(fapk::launch_fw_diag(f32, pred, djobs, nd[r], st));
+      {
         FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + op[r]), np[r],
                                             tp[r], packed, st));
         FAP_CUDA(fapk::launch_minplus_tiles(f32, pred, reinterpret_cast<const MpSegment *>(base + orr[r]),
@@ -2409,7 +2449,7 @@ int fap_floyd_batched(fap_engine *e, int32_t dtype, int32_t count, const int32_t
       }
     }
   }
-  if (packed) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (maxnb - 1) % 2], 0));  // join
+  if ((packed || f32) && maxnb > 0) FAP_CUDA(cudaStreamWaitEvent(st, e->ev_fw[1 + (maxnb - 1) % 2], 0));  // join
   FAP_CUDA(cudaStreamSynchronize(st));
   return check_status(e);
 }
