@@ -869,11 +869,13 @@ __device__ __forceinline__ int strip_resolve_f32(unsigned acc, int tag, const un
 // [k][sa] and Bs: B [k][sb] in the swizzled layout (swz); the thread's rows
 // are a0 .. a0 + 3 and a0 + kBlk .. a0 + kBlk + 3, its columns b0 .. b0 + 3.
 // With LEAN, the B operands load two columns at a time (24 operands live
-// instead of 32).
+// instead of 32).  Without `hi` (uniform over the CTA: the tile's second
+// 64-row block is empty) the rows a0 + kBlk .. are left as they are.
 template <bool PRED, bool LEAN = false>
 __device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&arg)[8][4],
                                                   const unsigned *As, int sa, int a0,
-                                                  const unsigned *Bs, int sb, int b0, int kseg) {
+                                                  const unsigned *Bs, int sb, int b0, int kseg,
+                                                  bool hi = true) {
   for (int kk = 0; kk < kseg; kk += 4) {
     const unsigned *acol = As + kk * sa + (a0 ^ swz<true>(kk));
     const unsigned *bcol = Bs + kk * sb + (b0 ^ swz<true>(kk));
@@ -887,6 +889,7 @@ __device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&a
     }
 #pragma unroll
     for (int h = 0; h < 2; h++) {
+      if (h == 1 && !hi) break;
       unsigned a[4][4];  // [row of the half][step]
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -915,6 +918,7 @@ __device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&a
     for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 4; c++) {
+        if (r >= 4 && !hi) continue;
         const int k0 = arg[r][c] > 0 ? arg[r][c] - 1 : 0;
         const int sw = swz<true>(k0);
         arg[r][c] = strip_resolve_f32(acc[r][c], arg[r][c], As + k0 * sa + (a0 ^ sw) + (r >> 2) * kBlk + (r & 3),
@@ -1714,10 +1718,12 @@ __global__ void __launch_bounds__(kThreads, TN == 128 ? 1 : 2)
       // FP32 with at least half of the steps active: all steps in groups of
       // four (steps that are not active hold "unreached" on one side)
       const bool grouped = F32 && CH == 1 && nact > 0 && 2 * nact >= kseg;
-      n_work += (unsigned long long)(nact == s.K || grouped ? kseg : nact) * kTile * TN;
+      // (the FP32 groups skip the rows of an empty second row block)
+      n_work += (unsigned long long)(nact == s.K || grouped ? kseg : nact) * (grouped && rbase1 < 0 ? kBlk : kTile) * TN;
       if (grouped) {
         if constexpr (F32 && CH == 1)
-          addmin_groups_f32<PRED>(acc, arg, &sm.A[0][0], kTile, ty * 4, &sm.B[buf][0][0], TN, tx * 4, kseg);
+          addmin_groups_f32<PRED>(acc, arg, &sm.A[0][0], kTile, ty * 4, &sm.B[buf][0][0], TN, tx * 4, kseg,
+                                  rbase1 >= 0);
       } else if (F32 && msk) {
         while (msk) {  // (the swizzled layout)
           const int kk = __ffsll(msk) - 1;
