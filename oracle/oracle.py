@@ -154,6 +154,11 @@ def run_part(part, ro, col, w, graph_id, pre, mp_rows=-1, out=None):
         p = np.zeros((sub, n), np.int32)
     else:
         d, p = out
+    # written through before the timed call, as the reference's rows are
+    # (std::vector::resize zero-fills them before fapGraph::run,
+    # fap/fap.cpp:532-534): the phase times then hold no first-touch faults
+    d.fill(0)
+    p.fill(0)
     t = _times()
     lib().oracle_run_part(int(part), n, _p(adj), _p(ro), _p(col), _p(w), _p(gid), _p(pre["st2ed"]),
                           _p(pre["ed2st"]), _p(pre["ver_num"]), _p(pre["ver_offset"]),
