@@ -666,7 +666,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 // per tile.  Shared memory (ks = K rounded up to 4):
 //   B[2][ks][TN] | Bp[1 + ks][TN] | colp[2][TN] | coll[2][TN] | ownidx[2][TN] |
 //   Fst[kOwnCap][128] | Fpst[kOwnCap][128] | A^T[ks][128]
-// and, FP32 only, Ar[128][strip_bc_stride(kseg)] (A row-major) |
+// and, FP32 only, Ar[128][strip_ar_stride(kseg)] (A row-major) |
 // Bq[ks / 4][64] (the current tile's B by step group: 16-byte unit (g, col)
 // holds steps 4g .. 4g + 3 of column col).
 // Row 0 of Bp holds -1, so the predecessor of every output is Bp[idx][col]
@@ -694,7 +694,7 @@ constexpr int kStripClasses = 2;
 // Row stride of the FP32 strip kernel's row-major copy of A for kseg
 // steps: kseg, or kseg + 4 when kseg / 4 is even, so that the stride in
 // 16-byte units is odd.
-__host__ __device__ constexpr int strip_bc_stride(int kseg) { return ((kseg >> 2) & 1) ? kseg : kseg + 4; }
+__host__ __device__ constexpr int strip_ar_stride(int kseg) { return ((kseg >> 2) & 1) ? kseg : kseg + 4; }
 
 // Shared memory of the strip kernel with TN-column tiles, in bytes; F32 adds
 // the row-major copy of A ([128][ks + 4] at most) and the step-group copy
@@ -928,7 +928,7 @@ __device__ __forceinline__ void addmin_groups_f32(unsigned (&acc)[8][4], int (&a
 }
 
 // The same for the strip min-plus, from row-major copies of the operands:
-// Ar[128][ars] (row m's steps contiguous, ars = strip_bc_stride(kseg)) and
+// Ar[128][ars] (row m's steps contiguous, ars = strip_ar_stride(kseg)) and
 // Bq, the tile's B by step group (16-byte unit g * 64 + col: steps 4g ..
 // 4g + 3 of column col).
 // One 16-byte load gives a row's or a column's four steps of a group, so the
@@ -1039,7 +1039,7 @@ __global__ void __launch_bounds__(kThreads, TN == 128 || F32 ? 2 : 3)
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
   const unsigned INF = F32 ? __float_as_uint(Dist<float>::inf()) : Dist<uint32_t>::inf();
   const int kseg = (s.K + 3) & ~3;  // this segment's K rounded up to 4 (<= ks)
-  const int ars = strip_bc_stride(kseg);  // F32: Ar's row stride
+  const int ars = strip_ar_stride(kseg);  // F32: Ar's row stride
   const bool vec_b = (s.ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(s.B) & 15) == 0;
   const bool vec_bp = PRED && (s.ldbp & 3) == 0 && (reinterpret_cast<uintptr_t>(s.Bp) & 15) == 0;
   const bool vec_c = vec_stores_ok<PRED>(s);
